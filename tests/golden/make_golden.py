@@ -1,0 +1,145 @@
+"""Generate the golden fixtures in tests/golden/ from the reference C backend.
+
+Run where the reference tree is mounted:
+
+    make -f oracle/ref.mk REF=/root/reference
+    python tests/golden/make_golden.py
+
+The reference's own kernels (tupan/lib/src/*_kernel.c, compiled unmodified by
+oracle/ref.mk into oracle/_ref/libtupan_ref_f64.so) are called through
+oracle.oracle.ReferenceLib on seeded inputs; inputs and outputs are stored as
+compressed .npz files.  The GPU machine has no reference tree, so these fixtures
+carry the pin there.
+
+Cases (the reference test suite, tupan/tests/test_extensions.py:28-127, asserts
+nothing and uses unseeded inputs; these restate its shapes, seeded):
+  sweep    n=96 particles, masses U(0,1), eps2=0, positions and velocities
+           U(0,10) (test_extensions.py:28-36); outputs for i=all vs j=prefix
+           and i=prefix vs j=all at prefix lengths 1,2,3,31,33,64,65,96
+           (test_extensions.py:45-85); eta=1/64, PN order 7 with c=128,
+           Sakura dt=1/64 with flags -2,-1,0,1,2.
+  plummer  n=384 Plummer sphere, equal masses, per-particle eps2 = 0.5e-4.
+  binary   n=64: 32 wide particles plus 16 pairs at separation ~1e-3 with
+           eps2=0 (Sakura's Kepler branch, PN order 5/7 with c=1e2).
+  edge     n=5 with two coincident particles (r2 = 0 for a distinct pair)
+           and a massless particle.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle.oracle import ReferenceLib, SPECS  # noqa: E402
+
+FIELDS = SPECS["snap_crackle"][0]
+PREFIXES = (1, 2, 3, 31, 33, 64, 65, 96)
+
+
+def sweep_set(rng, n=96):
+    ps = {f: rng.random(n) * 10 for f in FIELDS}
+    ps["mass"] = rng.random(n)
+    ps["eps2"] = np.zeros(n)
+    return ps
+
+
+def plummer_set(rng, n=384):
+    x1 = rng.random(n)
+    r = 1 / np.sqrt(x1 ** (-2.0 / 3.0) - 1)
+    ct = 2 * rng.random(n) - 1
+    st = np.sqrt(1 - ct * ct)
+    ph = 2 * np.pi * rng.random(n)
+    pos = np.stack([r * st * np.cos(ph), r * st * np.sin(ph), r * ct], 1) * (3 * np.pi / 16)
+    vel = rng.normal(size=(n, 3)) * 0.5
+    ps = {"mass": np.full(n, 1.0 / n), "eps2": np.full(n, 0.5e-4)}
+    for k, c in enumerate("xyz"):
+        ps["r" + c] = pos[:, k].copy()
+        ps["v" + c] = vel[:, k].copy()
+    for f in ("ax", "ay", "az", "jx", "jy", "jz"):
+        ps[f] = rng.normal(size=n)
+    return ps
+
+
+def binary_set(rng, n=64):
+    h = n // 2
+    base = rng.normal(size=(h, 3))
+    pos = np.concatenate([base, base + rng.normal(size=(h, 3)) * 1e-3])
+    vel = np.concatenate([rng.normal(size=(h, 3)) * 0.3, rng.normal(size=(h, 3)) * 3])
+    ps = {"mass": rng.random(n) / n, "eps2": np.zeros(n)}
+    for k, c in enumerate("xyz"):
+        ps["r" + c] = pos[:, k].copy()
+        ps["v" + c] = vel[:, k].copy()
+    for f in ("ax", "ay", "az", "jx", "jy", "jz"):
+        ps[f] = rng.normal(size=n)
+    return ps
+
+
+def edge_set():
+    ps = {f: np.zeros(5) for f in FIELDS}
+    ps["mass"][:] = [0.5, 0.25, 0.25, 0.0, 1.0]
+    ps["rx"][:] = [0.0, 1.0, 1.0, -2.0, 0.5]
+    ps["ry"][:] = [0.0, 0.0, 0.0, 1.0, 3.0]
+    ps["rz"][:] = [0.0, 0.0, 0.0, 0.0, -1.0]
+    ps["vx"][:] = [0.0, 0.5, -0.5, 0.1, 0.0]
+    ps["vy"][:] = [0.1, 0.0, 0.0, 0.0, 0.2]
+    ps["vz"][:] = [0.0, 0.0, 0.3, 0.0, 0.0]
+    ps["eps2"][:] = [1e-3, 0.0, 0.0, 1e-3, 0.0]
+    for f in ("ax", "ay", "az", "jx", "jy", "jz"):
+        ps[f][:] = np.linspace(-1, 1, 5)
+    return ps
+
+
+def pn_scalars(order, c):
+    return (order,) + tuple((1.0 / c) ** k for k in range(1, 8))
+
+
+def calls_for(case):
+    """(kernel, scalars) pairs exercised on each case."""
+    out = [("phi", ()), ("acc", ()), ("acc_jerk", ()), ("snap_crackle", ()),
+           ("tstep", (1.0 / 64,))]
+    if case == "sweep":
+        out += [("pnacc", pn_scalars(7, 128.0))]
+        out += [("sakura", (1.0 / 64, f)) for f in (-2, -1, 0, 1, 2)]
+    elif case == "binary":
+        out += [("pnacc", pn_scalars(5, 1e2)), ("pnacc", pn_scalars(7, 1e2))]
+        out += [("sakura", (1.0 / 64, f)) for f in (-2, -1, 1, 2)]
+        out += [("sakura", (0.3, 1))]
+    elif case == "plummer":
+        out += [("pnacc", pn_scalars(4, 1e2))]
+        out += [("tstep", (0.01,))]
+    elif case == "edge":
+        out += [("pnacc", pn_scalars(7, 10.0))]
+    return out
+
+
+def main():
+    ref = ReferenceLib()
+    rng = np.random.default_rng(20261203)
+    sets = {"sweep": sweep_set(rng), "plummer": plummer_set(rng),
+            "binary": binary_set(rng), "edge": edge_set()}
+    for case, ps in sets.items():
+        store = {"in_" + f: ps[f] for f in FIELDS}
+        calls = calls_for(case)
+        names = []
+        for k, (name, sc) in enumerate(calls):
+            key = "%02d_%s" % (k, name)
+            names.append(key)
+            store["scalars_" + key] = np.array(sc, dtype=np.float64)
+            res = ref.calc(name, ps, ps, *sc)
+            store["out_" + key] = np.stack(res)
+            if case == "sweep" and name != "sakura":
+                for p in PREFIXES:
+                    sub = {f: ps[f][:p] for f in FIELDS}
+                    store["outJ%d_" % p + key] = np.stack(ref.calc(name, ps, sub, *sc))
+                    store["outI%d_" % p + key] = np.stack(ref.calc(name, sub, ps, *sc))
+        store["calls"] = np.array(names)
+        path = os.path.join(HERE, "golden_%s.npz" % case)
+        np.savez_compressed(path, **store)
+        print("wrote", path, os.path.getsize(path), "bytes,", len(calls), "calls")
+
+
+if __name__ == "__main__":
+    main()
