@@ -1,0 +1,363 @@
+"""Benchmark: Gint/s of the split-FP32 Acc and AccJerk kernels on one GB300.
+
+Workload (the precision-form configuration): a Plummer sphere of N = 65536
+particles with a Salpeter mass function (slope -2.35, masses in [0.1, 100],
+total mass 1), pair softening eps2 = 1e-6 (eps = 1e-3), Henon units, seeded
+synthetic inputs.  One step = one Acc and one AccJerk evaluation of all N
+i-particles against all N j-particles in split FP32 (2 N^2 interactions).
+
+Printed JSON line (rank 0):
+  value        interactions / second over the timed steps, inputs resident in
+               HBM (device pointers through the C ABI), Gint/s
+  e2e          the same metric through the drop-in host entry points
+               acc_kernel / acc_jerk_kernel (libtupan.h signatures) with host
+               buffers, host<->device copies inside the timed region
+  roofline     the AccJerk kernel: reference-counted 42 flop/interaction x
+               interactions / kernel time, against the FP32 FMA peak measured
+               on this GPU by tg_probe_fma_tflops
+  fp64         the FP64 GPU kernels on the same workload (bit-identical to the
+               reference C backend) and the split-FP32 speed-up over them
+  force_error  per-particle |a_ds32 - a_fp64| / |a_fp64| (and jerk)
+  cpu_baseline the CPU oracle port (same algorithm and operation order as the
+               reference C backend) on the host cores, bounded sample
+  clocks       nvidia-smi SM clock and throttle reasons during the timed region
+
+`--impl reference` times the reference algorithm on the host CPU (the oracle
+port; the reference tree itself is not present on the GPU machine) on a
+bounded sample of the same workload and prints the same metric.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+N_DEFAULT = 65536
+EPS = 1e-3
+SEED = 20261203
+FLOP_ACC = 20       # tupan/lib/src/acc_kernel_common.h:38
+FLOP_ACC_JERK = 42  # tupan/lib/src/acc_jerk_kernel_common.h:56
+METRIC = "Gint/s Acc+AccJerk split-FP32 (N=65536 Plummer-Salpeter, eps2=1e-6)"
+P5 = ("mass", "rx", "ry", "rz", "eps2")
+P8 = P5 + ("vx", "vy", "vz")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--cpu-seconds", type=float, default=3.0,
+                    help="target wall time of each CPU baseline sample")
+    ap.add_argument("--no-fp64", action="store_true")
+    return ap.parse_args()
+
+
+def workload(n, rank):
+    from tupan_gb300.ics import Salpeter, plummer_arrays
+    return plummer_arrays(n, EPS, imf=Salpeter(0.1, 100.0), seed=SEED + rank)
+
+
+def config(n):
+    return {"workload": "plummer-salpeter", "n": n, "imf": "salpeter -2.35 [0.1,100], M=1",
+            "eps2_pair": 2 * (EPS * EPS / 2), "units": "henon", "step": "acc + acc_jerk, i=j=all",
+            "interactions_per_step": 2 * n * n, "precision": "ds32 (hi/lo positions, Kahan-folded FP32)",
+            "l2": "flushed between timed steps (256 MiB write)", "seed": SEED}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (oracle port of the reference algorithm)
+# ---------------------------------------------------------------------------
+def cpu_sample(d, seconds, threads):
+    """Time FP64 Acc + AccJerk of the first ni_s i-particles against all N.
+
+    ni_s is calibrated so one sample takes about `seconds` of wall time."""
+    from oracle.oracle import Oracle
+    orc = Oracle()
+    n = len(d["mass"])
+
+    def run(ni):
+        I = {k: v[:ni] for k, v in d.items()}
+        t0 = time.perf_counter()
+        orc.calc("acc", I, d, nthreads=threads)
+        orc.calc("acc_jerk", I, d, nthreads=threads)
+        return time.perf_counter() - t0
+
+    ni = max(threads, 64)
+    t = run(ni)
+    while t < 0.2 and ni < n:
+        ni = min(n, ni * 4)
+        t = run(ni)
+    ni = int(min(n, max(threads, ni * seconds / max(t, 1e-6))))
+    t = run(ni)
+    return {"value": 2.0 * ni * n / t / 1e9, "unit": "Gint/s", "cores": threads,
+            "kind": "port", "seconds": t,
+            "sample": "FP64 acc + acc_jerk, %d i-particles x %d j-particles (%.3g interactions)"
+                      % (ni, n, 2.0 * ni * n)}
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    from oracle import oracle as om
+    om.build()
+    d = workload(args.n, 0)
+    threads = os.cpu_count() or 1
+    for _ in range(max(args.warmup, 0)):
+        cpu_sample(d, min(args.cpu_seconds, 1.0), threads)
+    vals = [cpu_sample(d, args.cpu_seconds, threads) for _ in range(max(args.steps, 1))]
+    v = float(np.median([x["value"] for x in vals]))
+    secs = sum(x["seconds"] for x in vals)
+    base = dict(vals[0])
+    base["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Gint/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / len(vals),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config(args.n), "cpu_baseline": base,
+            "e2e": {"value": v, "unit": "Gint/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# clocks sampler
+# ---------------------------------------------------------------------------
+class Clocks(object):
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def rel_errors(got, want):
+    d = np.sqrt(((got - want) ** 2).sum(0))
+    n = np.sqrt((want ** 2).sum(0))
+    r = d[n > 0] / n[n > 0]
+    return {"max": float(r.max()), "p99": float(np.percentile(r, 99)),
+            "median": float(np.median(r)), "rms": float(np.sqrt((r * r).mean()))}
+
+
+def ours(args, rank, world, dist):
+    import torch
+    from tupan_gb300 import _native
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    n = args.n
+    d = workload(n, rank)
+    T = {k: torch.tensor(d[k], dtype=torch.float64, device=dev) for k in P8}
+    outs = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(9)]
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    ptr = lambda keys: [T[k].data_ptr() for k in keys]
+
+    def acc(prec, o):
+        _native.call_device("acc", n, ptr(P5), n, ptr(P5), (), [x.data_ptr() for x in o], prec, sp)
+
+    def acc_jerk(prec, o):
+        _native.call_device("acc_jerk", n, ptr(P8), n, ptr(P8), (), [x.data_ptr() for x in o], prec, sp)
+
+    DS = _native.PREC_DS32
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    clocks = Clocks(dev.index)
+    clocks.start()
+    # warm-up: W steps, and at least one second of load so clocks settle
+    t_end = time.perf_counter() + 1.0
+    w = 0
+    while w < max(args.warmup, 0) or time.perf_counter() < t_end:
+        acc(DS, outs[:3])
+        acc_jerk(DS, outs[3:])
+        torch.cuda.synchronize()
+        w += 1
+
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    for s in range(args.steps):
+        flush.zero_()
+        ev[s][0].record(stream)
+        acc(DS, outs[:3])
+        ev[s][1].record(stream)
+        acc_jerk(DS, outs[3:])
+        ev[s][2].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    st = _native.sync_status(sp)
+    if st:
+        raise RuntimeError("kernel status bits set: %d" % st)
+    t_acc = [ev[s][0].elapsed_time(ev[s][1]) for s in range(args.steps)]
+    t_aj = [ev[s][1].elapsed_time(ev[s][2]) for s in range(args.steps)]
+    step_ms = float(np.sum(t_acc) + np.sum(t_aj)) / args.steps
+    if dist:
+        t = torch.tensor([step_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms = float(t.item())
+    inter = 2.0 * n * n
+    value = world * inter / (step_ms * 1e-3) / 1e9
+    aj_ms = float(np.median(t_aj))
+    acc_ms = float(np.median(t_acc))
+
+    ds_acc = np.stack([x.cpu().numpy() for x in outs[:3]])
+    ds_aj = np.stack([x.cpu().numpy() for x in outs[3:]])
+
+    peak32 = _native.lib.tg_probe_fma_tflops(0, 20000, sp)
+    peak64 = _native.lib.tg_probe_fma_tflops(1, 2000, sp)
+    achieved = FLOP_ACC_JERK * n * n / (aj_ms * 1e-3) / 1e12
+    line = {"metric": METRIC, "value": value, "unit": "Gint/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "ds32", "data": "synthetic",
+            "config": config(n), "gpu_launches": 4 * args.steps,
+            "kernels": {"acc_ds32": {"ms": acc_ms, "gint_s": n * n / (acc_ms * 1e-3) / 1e9},
+                        "acc_jerk_ds32": {"ms": aj_ms, "gint_s": n * n / (aj_ms * 1e-3) / 1e9}},
+            "roofline": {"bound": "fp32", "kernel": "ds32_streamk<AccJerkDS>",
+                         "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
+                         "frac": achieved / peak32 if peak32 > 0 else None, "traffic": None,
+                         "flop_per_interaction": FLOP_ACC_JERK,
+                         "peak_source": "measured: tg_probe_fma_tflops (FFMA2 chains, this GPU)",
+                         "peak_fp64_tflops": peak64,
+                         "acc_frac": (FLOP_ACC * n * n / (acc_ms * 1e-3) / 1e12) / peak32 if peak32 > 0 else None},
+            "clocks": clk, "wall_s": wall}
+
+    if not args.no_fp64:
+        torch.cuda.synchronize()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        f_out = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(9)]
+        e[0].record(stream)
+        acc(_native.PREC_FP64, f_out[:3])
+        e[1].record(stream)
+        acc_jerk(_native.PREC_FP64, f_out[3:])
+        e[2].record(stream)
+        torch.cuda.synchronize()
+        f_acc_ms, f_aj_ms = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+        f_acc = np.stack([x.cpu().numpy() for x in f_out[:3]])
+        f_aj = np.stack([x.cpu().numpy() for x in f_out[3:]])
+        fp64_v = inter / ((f_acc_ms + f_aj_ms) * 1e-3) / 1e9
+        line["fp64"] = {"acc_ms": f_acc_ms, "acc_jerk_ms": f_aj_ms, "value": fp64_v, "unit": "Gint/s",
+                        "acc_jerk_gint_s": n * n / (f_aj_ms * 1e-3) / 1e9,
+                        "ds32_speedup": value / world / fp64_v,
+                        "acc_jerk_ds32_speedup": f_aj_ms / aj_ms}
+        line["force_error"] = {"acc": rel_errors(ds_acc, f_acc), "acc_in_acc_jerk": rel_errors(ds_aj[:3], f_aj[:3]),
+                               "jerk": rel_errors(ds_aj[3:], f_aj[3:]),
+                               "against": "FP64 GPU kernels (bit-identical to the reference C backend)"}
+
+    # ---- end to end through the drop-in host entry points ---------------
+    pin = {k: torch.tensor(d[k], dtype=torch.float64).pin_memory() for k in P8}
+    hp = {k: ctypes.c_void_p(v.data_ptr()) for k, v in pin.items()}
+    hout = [torch.empty(n, dtype=torch.float64).pin_memory() for _ in range(9)]
+    ho = [ctypes.c_void_p(x.data_ptr()) for x in hout]
+    _native.lib.tg_set_host_precision(DS)
+
+    def e2e_step():
+        _native.lib.acc_kernel(n, *[hp[k] for k in P5], n, *[hp[k] for k in P5], *ho[:3])
+        _native.lib.acc_jerk_kernel(n, *[hp[k] for k in P8], n, *[hp[k] for k in P8], *ho[3:])
+
+    e2e_step()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    _native.lib.tg_set_host_precision(_native.PREC_FP64)
+    line["e2e"] = {"value": world * inter / e2e_s / 1e9, "unit": "Gint/s",
+                   "h2d_bytes_per_step": 8 * n * (2 * 5 + 2 * 8), "d2h_bytes_per_step": 8 * n * (3 + 6),
+                   "ms_per_step": e2e_s * 1e3,
+                   "path": "acc_kernel + acc_jerk_kernel (libtupan.h signatures), pinned host buffers"}
+    if rank == 0:
+        line["cpu_baseline"] = cpu_sample(d, args.cpu_seconds, os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        backend = "nccl" if (args.impl == "ours" and torch.cuda.is_available()) else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        tdist.init_process_group(backend)
+        dist = tdist
+    try:
+        if args.impl == "reference":
+            reference_arm(args, rank, world)
+        else:
+            ours(args, rank, world, dist)
+    finally:
+        if dist:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,219 @@
+/*
+ * tupan_gb300.h -- C ABI of libtupan_gb300.so, the GB300 (sm_103a) backend
+ * for Tupan's direct-summation pairwise kernels.
+ *
+ * Two families of entry points:
+ *
+ * 1. Drop-in host entry points with the exact signatures of the reference's
+ *    C library (tupan/lib/src/libtupan.h:2-246, float64 build: UINT is
+ *    unsigned long, INT is long, REAL is double).  They take HOST pointers,
+ *    copy inputs to the GPU, run, copy outputs back and return when done, so
+ *    the reference's cffi backend can load this library in place of its own
+ *    build.  The arithmetic precision is chosen with
+ *    tg_set_host_precision() (default TG_PREC_FP64).
+ *
+ * 2. Device entry points tg_<kernel>(...) with the same argument order but
+ *    DEVICE pointers, a precision selector and a CUDA stream.  They are
+ *    asynchronous (stream-ordered) and return TG_OK or a negative TG_E*
+ *    code; device-side conditions (capped Kepler iterations, a bounded wait
+ *    that timed out) accumulate in a per-device status word read by
+ *    tg_sync_status().
+ *
+ * Common rules (libtupan.h conventions): structure-of-arrays float64 inputs,
+ * i-set then j-set then scalars then outputs; pair softening e2 = ie2 + je2;
+ * pairs with r2 == 0 (self pairs, coincident particles) contribute nothing;
+ * every output is overwritten (never accumulated); outputs must not alias
+ * inputs or each other; the i- and j-sets may be the same arrays.
+ * ni == 0 is a no-op; nj == 0 yields the empty-sum results.
+ */
+#ifndef TUPAN_GB300_H
+#define TUPAN_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* precision selectors */
+#define TG_PREC_FP64 0 /* IEEE double, per-pair operations in the reference's order */
+#define TG_PREC_DS32 1 /* split FP32: hi/lo positions, compensated FP32 sums */
+
+/* return codes */
+#define TG_OK 0
+#define TG_EINVAL (-1)   /* bad argument: null pointer, size, precision, flag */
+#define TG_ECUDA (-2)    /* CUDA runtime error (see tg_last_error) */
+#define TG_ENOMEM (-3)   /* workspace allocation failed */
+#define TG_ENODEV (-4)   /* no CUDA device */
+
+/* status bits returned by tg_sync_status() */
+#define TG_ST_MBAR_TIMEOUT 1u   /* a bounded shared-memory pipeline wait gave up */
+#define TG_ST_KEPLER_CAP 2u     /* Sakura: Kepler retry bound reached, last iterate kept */
+#define TG_ST_LAGUERRE_CAP 4u   /* Sakura: Laguerre iteration bound (64) reached */
+
+/* ---------------------------------------------------------------------- */
+/* Library state                                                           */
+/* ---------------------------------------------------------------------- */
+const char *tg_version(void);
+/* Text of the last error seen by this thread's calls ("" if none). */
+const char *tg_last_error(void);
+/* Synchronise `stream` and return (then clear) the status bits raised by
+ * kernels on the current device since the last call; negative on error. */
+int tg_sync_status(void *stream);
+/* Precision used by the drop-in host entry points (process-wide). */
+int tg_set_host_precision(int prec);
+int tg_get_host_precision(void);
+/* Streaming multiprocessors of the current device (0 if none). */
+int tg_device_sms(void);
+/* Measurement helper with no counterpart in the reference: dense FMA issue
+ * probe on the current device, returning TFLOP/s (2 flops per FMA) for FP32
+ * (which = 0, packed FFMA2) or FP64 (which = 1); negative on error.  It is
+ * the measured denominator of the pairwise kernels' FP32 roofline. */
+double tg_probe_fma_tflops(int which, int iters, void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* Device entry points (device pointers, asynchronous on `stream`)         */
+/* ---------------------------------------------------------------------- */
+
+/* replaces phi_kernel, tupan/lib/src/libtupan.h:2-15 */
+int tg_phi(size_t ni, const double *im, const double *irx, const double *iry,
+           const double *irz, const double *ie2,
+           size_t nj, const double *jm, const double *jrx, const double *jry,
+           const double *jrz, const double *je2,
+           double *iphi, int prec, void *stream);
+
+/* replaces acc_kernel, tupan/lib/src/libtupan.h:17-32 */
+int tg_acc(size_t ni, const double *im, const double *irx, const double *iry,
+           const double *irz, const double *ie2,
+           size_t nj, const double *jm, const double *jrx, const double *jry,
+           const double *jrz, const double *je2,
+           double *iax, double *iay, double *iaz, int prec, void *stream);
+
+/* replaces acc_jerk_kernel, tupan/lib/src/libtupan.h:34-58 */
+int tg_acc_jerk(size_t ni, const double *im, const double *irx, const double *iry,
+                const double *irz, const double *ie2,
+                const double *ivx, const double *ivy, const double *ivz,
+                size_t nj, const double *jm, const double *jrx, const double *jry,
+                const double *jrz, const double *je2,
+                const double *jvx, const double *jvy, const double *jvz,
+                double *iax, double *iay, double *iaz,
+                double *ijx, double *ijy, double *ijz, int prec, void *stream);
+
+/* replaces snap_crackle_kernel, tupan/lib/src/libtupan.h:60-96 */
+int tg_snap_crackle(size_t ni, const double *im, const double *irx, const double *iry,
+                    const double *irz, const double *ie2,
+                    const double *ivx, const double *ivy, const double *ivz,
+                    const double *iax, const double *iay, const double *iaz,
+                    const double *ijx, const double *ijy, const double *ijz,
+                    size_t nj, const double *jm, const double *jrx, const double *jry,
+                    const double *jrz, const double *je2,
+                    const double *jvx, const double *jvy, const double *jvz,
+                    const double *jax, const double *jay, const double *jaz,
+                    const double *jjx, const double *jjy, const double *jjz,
+                    double *isx, double *isy, double *isz,
+                    double *icx, double *icy, double *icz, int prec, void *stream);
+
+/* replaces tstep_kernel, tupan/lib/src/libtupan.h:98-119 */
+int tg_tstep(size_t ni, const double *im, const double *irx, const double *iry,
+             const double *irz, const double *ie2,
+             const double *ivx, const double *ivy, const double *ivz,
+             size_t nj, const double *jm, const double *jrx, const double *jry,
+             const double *jrz, const double *je2,
+             const double *jvx, const double *jvy, const double *jvz,
+             double eta, double *idt_a, double *idt_b, int prec, void *stream);
+
+/* replaces pnacc_kernel, tupan/lib/src/libtupan.h:121-150 */
+int tg_pnacc(size_t ni, const double *im, const double *irx, const double *iry,
+             const double *irz, const double *ie2,
+             const double *ivx, const double *ivy, const double *ivz,
+             size_t nj, const double *jm, const double *jrx, const double *jry,
+             const double *jrz, const double *je2,
+             const double *jvx, const double *jvy, const double *jvz,
+             unsigned long order, double inv1, double inv2, double inv3, double inv4,
+             double inv5, double inv6, double inv7,
+             double *ipnax, double *ipnay, double *ipnaz, int prec, void *stream);
+
+/* replaces sakura_kernel, tupan/lib/src/libtupan.h:203-229.  Always FP64
+ * (the Kepler solve needs double); prec is accepted and ignored. */
+int tg_sakura(size_t ni, const double *im, const double *irx, const double *iry,
+              const double *irz, const double *ie2,
+              const double *ivx, const double *ivy, const double *ivz,
+              size_t nj, const double *jm, const double *jrx, const double *jry,
+              const double *jrz, const double *je2,
+              const double *jvx, const double *jvy, const double *jvz,
+              double dt, long flag,
+              double *idrx, double *idry, double *idrz,
+              double *idvx, double *idvy, double *idvz, int prec, void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* Drop-in host entry points: exact libtupan.h signatures (float64 build)  */
+/* ---------------------------------------------------------------------- */
+
+/* tupan/lib/src/libtupan.h:2-15 */
+void phi_kernel(const unsigned long ni, const double *_im, const double *_irx,
+                const double *_iry, const double *_irz, const double *_ie2,
+                const unsigned long nj, const double *_jm, const double *_jrx,
+                const double *_jry, const double *_jrz, const double *_je2,
+                double *_iphi);
+/* tupan/lib/src/libtupan.h:17-32 */
+void acc_kernel(const unsigned long ni, const double *_im, const double *_irx,
+                const double *_iry, const double *_irz, const double *_ie2,
+                const unsigned long nj, const double *_jm, const double *_jrx,
+                const double *_jry, const double *_jrz, const double *_je2,
+                double *_iax, double *_iay, double *_iaz);
+/* tupan/lib/src/libtupan.h:34-58 */
+void acc_jerk_kernel(const unsigned long ni, const double *_im, const double *_irx,
+                     const double *_iry, const double *_irz, const double *_ie2,
+                     const double *_ivx, const double *_ivy, const double *_ivz,
+                     const unsigned long nj, const double *_jm, const double *_jrx,
+                     const double *_jry, const double *_jrz, const double *_je2,
+                     const double *_jvx, const double *_jvy, const double *_jvz,
+                     double *_iax, double *_iay, double *_iaz,
+                     double *_ijx, double *_ijy, double *_ijz);
+/* tupan/lib/src/libtupan.h:60-96 */
+void snap_crackle_kernel(const unsigned long ni, const double *_im, const double *_irx,
+                         const double *_iry, const double *_irz, const double *_ie2,
+                         const double *_ivx, const double *_ivy, const double *_ivz,
+                         const double *_iax, const double *_iay, const double *_iaz,
+                         const double *_ijx, const double *_ijy, const double *_ijz,
+                         const unsigned long nj, const double *_jm, const double *_jrx,
+                         const double *_jry, const double *_jrz, const double *_je2,
+                         const double *_jvx, const double *_jvy, const double *_jvz,
+                         const double *_jax, const double *_jay, const double *_jaz,
+                         const double *_jjx, const double *_jjy, const double *_jjz,
+                         double *_isx, double *_isy, double *_isz,
+                         double *_icx, double *_icy, double *_icz);
+/* tupan/lib/src/libtupan.h:98-119 */
+void tstep_kernel(const unsigned long ni, const double *_im, const double *_irx,
+                  const double *_iry, const double *_irz, const double *_ie2,
+                  const double *_ivx, const double *_ivy, const double *_ivz,
+                  const unsigned long nj, const double *_jm, const double *_jrx,
+                  const double *_jry, const double *_jrz, const double *_je2,
+                  const double *_jvx, const double *_jvy, const double *_jvz,
+                  const double eta, double *_idt_a, double *_idt_b);
+/* tupan/lib/src/libtupan.h:121-150 */
+void pnacc_kernel(const unsigned long ni, const double *_im, const double *_irx,
+                  const double *_iry, const double *_irz, const double *_ie2,
+                  const double *_ivx, const double *_ivy, const double *_ivz,
+                  const unsigned long nj, const double *_jm, const double *_jrx,
+                  const double *_jry, const double *_jrz, const double *_je2,
+                  const double *_jvx, const double *_jvy, const double *_jvz,
+                  unsigned long order, const double inv1, const double inv2,
+                  const double inv3, const double inv4, const double inv5,
+                  const double inv6, const double inv7,
+                  double *_ipnax, double *_ipnay, double *_ipnaz);
+/* tupan/lib/src/libtupan.h:203-229 */
+void sakura_kernel(const unsigned long ni, const double *_im, const double *_irx,
+                   const double *_iry, const double *_irz, const double *_ie2,
+                   const double *_ivx, const double *_ivy, const double *_ivz,
+                   const unsigned long nj, const double *_jm, const double *_jrx,
+                   const double *_jry, const double *_jrz, const double *_je2,
+                   const double *_jvx, const double *_jvy, const double *_jvz,
+                   const double dt, const long flag,
+                   double *_idrx, double *_idry, double *_idrz,
+                   double *_idvx, double *_idvy, double *_idvz);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TUPAN_GB300_H */

@@ -14,10 +14,12 @@
  * that results are bit-identical to the reference on the same machine.
  *
  * Deviation: the reference retries without bound (halving at :483-500,
- * doubling at :580-606).  Here both retry loops stop after ORC_MAX_SPLIT
- * doublings (at most 256 sub-steps) and keep the last iterate; this is only
- * reachable for inputs (radial free fall with v = 0, or softened close pairs whose energy
- * test never passes) on which the
+ * doubling at :580-606).  Here the halving stops after ORC_SPLIT_CAP
+ * doublings, the energy loop after ORC_ENERGY_CAP, and a pair evolution
+ * after ORC_SOLVE_BUDGET Kepler solves, keeping the last iterate (the same
+ * bounds as the GPU kernel).  Within the bounds the steps are the reference's;
+ * the bounds are reached only for inputs (radial free fall with v = 0, or
+ * softened close pairs whose energy test never passes) on which the
  * reference itself never returns.
  */
 #ifndef KEPLER_ORACLE_H
@@ -27,7 +29,9 @@
 
 #define ORC_TOL 2.2737367544323205948e-13 /* 2^-42 */
 #define ORC_MAXITER 64
-#define ORC_MAX_SPLIT 8
+#define ORC_SPLIT_CAP 6      /* up to 64 sub-steps after solver failures */
+#define ORC_ENERGY_CAP 4     /* up to 16 sub-steps for the energy test */
+#define ORC_SOLVE_BUDGET 1024
 #define ORC_PI 3.141592653589793
 
 static inline int orc_sign(double x) { return (x > 0) - (x < 0); }
@@ -106,9 +110,13 @@ static int orc_laguerre(double s0, double *s, const struct orc_kep *k)
     return 0;
 }
 
+/* Kepler solves spent on the current pair evolution (per thread). */
+static __thread int orc_solves;
+
 /* One Kepler solve over dt0; r,v updated in place only on success. */
 static int orc_kepler_once(double dt0, double m, double e2, double r[3], double v[3])
 {
+    orc_solves += 1;
     double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
     if (!(r2 > 0)) return 0;
     r2 += e2;
@@ -160,9 +168,10 @@ static void orc_kepler_split(double dt, double m, double e2,
         for (int q = 0; q < 3; ++q) { r[q] = r0[q]; v[q] = v0[q]; }
         int failed = 0;
         for (long i = 0; i < n; ++i) {
+            if (orc_solves >= ORC_SOLVE_BUDGET) return;
             if (orc_kepler_once(dt / n, m, e2, r, v) != 0) { failed = 1; break; }
         }
-        if (!failed || tries >= ORC_MAX_SPLIT) return;
+        if (!failed || tries >= ORC_SPLIT_CAP) return;
         n *= 2;
     }
 }
@@ -197,7 +206,7 @@ static void orc_kepler(double dt, double m, double e2,
     if (2 * err < tol * (u1 + u0)) return;
 
     long n = 1;
-    for (int tries = 0; tries < ORC_MAX_SPLIT; ++tries) {
+    for (int tries = 0; tries < ORC_ENERGY_CAP; ++tries) {
         n *= 2;
         for (int q = 0; q < 3; ++q) { r[q] = r0[q]; v[q] = v0[q]; }
         int bad = 0;
@@ -207,6 +216,7 @@ static void orc_kepler(double dt, double m, double e2,
             orc_energy(m, e2, r, v, &u1, &en1);
             err = fabs(en1 - en0);
             if (2 * err > tol * (u1 + u0)) { bad = 1; break; }
+            if (orc_solves >= ORC_SOLVE_BUDGET) return;
         }
         if (!bad) return;
     }
@@ -253,6 +263,7 @@ static void orc_twobody_evolve(double dt, long flag, double m, double e2,
 {
     double r[3] = {r0[0], r0[1], r0[2]}, v[3] = {v0[0], v0[1], v0[2]};
     double rt[3], vt[3];
+    orc_solves = 0;
     if (flag == -1) {
         for (int k = 0; k < 3; ++k) r[k] -= v[k] * dt;
         orc_twobody(dt, m, e2, r, v, rt, vt);

@@ -22,6 +22,7 @@
  * per-particle result because each i-sum runs over j in order).
  */
 #define _POSIX_C_SOURCE 200809L
+#define _GNU_SOURCE
 #include <math.h>
 #include <pthread.h>
 #include <stddef.h>

@@ -1,0 +1,103 @@
+"""ctypes binding of libtupan_gb300.so (include/tupan_gb300.h).
+
+The library is the only compute path: importing this module without the
+built library raises ImportError with the build command, and there is no
+CPU fallback anywhere in the package.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libtupan_gb300.so")
+
+PREC_FP64 = 0
+PREC_DS32 = 1
+
+OK = 0
+EINVAL = -1
+ECUDA = -2
+ENOMEM = -3
+ENODEV = -4
+
+ST_MBAR_TIMEOUT = 1
+ST_KEPLER_CAP = 2
+ST_LAGUERRE_CAP = 4
+
+P5 = ("mass", "rx", "ry", "rz", "eps2")
+P8 = P5 + ("vx", "vy", "vz")
+P14 = P8 + ("ax", "ay", "az", "jx", "jy", "jz")
+
+# kernel -> (particle fields, scalar ctypes, output names); libtupan.h:2-246
+SPECS = {
+    "phi": (P5, (), ("phi",)),
+    "acc": (P5, (), ("ax", "ay", "az")),
+    "acc_jerk": (P8, (), ("ax", "ay", "az", "jx", "jy", "jz")),
+    "snap_crackle": (P14, (), ("sx", "sy", "sz", "cx", "cy", "cz")),
+    "tstep": (P8, (ctypes.c_double,), ("tstep", "tstepij")),
+    "pnacc": (P8, (ctypes.c_ulong,) + (ctypes.c_double,) * 7, ("pnax", "pnay", "pnaz")),
+    "sakura": (P8, (ctypes.c_double, ctypes.c_long), ("drx", "dry", "drz", "dvx", "dvy", "dvz")),
+}
+
+_DP = ctypes.c_void_p
+
+
+class TupanGB300Error(RuntimeError):
+    """A call into libtupan_gb300 returned an error code."""
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            "libtupan_gb300.so is not built (%s); run `python -m tupan_gb300.build` "
+            "or __graft_entry__.build()" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (fields, scal, outs) in SPECS.items():
+        for prefix in ("tg_", ""):
+            fn = getattr(lib, prefix + name + ("" if prefix else "_kernel"))
+            args = [ctypes.c_size_t if prefix else ctypes.c_ulong] + [_DP] * len(fields)
+            args += [ctypes.c_size_t if prefix else ctypes.c_ulong] + [_DP] * len(fields)
+            args += list(scal) + [_DP] * len(outs)
+            if prefix:
+                args += [ctypes.c_int, _DP]
+                fn.restype = ctypes.c_int
+            else:
+                fn.restype = None
+            fn.argtypes = args
+    lib.tg_version.restype = ctypes.c_char_p
+    lib.tg_last_error.restype = ctypes.c_char_p
+    lib.tg_sync_status.restype = ctypes.c_int
+    lib.tg_sync_status.argtypes = [_DP]
+    lib.tg_set_host_precision.argtypes = [ctypes.c_int]
+    lib.tg_set_host_precision.restype = ctypes.c_int
+    lib.tg_get_host_precision.restype = ctypes.c_int
+    lib.tg_device_sms.restype = ctypes.c_int
+    lib.tg_probe_fma_tflops.restype = ctypes.c_double
+    lib.tg_probe_fma_tflops.argtypes = [ctypes.c_int, ctypes.c_int, _DP]
+    return lib
+
+
+lib = _load()
+
+
+def last_error():
+    return lib.tg_last_error().decode()
+
+
+def check(rc, what):
+    if rc != OK:
+        raise TupanGB300Error("%s failed (code %d): %s" % (what, rc, last_error()))
+    return rc
+
+
+def call_device(name, ni, iptrs, nj, jptrs, scalars, optrs, prec, stream):
+    """Call tg_<name> with raw device pointers (ints); raises on error."""
+    fn = getattr(lib, "tg_" + name)
+    rc = fn(ni, *iptrs, nj, *jptrs, *scalars, *optrs, int(prec), stream)
+    return check(rc, "tg_" + name)
+
+
+def sync_status(stream=None):
+    rc = lib.tg_sync_status(stream)
+    if rc < 0:
+        raise TupanGB300Error("tg_sync_status failed: %s" % last_error())
+    return rc

@@ -1,0 +1,473 @@
+// tg_api.cu -- C ABI of libtupan_gb300.so (declared in include/tupan_gb300.h).
+//
+// Responsibilities: argument validation, per-device context (SM count,
+// workspace, status word), dispatch to the FP64 or split-FP32 launchers, and
+// the drop-in host entry points with the reference's libtupan.h signatures.
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/tupan_gb300.h"
+#include "tg_device.cuh"
+#include "tg_internal.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *what, cudaError_t e = cudaSuccess) {
+    char buf[512];
+    if (e != cudaSuccess)
+        snprintf(buf, sizeof buf, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+    else
+        snprintf(buf, sizeof buf, "%s", what);
+    g_err = buf;
+    return code;
+}
+
+constexpr int MAX_DEV = 64;
+
+struct DevCtx {
+    std::mutex mu;
+    bool ready = false;
+    int sms = 0;
+    void *ws = nullptr;
+    size_t ws_bytes = 0;
+    unsigned *status = nullptr;   // device word, sticky until tg_sync_status
+};
+DevCtx g_dev[MAX_DEV];
+
+int current_ctx(DevCtx **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(TG_ENODEV, "cudaGetDevice", e);
+    if (dev < 0 || dev >= MAX_DEV) return fail(TG_ENODEV, "device index out of range");
+    DevCtx &c = g_dev[dev];
+    std::lock_guard<std::mutex> lk(c.mu);
+    if (!c.ready) {
+        e = cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return fail(TG_ECUDA, "cudaDeviceGetAttribute", e);
+        e = cudaMalloc(&c.status, sizeof(unsigned));
+        if (e != cudaSuccess) return fail(TG_ENOMEM, "cudaMalloc(status)", e);
+        e = cudaMemset(c.status, 0, sizeof(unsigned));
+        if (e != cudaSuccess) return fail(TG_ECUDA, "cudaMemset(status)", e);
+        c.ready = true;
+    }
+    *out = &c;
+    return TG_OK;
+}
+
+// Grow-only workspace.  Calls that need scratch memory serialise on the
+// context mutex on the host; GPU-side, two calls on different streams that
+// overlap in time must not share a device (documented in the header).
+int ensure_ws(DevCtx &c, size_t bytes, cudaStream_t s) {
+    if (bytes <= c.ws_bytes) return TG_OK;
+    if (c.ws) {
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return fail(TG_ECUDA, "cudaStreamSynchronize", e);
+        cudaFree(c.ws);
+        c.ws = nullptr;
+        c.ws_bytes = 0;
+    }
+    size_t want = bytes + bytes / 4;
+    cudaError_t e = cudaMalloc(&c.ws, want);
+    if (e != cudaSuccess) return fail(TG_ENOMEM, "cudaMalloc(workspace)", e);
+    c.ws_bytes = want;
+    return TG_OK;
+}
+
+constexpr size_t MAX_N = (size_t)1 << 31;
+
+int run(int kernel, tg::PairArgs &a, int prec, void *stream) {
+    g_err.clear();
+    if (prec != TG_PREC_FP64 && prec != TG_PREC_DS32) return fail(TG_EINVAL, "unknown precision");
+    if (a.ni > MAX_N || a.nj > MAX_N) return fail(TG_EINVAL, "ni or nj above 2^31");
+    const int nf = tg::kernel_fields(kernel), no = tg::kernel_outputs(kernel);
+    if (a.ni > 0) {
+        for (int f = 0; f < nf; ++f)
+            if (!a.I.f[f]) return fail(TG_EINVAL, "null i-set pointer");
+        for (int o = 0; o < no; ++o)
+            if (!a.out[o]) return fail(TG_EINVAL, "null output pointer");
+    }
+    if (a.nj > 0)
+        for (int f = 0; f < nf; ++f)
+            if (!a.J.f[f]) return fail(TG_EINVAL, "null j-set pointer");
+    if (a.ni == 0) return TG_OK;
+    DevCtx *c = nullptr;
+    int rc = current_ctx(&c);
+    if (rc != TG_OK) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    a.status = c->status;
+    cudaError_t e;
+    if (prec == TG_PREC_FP64 || !tg::ds32_supported(kernel) || a.nj == 0) {
+        e = tg::launch_fp64(kernel, a, s);
+    } else {
+        std::lock_guard<std::mutex> lk(c->mu);
+        const size_t need = tg::ds32_workspace_bytes(kernel, a.ni, a.nj, c->sms);
+        rc = ensure_ws(*c, need, s);
+        if (rc != TG_OK) return rc;
+        e = tg::launch_ds32(kernel, a, c->ws, c->ws_bytes, c->sms, s);
+    }
+    if (e != cudaSuccess) return fail(TG_ECUDA, "kernel launch", e);
+    return TG_OK;
+}
+
+void set5(tg::PSet &p, const double *m, const double *x, const double *y, const double *z,
+          const double *e) {
+    std::memset(&p, 0, sizeof p);
+    p.f[tg::F_M] = m; p.f[tg::F_RX] = x; p.f[tg::F_RY] = y; p.f[tg::F_RZ] = z; p.f[tg::F_E2] = e;
+}
+void setv(tg::PSet &p, const double *u, const double *v, const double *w) {
+    p.f[tg::F_VX] = u; p.f[tg::F_VY] = v; p.f[tg::F_VZ] = w;
+}
+tg::PairArgs blank() {
+    tg::PairArgs a;
+    std::memset(&a, 0, sizeof a);
+    return a;
+}
+
+int g_host_prec = TG_PREC_FP64;
+
+// ---------------------------------------------------------------------------
+// Host staging for the drop-in entry points: one library stream and cached
+// device buffers per device.
+// ---------------------------------------------------------------------------
+struct HostStage {
+    std::mutex mu;
+    cudaStream_t stream = nullptr;
+    double *buf = nullptr;
+    size_t cap = 0;   // doubles
+};
+HostStage g_stage[MAX_DEV];
+
+struct HostCall {
+    int kernel;
+    size_t ni, nj;
+    const double *in_i[14];
+    const double *in_j[14];
+    double *out[6];
+};
+
+// Copies the host arrays in, runs `launch` on device copies, copies out.
+template <class F>
+void host_call(const HostCall &h, F launch) {
+    g_err.clear();
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEV) {
+        fail(TG_ENODEV, "no CUDA device for host entry point");
+        fprintf(stderr, "tupan_gb300: %s\n", g_err.c_str());
+        return;
+    }
+    HostStage &st = g_stage[dev];
+    std::lock_guard<std::mutex> lk(st.mu);
+    const int nf = tg::kernel_fields(h.kernel), no = tg::kernel_outputs(h.kernel);
+    const size_t need = (size_t)nf * (h.ni + h.nj) + (size_t)no * h.ni + 8;
+    cudaError_t e = cudaSuccess;
+    if (!st.stream) e = cudaStreamCreateWithFlags(&st.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess && need > st.cap) {
+        if (st.buf) cudaFree(st.buf);
+        st.buf = nullptr;
+        st.cap = 0;
+        e = cudaMalloc(&st.buf, need * sizeof(double));
+        if (e == cudaSuccess) st.cap = need;
+    }
+    if (e != cudaSuccess) {
+        fail(TG_ECUDA, "host entry point staging", e);
+        fprintf(stderr, "tupan_gb300: %s\n", g_err.c_str());
+        return;
+    }
+    double *p = st.buf;
+    const double *di[14] = {}, *dj[14] = {};
+    double *dout[6] = {};
+    for (int f = 0; f < nf && e == cudaSuccess; ++f) {
+        if (h.ni) e = cudaMemcpyAsync(p, h.in_i[f], h.ni * sizeof(double), cudaMemcpyHostToDevice, st.stream);
+        di[f] = p; p += h.ni;
+    }
+    for (int f = 0; f < nf && e == cudaSuccess; ++f) {
+        if (h.nj) e = cudaMemcpyAsync(p, h.in_j[f], h.nj * sizeof(double), cudaMemcpyHostToDevice, st.stream);
+        dj[f] = p; p += h.nj;
+    }
+    for (int o = 0; o < no; ++o) { dout[o] = p; p += h.ni; }
+    int rc = (e == cudaSuccess) ? launch(di, dj, dout, st.stream) : TG_ECUDA;
+    for (int o = 0; o < no && rc == TG_OK && e == cudaSuccess; ++o)
+        if (h.ni) e = cudaMemcpyAsync(h.out[o], dout[o], h.ni * sizeof(double), cudaMemcpyDeviceToHost, st.stream);
+    cudaError_t se = cudaStreamSynchronize(st.stream);
+    if (e == cudaSuccess) e = se;
+    if (rc != TG_OK || e != cudaSuccess) {
+        if (e != cudaSuccess) fail(TG_ECUDA, "host entry point", e);
+        fprintf(stderr, "tupan_gb300: %s\n", g_err.c_str());
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *tg_version(void) { return "tupan_gb300 0.1.0 (sm_103a)"; }
+const char *tg_last_error(void) { return g_err.c_str(); }
+
+int tg_device_sms(void) {
+    DevCtx *c = nullptr;
+    if (current_ctx(&c) != TG_OK) return 0;
+    return c->sms;
+}
+
+int tg_sync_status(void *stream) {
+    DevCtx *c = nullptr;
+    int rc = current_ctx(&c);
+    if (rc != TG_OK) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, c->status, sizeof h, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->status, 0, sizeof(unsigned), s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(TG_ECUDA, "tg_sync_status", e);
+    return (int)h;
+}
+
+int tg_set_host_precision(int prec) {
+    if (prec != TG_PREC_FP64 && prec != TG_PREC_DS32) return fail(TG_EINVAL, "unknown precision");
+    g_host_prec = prec;
+    return TG_OK;
+}
+int tg_get_host_precision(void) { return g_host_prec; }
+
+int tg_phi(size_t ni, const double *im, const double *irx, const double *iry, const double *irz,
+           const double *ie2, size_t nj, const double *jm, const double *jrx, const double *jry,
+           const double *jrz, const double *je2, double *iphi, int prec, void *stream) {
+    tg::PairArgs a = blank();
+    set5(a.I, im, irx, iry, irz, ie2);
+    set5(a.J, jm, jrx, jry, jrz, je2);
+    a.ni = ni; a.nj = nj; a.out[0] = iphi;
+    return run(tg::K_PHI, a, prec, stream);
+}
+
+int tg_acc(size_t ni, const double *im, const double *irx, const double *iry, const double *irz,
+           const double *ie2, size_t nj, const double *jm, const double *jrx, const double *jry,
+           const double *jrz, const double *je2, double *iax, double *iay, double *iaz, int prec,
+           void *stream) {
+    tg::PairArgs a = blank();
+    set5(a.I, im, irx, iry, irz, ie2);
+    set5(a.J, jm, jrx, jry, jrz, je2);
+    a.ni = ni; a.nj = nj; a.out[0] = iax; a.out[1] = iay; a.out[2] = iaz;
+    return run(tg::K_ACC, a, prec, stream);
+}
+
+int tg_acc_jerk(size_t ni, const double *im, const double *irx, const double *iry,
+                const double *irz, const double *ie2, const double *ivx, const double *ivy,
+                const double *ivz, size_t nj, const double *jm, const double *jrx,
+                const double *jry, const double *jrz, const double *je2, const double *jvx,
+                const double *jvy, const double *jvz, double *iax, double *iay, double *iaz,
+                double *ijx, double *ijy, double *ijz, int prec, void *stream) {
+    tg::PairArgs a = blank();
+    set5(a.I, im, irx, iry, irz, ie2); setv(a.I, ivx, ivy, ivz);
+    set5(a.J, jm, jrx, jry, jrz, je2); setv(a.J, jvx, jvy, jvz);
+    a.ni = ni; a.nj = nj;
+    a.out[0] = iax; a.out[1] = iay; a.out[2] = iaz; a.out[3] = ijx; a.out[4] = ijy; a.out[5] = ijz;
+    return run(tg::K_ACC_JERK, a, prec, stream);
+}
+
+int tg_snap_crackle(size_t ni, const double *im, const double *irx, const double *iry,
+                    const double *irz, const double *ie2, const double *ivx, const double *ivy,
+                    const double *ivz, const double *iax, const double *iay, const double *iaz,
+                    const double *ijx, const double *ijy, const double *ijz, size_t nj,
+                    const double *jm, const double *jrx, const double *jry, const double *jrz,
+                    const double *je2, const double *jvx, const double *jvy, const double *jvz,
+                    const double *jax, const double *jay, const double *jaz, const double *jjx,
+                    const double *jjy, const double *jjz, double *isx, double *isy, double *isz,
+                    double *icx, double *icy, double *icz, int prec, void *stream) {
+    tg::PairArgs a = blank();
+    set5(a.I, im, irx, iry, irz, ie2); setv(a.I, ivx, ivy, ivz);
+    a.I.f[tg::F_AX] = iax; a.I.f[tg::F_AY] = iay; a.I.f[tg::F_AZ] = iaz;
+    a.I.f[tg::F_JX] = ijx; a.I.f[tg::F_JY] = ijy; a.I.f[tg::F_JZ] = ijz;
+    set5(a.J, jm, jrx, jry, jrz, je2); setv(a.J, jvx, jvy, jvz);
+    a.J.f[tg::F_AX] = jax; a.J.f[tg::F_AY] = jay; a.J.f[tg::F_AZ] = jaz;
+    a.J.f[tg::F_JX] = jjx; a.J.f[tg::F_JY] = jjy; a.J.f[tg::F_JZ] = jjz;
+    a.ni = ni; a.nj = nj;
+    a.out[0] = isx; a.out[1] = isy; a.out[2] = isz; a.out[3] = icx; a.out[4] = icy; a.out[5] = icz;
+    return run(tg::K_SNAP_CRACKLE, a, prec, stream);
+}
+
+int tg_tstep(size_t ni, const double *im, const double *irx, const double *iry, const double *irz,
+             const double *ie2, const double *ivx, const double *ivy, const double *ivz, size_t nj,
+             const double *jm, const double *jrx, const double *jry, const double *jrz,
+             const double *je2, const double *jvx, const double *jvy, const double *jvz,
+             double eta, double *idt_a, double *idt_b, int prec, void *stream) {
+    tg::PairArgs a = blank();
+    set5(a.I, im, irx, iry, irz, ie2); setv(a.I, ivx, ivy, ivz);
+    set5(a.J, jm, jrx, jry, jrz, je2); setv(a.J, jvx, jvy, jvz);
+    a.ni = ni; a.nj = nj; a.eta = eta; a.out[0] = idt_a; a.out[1] = idt_b;
+    return run(tg::K_TSTEP, a, prec, stream);
+}
+
+int tg_pnacc(size_t ni, const double *im, const double *irx, const double *iry, const double *irz,
+             const double *ie2, const double *ivx, const double *ivy, const double *ivz, size_t nj,
+             const double *jm, const double *jrx, const double *jry, const double *jrz,
+             const double *je2, const double *jvx, const double *jvy, const double *jvz,
+             unsigned long order, double inv1, double inv2, double inv3, double inv4, double inv5,
+             double inv6, double inv7, double *ipnax, double *ipnay, double *ipnaz, int prec,
+             void *stream) {
+    tg::PairArgs a = blank();
+    set5(a.I, im, irx, iry, irz, ie2); setv(a.I, ivx, ivy, ivz);
+    set5(a.J, jm, jrx, jry, jrz, je2); setv(a.J, jvx, jvy, jvz);
+    a.ni = ni; a.nj = nj; a.order = order;
+    a.inv[1] = inv1; a.inv[2] = inv2; a.inv[3] = inv3; a.inv[4] = inv4;
+    a.inv[5] = inv5; a.inv[6] = inv6; a.inv[7] = inv7;
+    a.out[0] = ipnax; a.out[1] = ipnay; a.out[2] = ipnaz;
+    return run(tg::K_PNACC, a, prec, stream);
+}
+
+int tg_sakura(size_t ni, const double *im, const double *irx, const double *iry, const double *irz,
+              const double *ie2, const double *ivx, const double *ivy, const double *ivz, size_t nj,
+              const double *jm, const double *jrx, const double *jry, const double *jrz,
+              const double *je2, const double *jvx, const double *jvy, const double *jvz, double dt,
+              long flag, double *idrx, double *idry, double *idrz, double *idvx, double *idvy,
+              double *idvz, int prec, void *stream) {
+    tg::PairArgs a = blank();
+    set5(a.I, im, irx, iry, irz, ie2); setv(a.I, ivx, ivy, ivz);
+    set5(a.J, jm, jrx, jry, jrz, je2); setv(a.J, jvx, jvy, jvz);
+    a.ni = ni; a.nj = nj; a.dt = dt; a.flag = flag;
+    a.out[0] = idrx; a.out[1] = idry; a.out[2] = idrz; a.out[3] = idvx; a.out[4] = idvy; a.out[5] = idvz;
+    (void)prec;
+    return run(tg::K_SAKURA, a, TG_PREC_FP64, stream);
+}
+
+// ---------------------------------------------------------------------------
+// Drop-in host entry points (libtupan.h signatures).
+// ---------------------------------------------------------------------------
+#define HC_BEGIN(K, NI, NJ)                        \
+    HostCall h;                                    \
+    std::memset(&h, 0, sizeof h);                  \
+    h.kernel = (K); h.ni = (NI); h.nj = (NJ);
+#define I5(m, x, y, z, e) h.in_i[0] = m; h.in_i[1] = x; h.in_i[2] = y; h.in_i[3] = z; h.in_i[4] = e;
+#define J5(m, x, y, z, e) h.in_j[0] = m; h.in_j[1] = x; h.in_j[2] = y; h.in_j[3] = z; h.in_j[4] = e;
+#define IV(u, v, w) h.in_i[5] = u; h.in_i[6] = v; h.in_i[7] = w;
+#define JV(u, v, w) h.in_j[5] = u; h.in_j[6] = v; h.in_j[7] = w;
+
+void phi_kernel(const unsigned long ni, const double *_im, const double *_irx, const double *_iry,
+                const double *_irz, const double *_ie2, const unsigned long nj, const double *_jm,
+                const double *_jrx, const double *_jry, const double *_jrz, const double *_je2,
+                double *_iphi) {
+    HC_BEGIN(tg::K_PHI, ni, nj)
+    I5(_im, _irx, _iry, _irz, _ie2) J5(_jm, _jrx, _jry, _jrz, _je2)
+    h.out[0] = _iphi;
+    host_call(h, [&](const double **i, const double **j, double **o, cudaStream_t s) {
+        return tg_phi(ni, i[0], i[1], i[2], i[3], i[4], nj, j[0], j[1], j[2], j[3], j[4], o[0],
+                      g_host_prec, s);
+    });
+}
+
+void acc_kernel(const unsigned long ni, const double *_im, const double *_irx, const double *_iry,
+                const double *_irz, const double *_ie2, const unsigned long nj, const double *_jm,
+                const double *_jrx, const double *_jry, const double *_jrz, const double *_je2,
+                double *_iax, double *_iay, double *_iaz) {
+    HC_BEGIN(tg::K_ACC, ni, nj)
+    I5(_im, _irx, _iry, _irz, _ie2) J5(_jm, _jrx, _jry, _jrz, _je2)
+    h.out[0] = _iax; h.out[1] = _iay; h.out[2] = _iaz;
+    host_call(h, [&](const double **i, const double **j, double **o, cudaStream_t s) {
+        return tg_acc(ni, i[0], i[1], i[2], i[3], i[4], nj, j[0], j[1], j[2], j[3], j[4], o[0],
+                      o[1], o[2], g_host_prec, s);
+    });
+}
+
+void acc_jerk_kernel(const unsigned long ni, const double *_im, const double *_irx,
+                     const double *_iry, const double *_irz, const double *_ie2,
+                     const double *_ivx, const double *_ivy, const double *_ivz,
+                     const unsigned long nj, const double *_jm, const double *_jrx,
+                     const double *_jry, const double *_jrz, const double *_je2,
+                     const double *_jvx, const double *_jvy, const double *_jvz, double *_iax,
+                     double *_iay, double *_iaz, double *_ijx, double *_ijy, double *_ijz) {
+    HC_BEGIN(tg::K_ACC_JERK, ni, nj)
+    I5(_im, _irx, _iry, _irz, _ie2) IV(_ivx, _ivy, _ivz)
+    J5(_jm, _jrx, _jry, _jrz, _je2) JV(_jvx, _jvy, _jvz)
+    h.out[0] = _iax; h.out[1] = _iay; h.out[2] = _iaz; h.out[3] = _ijx; h.out[4] = _ijy; h.out[5] = _ijz;
+    host_call(h, [&](const double **i, const double **j, double **o, cudaStream_t s) {
+        return tg_acc_jerk(ni, i[0], i[1], i[2], i[3], i[4], i[5], i[6], i[7], nj, j[0], j[1], j[2],
+                           j[3], j[4], j[5], j[6], j[7], o[0], o[1], o[2], o[3], o[4], o[5],
+                           g_host_prec, s);
+    });
+}
+
+void snap_crackle_kernel(const unsigned long ni, const double *_im, const double *_irx,
+                         const double *_iry, const double *_irz, const double *_ie2,
+                         const double *_ivx, const double *_ivy, const double *_ivz,
+                         const double *_iax, const double *_iay, const double *_iaz,
+                         const double *_ijx, const double *_ijy, const double *_ijz,
+                         const unsigned long nj, const double *_jm, const double *_jrx,
+                         const double *_jry, const double *_jrz, const double *_je2,
+                         const double *_jvx, const double *_jvy, const double *_jvz,
+                         const double *_jax, const double *_jay, const double *_jaz,
+                         const double *_jjx, const double *_jjy, const double *_jjz, double *_isx,
+                         double *_isy, double *_isz, double *_icx, double *_icy, double *_icz) {
+    HC_BEGIN(tg::K_SNAP_CRACKLE, ni, nj)
+    I5(_im, _irx, _iry, _irz, _ie2) IV(_ivx, _ivy, _ivz)
+    J5(_jm, _jrx, _jry, _jrz, _je2) JV(_jvx, _jvy, _jvz)
+    h.in_i[8] = _iax; h.in_i[9] = _iay; h.in_i[10] = _iaz;
+    h.in_i[11] = _ijx; h.in_i[12] = _ijy; h.in_i[13] = _ijz;
+    h.in_j[8] = _jax; h.in_j[9] = _jay; h.in_j[10] = _jaz;
+    h.in_j[11] = _jjx; h.in_j[12] = _jjy; h.in_j[13] = _jjz;
+    h.out[0] = _isx; h.out[1] = _isy; h.out[2] = _isz; h.out[3] = _icx; h.out[4] = _icy; h.out[5] = _icz;
+    host_call(h, [&](const double **i, const double **j, double **o, cudaStream_t s) {
+        return tg_snap_crackle(ni, i[0], i[1], i[2], i[3], i[4], i[5], i[6], i[7], i[8], i[9], i[10],
+                               i[11], i[12], i[13], nj, j[0], j[1], j[2], j[3], j[4], j[5], j[6],
+                               j[7], j[8], j[9], j[10], j[11], j[12], j[13], o[0], o[1], o[2], o[3],
+                               o[4], o[5], g_host_prec, s);
+    });
+}
+
+void tstep_kernel(const unsigned long ni, const double *_im, const double *_irx, const double *_iry,
+                  const double *_irz, const double *_ie2, const double *_ivx, const double *_ivy,
+                  const double *_ivz, const unsigned long nj, const double *_jm,
+                  const double *_jrx, const double *_jry, const double *_jrz, const double *_je2,
+                  const double *_jvx, const double *_jvy, const double *_jvz, const double eta,
+                  double *_idt_a, double *_idt_b) {
+    HC_BEGIN(tg::K_TSTEP, ni, nj)
+    I5(_im, _irx, _iry, _irz, _ie2) IV(_ivx, _ivy, _ivz)
+    J5(_jm, _jrx, _jry, _jrz, _je2) JV(_jvx, _jvy, _jvz)
+    h.out[0] = _idt_a; h.out[1] = _idt_b;
+    host_call(h, [&](const double **i, const double **j, double **o, cudaStream_t s) {
+        return tg_tstep(ni, i[0], i[1], i[2], i[3], i[4], i[5], i[6], i[7], nj, j[0], j[1], j[2],
+                        j[3], j[4], j[5], j[6], j[7], eta, o[0], o[1], g_host_prec, s);
+    });
+}
+
+void pnacc_kernel(const unsigned long ni, const double *_im, const double *_irx, const double *_iry,
+                  const double *_irz, const double *_ie2, const double *_ivx, const double *_ivy,
+                  const double *_ivz, const unsigned long nj, const double *_jm,
+                  const double *_jrx, const double *_jry, const double *_jrz, const double *_je2,
+                  const double *_jvx, const double *_jvy, const double *_jvz, unsigned long order,
+                  const double inv1, const double inv2, const double inv3, const double inv4,
+                  const double inv5, const double inv6, const double inv7, double *_ipnax,
+                  double *_ipnay, double *_ipnaz) {
+    HC_BEGIN(tg::K_PNACC, ni, nj)
+    I5(_im, _irx, _iry, _irz, _ie2) IV(_ivx, _ivy, _ivz)
+    J5(_jm, _jrx, _jry, _jrz, _je2) JV(_jvx, _jvy, _jvz)
+    h.out[0] = _ipnax; h.out[1] = _ipnay; h.out[2] = _ipnaz;
+    host_call(h, [&](const double **i, const double **j, double **o, cudaStream_t s) {
+        return tg_pnacc(ni, i[0], i[1], i[2], i[3], i[4], i[5], i[6], i[7], nj, j[0], j[1], j[2],
+                        j[3], j[4], j[5], j[6], j[7], order, inv1, inv2, inv3, inv4, inv5, inv6,
+                        inv7, o[0], o[1], o[2], g_host_prec, s);
+    });
+}
+
+void sakura_kernel(const unsigned long ni, const double *_im, const double *_irx, const double *_iry,
+                   const double *_irz, const double *_ie2, const double *_ivx, const double *_ivy,
+                   const double *_ivz, const unsigned long nj, const double *_jm,
+                   const double *_jrx, const double *_jry, const double *_jrz, const double *_je2,
+                   const double *_jvx, const double *_jvy, const double *_jvz, const double dt,
+                   const long flag, double *_idrx, double *_idry, double *_idrz, double *_idvx,
+                   double *_idvy, double *_idvz) {
+    HC_BEGIN(tg::K_SAKURA, ni, nj)
+    I5(_im, _irx, _iry, _irz, _ie2) IV(_ivx, _ivy, _ivz)
+    J5(_jm, _jrx, _jry, _jrz, _je2) JV(_jvx, _jvy, _jvz)
+    h.out[0] = _idrx; h.out[1] = _idry; h.out[2] = _idrz; h.out[3] = _idvx; h.out[4] = _idvy; h.out[5] = _idvz;
+    host_call(h, [&](const double **i, const double **j, double **o, cudaStream_t s) {
+        return tg_sakura(ni, i[0], i[1], i[2], i[3], i[4], i[5], i[6], i[7], nj, j[0], j[1], j[2],
+                         j[3], j[4], j[5], j[6], j[7], dt, flag, o[0], o[1], o[2], o[3], o[4], o[5],
+                         TG_PREC_FP64, s);
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,127 @@
+// tg_device.cuh -- device-side building blocks shared by the pairwise kernels.
+//
+//  * exact IEEE double helpers (no FMA contraction) so the FP64 kernels keep
+//    the reference's per-operation rounding (tupan/lib/src/*_kernel_common.h);
+//  * packed f32x2 arithmetic (Blackwell FADD2/FMUL2/FFMA2) for the split-FP32
+//    kernels, which evaluate two j-particles per instruction;
+//  * mbarrier + cp.async.bulk (TMA bulk copy, no multicast) wrappers with
+//    bounded waits for staging j-tiles into shared memory.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tg {
+
+// ---------------------------------------------------------------------------
+// Status bits written by kernels into the per-call device status word.
+// ---------------------------------------------------------------------------
+enum : unsigned {
+    ST_MBAR_TIMEOUT = 1u << 0,   // a bounded mbarrier wait gave up
+    ST_KEPLER_CAP = 1u << 1,     // Sakura: Kepler retry cap reached
+    ST_LAGUERRE_CAP = 1u << 2,   // Sakura: Laguerre iteration cap reached
+};
+
+// ---------------------------------------------------------------------------
+// Exact double arithmetic: every operation rounds once, never contracted.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ double dsqrt(double a) { return __dsqrt_rn(a); }
+// a*a + b*b + c*c evaluated left to right, as `rx * rx + ry * ry + rz * rz`
+__device__ __forceinline__ double ddot3(double a0, double a1, double a2,
+                                        double b0, double b1, double b2) {
+    return dadd(dadd(dmul(a0, b0), dmul(a1, b1)), dmul(a2, b2));
+}
+
+// ---------------------------------------------------------------------------
+// Packed float pairs.  Lane .x holds an even j, lane .y the next odd j.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    return __fadd2_rn(a, make_float2(-b.x, -b.y));
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// c - a*b
+__device__ __forceinline__ float2 fnma2(float2 a, float2 b, float2 c) {
+    return __ffma2_rn(make_float2(-a.x, -a.y), b, c);
+}
+
+// Hardware reciprocal square root (MUFU.RSQ), then one Newton step
+// y <- y + y*(1/2 - (s/2) y^2): relative error ~1 ulp instead of ~2 ulp.
+__device__ __forceinline__ float rsqrt_hw(float s) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(s));
+    return y;
+}
+
+// Pair exclusion: lane is kept when r != 0, i.e. any of dx, dy, dz is
+// nonzero (exact differences of equal coordinates are +0).  Equivalent to
+// the reference's `r2 > 0` except for |dr| below 1e-19 where r2 underflows.
+__device__ __forceinline__ bool nonzero3(float a, float b, float c) {
+    return ((__float_as_uint(a) | __float_as_uint(b) | __float_as_uint(c)) << 1) != 0u;
+}
+
+// ---------------------------------------------------------------------------
+// Compensated accumulator: value = hi + lo, updated once per j-block with
+// Kahan/Neumaier-free TwoSum-lite (Fast2Sum needs |hi| >= |x|; plain Kahan is
+// used instead, which holds regardless of magnitudes).
+// ---------------------------------------------------------------------------
+struct Comp {
+    float s, c;   // running sum and (negated) lost low part
+};
+__device__ __forceinline__ void comp_add(Comp &k, float x) {
+    float y = __fsub_rn(x, k.c);
+    float t = __fadd_rn(k.s, y);
+    k.c = __fsub_rn(__fsub_rn(t, k.s), y);
+    k.s = t;
+}
+__device__ __forceinline__ double comp_value(const Comp &k) {
+    return (double)k.s - (double)k.c;
+}
+
+// ---------------------------------------------------------------------------
+// mbarrier / bulk-copy PTX (sm_90+ forms, valid on sm_103a).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                 ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+// Global -> shared bulk copy completing on `bar`.  dst, src 16-byte aligned,
+// bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+// Bounded wait: gives up after `limit` polls and reports false.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t limit = (1u << 22)) {
+    for (uint32_t it = 0; it < limit; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+    }
+    return false;
+}
+
+}  // namespace tg

@@ -1,0 +1,296 @@
+// tg_fp64.cu -- FP64 pairwise kernels.
+//
+// One thread owns one i-particle and walks the j-set in order, exactly like
+// the reference loops (tupan/lib/src/<name>_kernel.c), staging j-tiles of
+// the needed fields through shared memory.  Every per-pair operation uses
+// the uncontracted IEEE helpers of tg_device.cuh in the reference's order
+// (tupan/lib/src/<name>_kernel_common.h, smoothing.h), so Phi, Acc, AccJerk,
+// SnapCrackle and Tstep return results bit-identical to the reference C
+// backend.  PNAcc evaluates the post-Newtonian polynomial in its own order
+// (tg_pn_terms.cuh); Sakura uses the bounded Kepler solver of tg_kepler.cuh.
+//
+// Roofline: FP64 issue.  GB300 executes FP64 at a small fraction of the FP32
+// rate and each pair needs one IEEE divide and one square root, so these
+// kernels are the accuracy reference on the GPU, not the fast path.
+#include "tg_device.cuh"
+#include "tg_internal.h"
+#include "tg_kepler.cuh"
+#include "tg_pn_terms.cuh"
+
+namespace tg {
+
+constexpr int F64_THREADS = 128;
+constexpr int F64_TILE = 64;
+
+// Plummer-softened 1/(r2+e2), zero when r2 > 0 fails (smoothing.h:10-67).
+__device__ __forceinline__ double soft_q2(double r2, double e2) {
+    double q = ddiv(1.0, dadd(r2, e2));
+    return (r2 > 0) ? q : 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Per-kernel pair functors.  `sj[f][jj]` is the staged j-tile.
+// ---------------------------------------------------------------------------
+struct Phi64 {
+    static constexpr int NF = 5, NO = 1;
+    struct St { double x, y, z, e, phi; };
+    __device__ static void init(St &s, const PairArgs &a, size_t i) {
+        s = {a.I.f[F_RX][i], a.I.f[F_RY][i], a.I.f[F_RZ][i], a.I.f[F_E2][i], 0.0};
+    }
+    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &) {
+        double dx = dsub(s.x, sj[F_RX][jj]), dy = dsub(s.y, sj[F_RY][jj]), dz = dsub(s.z, sj[F_RZ][jj]);
+        double e2 = dadd(s.e, sj[F_E2][jj]);
+        double r2 = ddot3(dx, dy, dz, dx, dy, dz);
+        double q1 = dsqrt(soft_q2(r2, e2));
+        s.phi = dsub(s.phi, dmul(sj[F_M][jj], q1));
+    }
+    __device__ static void store(const St &s, const PairArgs &a, size_t i) { a.out[0][i] = s.phi; }
+};
+
+struct Acc64 {
+    static constexpr int NF = 5, NO = 3;
+    struct St { double x, y, z, e, ax, ay, az; };
+    __device__ static void init(St &s, const PairArgs &a, size_t i) {
+        s = {a.I.f[F_RX][i], a.I.f[F_RY][i], a.I.f[F_RZ][i], a.I.f[F_E2][i], 0.0, 0.0, 0.0};
+    }
+    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &) {
+        double dx = dsub(s.x, sj[F_RX][jj]), dy = dsub(s.y, sj[F_RY][jj]), dz = dsub(s.z, sj[F_RZ][jj]);
+        double e2 = dadd(s.e, sj[F_E2][jj]);
+        double r2 = ddot3(dx, dy, dz, dx, dy, dz);
+        double q2 = soft_q2(r2, e2);
+        double q3 = dmul(dmul(q2, dsqrt(q2)), sj[F_M][jj]);
+        s.ax = dsub(s.ax, dmul(q3, dx));
+        s.ay = dsub(s.ay, dmul(q3, dy));
+        s.az = dsub(s.az, dmul(q3, dz));
+    }
+    __device__ static void store(const St &s, const PairArgs &a, size_t i) {
+        a.out[0][i] = s.ax; a.out[1][i] = s.ay; a.out[2][i] = s.az;
+    }
+};
+
+struct AccJerk64 {
+    static constexpr int NF = 8, NO = 6;
+    struct St { double x, y, z, e, u, v, w, a[3], j[3]; };
+    __device__ static void init(St &s, const PairArgs &a, size_t i) {
+        s.x = a.I.f[F_RX][i]; s.y = a.I.f[F_RY][i]; s.z = a.I.f[F_RZ][i]; s.e = a.I.f[F_E2][i];
+        s.u = a.I.f[F_VX][i]; s.v = a.I.f[F_VY][i]; s.w = a.I.f[F_VZ][i];
+        for (int k = 0; k < 3; ++k) { s.a[k] = 0.0; s.j[k] = 0.0; }
+    }
+    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &) {
+        double dx = dsub(s.x, sj[F_RX][jj]), dy = dsub(s.y, sj[F_RY][jj]), dz = dsub(s.z, sj[F_RZ][jj]);
+        double e2 = dadd(s.e, sj[F_E2][jj]);
+        double du = dsub(s.u, sj[F_VX][jj]), dv = dsub(s.v, sj[F_VY][jj]), dw = dsub(s.w, sj[F_VZ][jj]);
+        double r2 = ddot3(dx, dy, dz, dx, dy, dz);
+        double rv = ddot3(dx, dy, dz, du, dv, dw);
+        double q2 = soft_q2(r2, e2);
+        double q3 = dmul(q2, dsqrt(q2));
+        double al = dmul(dmul(3.0, rv), q2);
+        du = dsub(du, dmul(al, dx));
+        dv = dsub(dv, dmul(al, dy));
+        dw = dsub(dw, dmul(al, dz));
+        q3 = dmul(q3, sj[F_M][jj]);
+        s.a[0] = dsub(s.a[0], dmul(q3, dx)); s.a[1] = dsub(s.a[1], dmul(q3, dy)); s.a[2] = dsub(s.a[2], dmul(q3, dz));
+        s.j[0] = dsub(s.j[0], dmul(q3, du)); s.j[1] = dsub(s.j[1], dmul(q3, dv)); s.j[2] = dsub(s.j[2], dmul(q3, dw));
+    }
+    __device__ static void store(const St &s, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 3; ++k) { a.out[k][i] = s.a[k]; a.out[3 + k][i] = s.j[k]; }
+    }
+};
+
+struct SnapCrackle64 {
+    static constexpr int NF = 14, NO = 6;
+    struct St { double f[14]; double s[3], c[3]; };
+    __device__ static void init(St &s, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 14; ++k) s.f[k] = a.I.f[k][i];
+        for (int k = 0; k < 3; ++k) { s.s[k] = 0.0; s.c[k] = 0.0; }
+    }
+    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &) {
+        double r[3], v[3], A[3], J[3];
+        for (int k = 0; k < 3; ++k) {
+            r[k] = dsub(s.f[F_RX + k], sj[F_RX + k][jj]);
+            v[k] = dsub(s.f[F_VX + k], sj[F_VX + k][jj]);
+            A[k] = dsub(s.f[F_AX + k], sj[F_AX + k][jj]);
+            J[k] = dsub(s.f[F_JX + k], sj[F_JX + k][jj]);
+        }
+        double e2 = dadd(s.f[F_E2], sj[F_E2][jj]);
+        double r2 = ddot3(r[0], r[1], r[2], r[0], r[1], r[2]);
+        double rv = ddot3(r[0], r[1], r[2], v[0], v[1], v[2]);
+        double v2 = ddot3(v[0], v[1], v[2], v[0], v[1], v[2]);
+        double rJ = ddot3(r[0], r[1], r[2], J[0], J[1], J[2]);
+        double rA = ddot3(r[0], r[1], r[2], A[0], A[1], A[2]);
+        double vA = ddot3(v[0], v[1], v[2], A[0], A[1], A[2]);
+        double q2 = soft_q2(r2, e2);
+        double q3 = dmul(q2, dsqrt(q2));
+        double al = dmul(rv, q2);
+        double al2 = dmul(al, al);
+        double be = dmul(3.0, dadd(dmul(dadd(v2, rA), q2), al2));
+        double ga = dadd(dmul(dadd(dmul(3.0, vA), rJ), q2), dmul(al, dsub(be, dmul(4.0, al2))));
+        al = dmul(al, 3.0);
+        ga = dmul(ga, 3.0);
+        for (int k = 0; k < 3; ++k) v[k] = dsub(v[k], dmul(al, r[k]));
+        double two_al = dmul(2.0, al);
+        for (int k = 0; k < 3; ++k) A[k] = dsub(A[k], dadd(dmul(two_al, v[k]), dmul(be, r[k])));
+        al = dmul(al, 3.0);
+        be = dmul(be, 3.0);
+        for (int k = 0; k < 3; ++k)
+            J[k] = dsub(J[k], dadd(dadd(dmul(al, A[k]), dmul(be, v[k])), dmul(ga, r[k])));
+        q3 = dmul(q3, sj[F_M][jj]);
+        for (int k = 0; k < 3; ++k) {
+            s.s[k] = dsub(s.s[k], dmul(q3, A[k]));
+            s.c[k] = dsub(s.c[k], dmul(q3, J[k]));
+        }
+    }
+    __device__ static void store(const St &s, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 3; ++k) { a.out[k][i] = s.s[k]; a.out[3 + k][i] = s.c[k]; }
+    }
+};
+
+struct Tstep64 {
+    static constexpr int NF = 8, NO = 2;
+    struct St { double m, x, y, z, e, u, v, w, wsum, wmax; };
+    __device__ static void init(St &s, const PairArgs &a, size_t i) {
+        s.m = a.I.f[F_M][i]; s.x = a.I.f[F_RX][i]; s.y = a.I.f[F_RY][i]; s.z = a.I.f[F_RZ][i];
+        s.e = a.I.f[F_E2][i]; s.u = a.I.f[F_VX][i]; s.v = a.I.f[F_VY][i]; s.w = a.I.f[F_VZ][i];
+        s.wsum = 0.0; s.wmax = 0.0;
+    }
+    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a) {
+        double dx = dsub(s.x, sj[F_RX][jj]), dy = dsub(s.y, sj[F_RY][jj]), dz = dsub(s.z, sj[F_RZ][jj]);
+        double e2 = dadd(s.e, sj[F_E2][jj]);
+        double du = dsub(s.u, sj[F_VX][jj]), dv = dsub(s.v, sj[F_VY][jj]), dw = dsub(s.w, sj[F_VZ][jj]);
+        double m = dadd(s.m, sj[F_M][jj]);
+        double r2 = ddot3(dx, dy, dz, dx, dy, dz);
+        double rv = ddot3(dx, dy, dz, du, dv, dw);
+        double v2 = ddot3(du, dv, dw, du, dv, dw);
+        double q2 = soft_q2(r2, e2);
+        double q1 = dsqrt(q2);
+        double b = dmul(2.0, q2);             // (1 + a/2) inv_r2 with a = 2
+        double phi = dmul(m, q1);
+        double w2 = dmul(q2, dadd(v2, dmul(2.0, phi)));
+        double gam = dmul(q2, dadd(w2, dmul(b, phi)));
+        gam = dmul(gam, ddiv(a.eta, dsqrt(w2)));
+        w2 = dsub(w2, dmul(gam, rv));
+        if (!(r2 > 0)) w2 = 0.0;
+        s.wsum = dadd(s.wsum, w2);
+        s.wmax = fmax(w2, s.wmax);
+    }
+    __device__ static void store(const St &s, const PairArgs &a, size_t i) {
+        a.out[0][i] = ddiv(a.eta, dsqrt(dadd(1.0, s.wsum)));
+        a.out[1][i] = ddiv(a.eta, dsqrt(dadd(1.0, s.wmax)));
+    }
+};
+
+struct PNAcc64 {
+    static constexpr int NF = 8, NO = 3;
+    struct St { double m, x, y, z, e, u, v, w, iv2, a[3]; };
+    __device__ static void init(St &s, const PairArgs &a, size_t i) {
+        s.m = a.I.f[F_M][i]; s.x = a.I.f[F_RX][i]; s.y = a.I.f[F_RY][i]; s.z = a.I.f[F_RZ][i];
+        s.e = a.I.f[F_E2][i]; s.u = a.I.f[F_VX][i]; s.v = a.I.f[F_VY][i]; s.w = a.I.f[F_VZ][i];
+        s.iv2 = s.u * s.u + s.v * s.v + s.w * s.w;
+        s.a[0] = s.a[1] = s.a[2] = 0.0;
+    }
+    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a) {
+        double jm = sj[F_M][jj];
+        double ju = sj[F_VX][jj], jv = sj[F_VY][jj], jw = sj[F_VZ][jj];
+        double rx = s.x - sj[F_RX][jj], ry = s.y - sj[F_RY][jj], rz = s.z - sj[F_RZ][jj];
+        double e2 = s.e + sj[F_E2][jj];
+        double vx = s.u - ju, vy = s.v - jv, vz = s.w - jw;
+        double r2 = rx * rx + ry * ry + rz * rz;
+        double v2 = vx * vx + vy * vy + vz * vz;
+        double q2 = soft_q2(r2, e2);
+        double q1 = dsqrt(q2);
+        double q3 = q2 * q1;
+        double nx = rx * q1, ny = ry * q1, nz = rz * q1;
+        double jv2 = ju * ju + jv * jv + jw * jw;
+        double ivjv = s.u * ju + s.v * jv + s.w * jw;
+        double niv = nx * s.u + ny * s.v + nz * s.w;
+        double njv = nx * ju + ny * jv + nz * jw;
+        double nv = nx * vx + ny * vy + nz * vz;
+        double A, B;
+        pn_factors<double>(a.order, s.m, jm, q1, s.iv2, jv2, ivjv, niv, njv, nv, v2,
+                           a.inv[2], a.inv[4], a.inv[5], a.inv[6], a.inv[7], A, B);
+        A *= jm * q3;
+        B *= jm * q2;
+        s.a[0] += A * rx + B * vx;
+        s.a[1] += A * ry + B * vy;
+        s.a[2] += A * rz + B * vz;
+    }
+    __device__ static void store(const St &s, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 3; ++k) a.out[k][i] = s.a[k];
+    }
+};
+
+struct Sakura64 {
+    static constexpr int NF = 8, NO = 6;
+    struct St { double f[8]; double d[6]; unsigned flags; };
+    __device__ static void init(St &s, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 8; ++k) s.f[k] = a.I.f[k][i];
+        for (int k = 0; k < 6; ++k) s.d[k] = 0.0;
+        s.flags = 0;
+    }
+    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a) {
+        double r0[3], v0[3], r1[3], v1[3];
+        for (int k = 0; k < 3; ++k) {
+            r0[k] = dsub(s.f[F_RX + k], sj[F_RX + k][jj]);
+            v0[k] = dsub(s.f[F_VX + k], sj[F_VX + k][jj]);
+        }
+        double e2 = dadd(s.f[F_E2], sj[F_E2][jj]);
+        double m = dadd(s.f[F_M], sj[F_M][jj]);
+        KepBudget b;
+        pair_evolve(a.dt, a.flag, m, e2, r0, v0, r1, v1, b);
+        s.flags |= b.flags;
+        double w = ddiv(sj[F_M][jj], m);
+        for (int k = 0; k < 3; ++k) {
+            s.d[k] = dadd(s.d[k], dmul(w, dsub(r1[k], r0[k])));
+            s.d[3 + k] = dadd(s.d[3 + k], dmul(w, dsub(v1[k], v0[k])));
+        }
+    }
+    __device__ static void store(const St &s, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 6; ++k) a.out[k][i] = s.d[k];
+        if (s.flags) atomicOr(a.status, s.flags);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Generic sequential-j engine.
+// ---------------------------------------------------------------------------
+template <class K>
+__global__ void __launch_bounds__(F64_THREADS) fp64_pairwise(PairArgs a) {
+    __shared__ double sj[K::NF][F64_TILE];
+    const size_t i = (size_t)blockIdx.x * F64_THREADS + threadIdx.x;
+    const bool live = i < a.ni;
+    typename K::St st;
+    K::init(st, a, live ? i : 0);
+    for (size_t j0 = 0; j0 < a.nj; j0 += F64_TILE) {
+        const int nt = (int)((a.nj - j0) < (size_t)F64_TILE ? (a.nj - j0) : F64_TILE);
+        for (int q = threadIdx.x; q < K::NF * F64_TILE; q += F64_THREADS) {
+            const int f = q / F64_TILE, jj = q % F64_TILE;
+            if (jj < nt) sj[f][jj] = a.J.f[f][j0 + jj];
+        }
+        __syncthreads();
+        for (int jj = 0; jj < nt; ++jj) K::pair(st, sj, jj, a);
+        __syncthreads();
+    }
+    if (live) K::store(st, a, i);
+}
+
+template <class K>
+static cudaError_t run(const PairArgs &a, cudaStream_t s) {
+    const size_t blocks = (a.ni + F64_THREADS - 1) / F64_THREADS;
+    fp64_pairwise<K><<<(unsigned)blocks, F64_THREADS, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fp64(int kernel, const PairArgs &a, cudaStream_t s) {
+    switch (kernel) {
+        case K_PHI: return run<Phi64>(a, s);
+        case K_ACC: return run<Acc64>(a, s);
+        case K_ACC_JERK: return run<AccJerk64>(a, s);
+        case K_SNAP_CRACKLE: return run<SnapCrackle64>(a, s);
+        case K_TSTEP: return run<Tstep64>(a, s);
+        case K_PNACC: return run<PNAcc64>(a, s);
+        case K_SAKURA: return run<Sakura64>(a, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace tg

@@ -1,0 +1,55 @@
+// tg_internal.h -- declarations shared by the library's translation units.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tg {
+
+// Particle attributes in the order of tupan/particles/body.py:26-39 plus the
+// derivative fields the SnapCrackle kernel reads (extensions.py:290-300).
+enum Field : int {
+    F_M = 0, F_RX, F_RY, F_RZ, F_E2, F_VX, F_VY, F_VZ,
+    F_AX, F_AY, F_AZ, F_JX, F_JY, F_JZ, F_COUNT
+};
+
+enum Kernel : int { K_PHI = 0, K_ACC, K_ACC_JERK, K_SNAP_CRACKLE, K_TSTEP, K_PNACC, K_SAKURA, K_COUNT };
+
+// Number of per-particle input fields each kernel reads (libtupan.h:2-246).
+constexpr int kernel_fields(int k) {
+    return k == K_PHI || k == K_ACC ? 5 : (k == K_SNAP_CRACKLE ? 14 : 8);
+}
+// Number of output arrays.
+constexpr int kernel_outputs(int k) {
+    return k == K_PHI ? 1 : (k == K_ACC || k == K_PNACC ? 3 : (k == K_TSTEP ? 2 : 6));
+}
+
+struct PSet {
+    const double *f[F_COUNT];
+};
+
+struct PairArgs {
+    PSet I, J;
+    size_t ni, nj;
+    double *out[6];
+    double eta;               // Tstep
+    double dt;                // Sakura
+    long long flag;           // Sakura
+    unsigned long order;      // PNAcc
+    double inv[8];            // PNAcc: inv[k] = 1/c^k
+    unsigned *status;         // device status word (tg::ST_* bits)
+};
+
+// Launchers (stream-ordered, asynchronous).  Return a cudaError_t.
+cudaError_t launch_fp64(int kernel, const PairArgs &a, cudaStream_t s);
+
+// Split-FP32 path: packs j-records into `ws` and runs the stream-K kernel.
+struct Ds32Plan {
+    size_t ws_bytes;
+};
+size_t ds32_workspace_bytes(int kernel, size_t ni, size_t nj, int sms);
+cudaError_t launch_ds32(int kernel, const PairArgs &a, void *ws, size_t ws_bytes, int sms,
+                        cudaStream_t s);
+bool ds32_supported(int kernel);
+
+}  // namespace tg

@@ -1,0 +1,80 @@
+// tg_probe.cu -- issue-rate probes that measure this GPU's FP32 and FP64
+// FMA peaks, the denominators of the pairwise kernels' roofline.
+//
+// Each thread runs NCHAIN independent FMA chains for `iters` rounds; the
+// grid is SMs x 8 CTAs of 256 threads.  The FP32 probe uses packed FFMA2 (two
+// FMAs per instruction, so the FMA pipe rather than instruction issue is the
+// limit).  Seconds come from CUDA events on the caller's stream.
+#include <cuda_runtime.h>
+
+#include "../../include/tupan_gb300.h"
+
+namespace {
+
+constexpr int NCHAIN = 8;
+
+__global__ void probe_fp32(float *sink, int iters, float a, float b) {
+    float2 acc[NCHAIN];
+    for (int k = 0; k < NCHAIN; ++k) acc[k] = make_float2(threadIdx.x * 1e-7f + k, k * 1e-3f);
+    const float2 va = make_float2(a, a), vb = make_float2(b, b);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int k = 0; k < NCHAIN; ++k) acc[k] = __ffma2_rn(acc[k], va, vb);
+    }
+    float s = 0.f;
+    for (int k = 0; k < NCHAIN; ++k) s += acc[k].x + acc[k].y;
+    if (s == 12345.678f) sink[blockIdx.x] = s;   // keeps the chains alive
+}
+
+__global__ void probe_fp64(double *sink, int iters, double a, double b) {
+    double acc[NCHAIN];
+    for (int k = 0; k < NCHAIN; ++k) acc[k] = threadIdx.x * 1e-7 + k;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int k = 0; k < NCHAIN; ++k) acc[k] = fma(acc[k], a, b);
+    }
+    double s = 0.0;
+    for (int k = 0; k < NCHAIN; ++k) s += acc[k];
+    if (s == 12345.678) sink[blockIdx.x] = s;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Measured dense FMA throughput in TFLOP/s (2 flops per FMA) for FP32
+// (which = 0) or FP64 (which = 1) on the current device; negative on error.
+double tg_probe_fma_tflops(int which, int iters, void *stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1.0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1.0;
+    const int blocks = sms * 8, threads = 256;
+    void *sink = nullptr;
+    if (cudaMalloc(&sink, blocks * sizeof(double)) != cudaSuccess) return -1.0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    double best = 0.0;
+    for (int rep = 0; rep < 4; ++rep) {
+        cudaEventRecord(e0, s);
+        if (which == 0)
+            probe_fp32<<<blocks, threads, 0, s>>>(static_cast<float *>(sink), iters, 0.999999f, 1e-6f);
+        else
+            probe_fp64<<<blocks, threads, 0, s>>>(static_cast<double *>(sink), iters, 0.999999, 1e-6);
+        cudaEventRecord(e1, s);
+        if (cudaEventSynchronize(e1) != cudaSuccess) { best = -1.0; break; }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double fmas = (double)blocks * threads * iters * NCHAIN * (which == 0 ? 2.0 : 1.0);
+        const double tf = 2.0 * fmas / (ms * 1e-3) / 1e12;
+        if (rep > 0 && tf > best) best = tf;   // first launch is warm-up
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    if (cudaGetLastError() != cudaSuccess) return -1.0;
+    return best;
+}
+
+}  // extern "C"

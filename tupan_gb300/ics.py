@@ -1,0 +1,121 @@
+"""Initial conditions: Plummer spheres, a Salpeter mass function and binaries.
+
+Restates the generators of tupan/ics/plummer.py:21-221 (Plummer.set_pos:
+mass-stratified radii r = (m^(-2/3) - 1)^(-1/2) with mfrac = 0.999;
+set_vel: |v| = sqrt(-2 q phi) with q drawn from the triangular density
+2(1 - q) by pairwise rejection; per-particle eps2 = eps^2 / 2 for constant
+softening; then com_to_origin, to_nbody_units and scale_to_virial) and of
+tupan/ics/fewbody.py:13-50 (a two-body orbit of given a, e).  The potential
+used for the velocities and the unit scalings comes from the GPU Phi kernel.
+Random numbers come from numpy.random.Generator(PCG64(seed)).
+
+The Salpeter IMF draws dN/dm ~ m^-2.35 on [mlow, mhigh] by inverse CDF; the
+reference's IMF class refuses mlow < 0.4 (ics/imf.py:85-88), so this one is
+used for the [0.1, 100] range of the precision workload.
+"""
+import numpy as np
+import torch
+
+from .particles import ParticleSystem
+
+
+class Salpeter(object):
+    def __init__(self, mlow=0.1, mhigh=100.0, alpha=-2.35):
+        self.mlow, self.mhigh, self.alpha = float(mlow), float(mhigh), float(alpha)
+
+    def sample(self, n, rng):
+        a = self.alpha + 1.0
+        u = rng.random(n)
+        lo, hi = self.mlow ** a, self.mhigh ** a
+        return (lo + u * (hi - lo)) ** (1.0 / a)
+
+
+class EqualMass(object):
+    def sample(self, n, rng):
+        return np.ones(n)
+
+
+def plummer_positions(n, rng, mfrac=0.999):
+    irand = rng.permutation(n)
+    mrand = (irand + rng.random(n)) * mfrac / n
+    radius = 1.0 / np.sqrt(np.power(mrand, -2.0 / 3.0) - 1.0)
+    theta = np.arccos(rng.uniform(-1.0, 1.0, size=n))
+    phi = rng.uniform(0.0, 2.0 * np.pi, size=n)
+    return (radius * np.sin(theta) * np.cos(phi), radius * np.sin(theta) * np.sin(phi),
+            radius * np.cos(theta))
+
+
+def triangular(n, rng):
+    """q with density 2(1 - q) on [0, 1]: keep r2 when r2 < r1."""
+    out = np.empty(0)
+    while out.size < n:
+        r1 = rng.random(2 * n)
+        r2 = rng.random(2 * n)
+        out = np.concatenate([out, r2[r2 < r1]])
+    return out[:n]
+
+
+def make_plummer(n, eps, imf=None, seed=0, device=None, prec="float64"):
+    """Plummer sphere in N-body (Henon) units: M = 1, E = -1/4, Q = 1/2."""
+    from .lib import extensions
+    rng = np.random.default_rng(seed)
+    imf = imf or EqualMass()
+    mass = imf.sample(n, rng)
+    mass = mass / mass.sum()
+    ps = ParticleSystem(n, device=device)
+    ps.set_array("mass", mass)
+    ps.set_array("eps2", np.full(n, eps * eps / 2.0))
+    rx, ry, rz = plummer_positions(n, rng)
+    ps.set_array("rx", rx); ps.set_array("ry", ry); ps.set_array("rz", rz)
+    extensions.Phi("CUDA", prec).calc(ps, ps)
+    q = triangular(n, rng)
+    v = np.sqrt(-2.0 * q * ps.phi.cpu().numpy())
+    theta = np.arccos(rng.uniform(-1.0, 1.0, size=n))
+    phi = rng.uniform(0.0, 2.0 * np.pi, size=n)
+    ps.set_array("vx", v * np.sin(theta) * np.cos(phi))
+    ps.set_array("vy", v * np.sin(theta) * np.sin(phi))
+    ps.set_array("vz", v * np.cos(theta))
+    ps.com_to_origin()
+    ps.to_nbody_units()
+    ps.scale_to_virial()
+    return ps
+
+
+def make_binary(m1, m2, a, e, rng=None):
+    """Relative orbit at pericentre, c.o.m. at rest (fewbody.py:13-50)."""
+    m = m1 + m2
+    rp = a * (1 - e)
+    vp = np.sqrt(m * (1 + e) / rp)
+    r = np.array([[m2 / m * rp, 0, 0], [-m1 / m * rp, 0, 0]])
+    v = np.array([[0, m2 / m * vp, 0], [0, -m1 / m * vp, 0]])
+    if rng is not None:   # random orientation
+        q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        r, v = r @ q.T, v @ q.T
+    return np.array([m1, m2]), r, v
+
+
+def plummer_arrays(n, eps, imf=None, seed=0, mfrac=0.999):
+    """Host-only Plummer sphere (numpy arrays) for benchmarks and CPU tests.
+
+    Same sampling as make_plummer, but the potential used for the velocity
+    magnitudes is the smooth Plummer potential -1/sqrt(1 + r^2) and the
+    scaling to Henon units is the analytic one (length 3 pi / 16, velocity
+    its inverse square root), so no O(N^2) pass is needed.
+    """
+    rng = np.random.default_rng(seed)
+    imf = imf or EqualMass()
+    mass = imf.sample(n, rng)
+    mass = mass / mass.sum()
+    rx, ry, rz = plummer_positions(n, rng, mfrac)
+    pot = -1.0 / np.sqrt(1.0 + rx * rx + ry * ry + rz * rz)
+    q = triangular(n, rng)
+    v = np.sqrt(-2.0 * q * pot)
+    theta = np.arccos(rng.uniform(-1.0, 1.0, size=n))
+    ph = rng.uniform(0.0, 2.0 * np.pi, size=n)
+    vx, vy, vz = v * np.sin(theta) * np.cos(ph), v * np.sin(theta) * np.sin(ph), v * np.cos(theta)
+    s = 3.0 * np.pi / 16.0
+    d = {"mass": mass, "eps2": np.full(n, eps * eps / 2.0)}
+    for k, (r, u) in zip("xyz", ((rx, vx), (ry, vy), (rz, vz))):
+        d["r" + k] = (r - np.dot(mass, r)) * s
+        d["v" + k] = (u - np.dot(mass, u)) / np.sqrt(s)
+    return d
