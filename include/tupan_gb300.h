@@ -49,7 +49,6 @@ extern "C" {
 /* status bits returned by tg_sync_status() */
 #define TG_ST_MBAR_TIMEOUT 1u   /* a bounded shared-memory pipeline wait gave up */
 #define TG_ST_KEPLER_CAP 2u     /* Sakura: Kepler retry bound reached, last iterate kept */
-#define TG_ST_LAGUERRE_CAP 4u   /* Sakura: Laguerre iteration bound (64) reached */
 
 /* ---------------------------------------------------------------------- */
 /* Library state                                                           */

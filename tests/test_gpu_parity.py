@@ -37,7 +37,11 @@ def ext():
 
 
 class PS(object):
-    """Minimal particle set over CUDA tensors (reference attribute names)."""
+    """Minimal particle set over CUDA tensors (reference attribute names).
+
+    Acc/AccJerk write their outputs into the `ax`.. `jz` attributes, which are
+    also SnapCrackle inputs (as in the reference); tests therefore build a
+    fresh set for every call so each kernel sees the fixture's inputs."""
 
     def __init__(self, d):
         self.n = len(d["mass"])
@@ -93,9 +97,9 @@ def rel_err(name, got, want):
 @pytest.mark.parametrize("case", CASES)
 def test_fp64_matches_golden(ext, case):
     z, ps, calls = load(case)
-    P = PS(ps)
     for key, name, sc in calls:
         sc = typed_scalars(name, sc)
+        P = PS(ps)
         got = run_kernel(ext, name, "float64", P, P, sc)
         assert_fp64(name, got, z["out_" + key])
 
@@ -103,25 +107,25 @@ def test_fp64_matches_golden(ext, case):
 def test_fp64_prefix_sweeps(ext):
     """i=all vs j=prefix and i=prefix vs j=all (test_extensions.py:45-85)."""
     z, ps, calls = load("sweep")
-    P = PS(ps)
     for key, name, sc in calls:
         if name == "sakura":
             continue
         sc = typed_scalars(name, sc)
         for p in PREFIXES:
-            S = PS({f: ps[f][:p] for f in FIELDS})
+            P, S = PS(ps), PS({f: ps[f][:p] for f in FIELDS})
             assert_fp64(name, run_kernel(ext, name, "float64", P, S, sc), z["outJ%d_" % p + key])
+            P, S = PS(ps), PS({f: ps[f][:p] for f in FIELDS})
             assert_fp64(name, run_kernel(ext, name, "float64", S, P, sc), z["outI%d_" % p + key])
 
 
 @pytest.mark.parametrize("case", ["plummer", "binary", "sweep"])
 def test_ds32_against_golden(ext, case):
     z, ps, calls = load(case)
-    P = PS(ps)
     for key, name, sc in calls:
         if name == "sakura":
             continue
         sc = typed_scalars(name, sc)
+        P = PS(ps)
         got = run_kernel(ext, name, "ds32", P, P, sc)
         err = rel_err(name, got, z["out_" + key])
         assert err <= DS32_TOL[name], "%s %s ds32 error %.3e" % (case, name, err)
@@ -129,15 +133,15 @@ def test_ds32_against_golden(ext, case):
 
 def test_ds32_prefix_sweeps(ext):
     z, ps, calls = load("sweep")
-    P = PS(ps)
     for key, name, sc in calls:
         if name == "sakura":
             continue
         sc = typed_scalars(name, sc)
         for p in PREFIXES:
-            S = PS({f: ps[f][:p] for f in FIELDS})
+            P, S = PS(ps), PS({f: ps[f][:p] for f in FIELDS})
             err = rel_err(name, run_kernel(ext, name, "ds32", P, S, sc), z["outJ%d_" % p + key])
             assert err <= DS32_TOL[name], (name, p, err)
+            P, S = PS(ps), PS({f: ps[f][:p] for f in FIELDS})
             err = rel_err(name, run_kernel(ext, name, "ds32", S, P, sc), z["outI%d_" % p + key])
             assert err <= DS32_TOL[name], (name, p, err)
 
@@ -173,7 +177,8 @@ def test_streamk_shapes_ds32_vs_oracle(ext, orc, ni, nj):
     d = plummer(max(ni, nj), seed=ni * 7 + nj)
     I = {f: d[f][:ni] for f in FIELDS}
     J = {f: d[f][-nj:] for f in FIELDS}
-    for name, sc in [("acc", ()), ("acc_jerk", ()), ("phi", ()), ("tstep", (0.01,))]:
+    for name, sc in [("acc", ()), ("acc_jerk", ()), ("phi", ()), ("tstep", (0.01,)),
+                     ("snap_crackle", ())]:
         want = np.stack(orc.calc(name, I, J, *sc, nthreads=4))
         got = run_kernel(ext, name, "ds32", PS(I), PS(J), sc)
         assert rel_err(name, got, want) <= DS32_TOL[name], (name, ni, nj)

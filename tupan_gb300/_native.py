@@ -21,7 +21,6 @@ ENODEV = -4
 
 ST_MBAR_TIMEOUT = 1
 ST_KEPLER_CAP = 2
-ST_LAGUERRE_CAP = 4
 
 P5 = ("mass", "rx", "ry", "rz", "eps2")
 P8 = P5 + ("vx", "vy", "vz")

@@ -18,7 +18,6 @@ namespace tg {
 enum : unsigned {
     ST_MBAR_TIMEOUT = 1u << 0,   // a bounded mbarrier wait gave up
     ST_KEPLER_CAP = 1u << 1,     // Sakura: Kepler retry cap reached
-    ST_LAGUERRE_CAP = 1u << 2,   // Sakura: Laguerre iteration cap reached
 };
 
 // ---------------------------------------------------------------------------

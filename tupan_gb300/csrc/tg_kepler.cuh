@@ -96,7 +96,7 @@ __device__ int kep_laguerre(double s0, double &s, const KepEq &k, KepBudget &b) 
         step = ddiv(-g, h);
         x = dadd(x, step);
         it += 1;
-        if (it > KEP_MAXITER) { s = x; b.flags |= ST_LAGUERRE_CAP; return -2; }
+        if (it > KEP_MAXITER) { s = x; return -2; }   // caller halves the step
     } while (fabs(step) > KEP_TOL);
     s = x;
     if (ksign(x) != ksign(s0)) return -3;
