@@ -66,7 +66,8 @@ int tg_get_host_precision(void);
 int tg_device_sms(void);
 /* Measurement helper with no counterpart in the reference: dense FMA issue
  * probe on the current device, returning TFLOP/s (2 flops per FMA) for FP32
- * (which = 0, packed FFMA2) or FP64 (which = 1); negative on error.  It is
+ * (which = 0, packed FFMA2), FP64 (which = 1) or packed FFMA2 interleaved
+ * with scalar FFMA (which = 2); negative on error.  It is
  * the measured denominator of the pairwise kernels' FP32 roofline. */
 double tg_probe_fma_tflops(int which, int iters, void *stream);
 

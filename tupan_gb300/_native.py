@@ -8,7 +8,7 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_lib", "libtupan_gb300.so")
+LIB_PATH = os.environ.get("TUPAN_GB300_LIB") or os.path.join(HERE, "_lib", "libtupan_gb300.so")
 
 PREC_FP64 = 0
 PREC_DS32 = 1

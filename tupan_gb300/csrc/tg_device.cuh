@@ -58,10 +58,13 @@ __device__ __forceinline__ float rsqrt_hw(float s) {
 }
 
 // Pair exclusion: lane is kept when r != 0, i.e. any of dx, dy, dz is
-// nonzero (exact differences of equal coordinates are +0).  Equivalent to
-// the reference's `r2 > 0` except for |dr| below 1e-19 where r2 underflows.
+// nonzero.  The split-FP32 kernels store every coordinate with -0 turned
+// into +0, so the difference of two equal coordinates is +0 (all bits zero)
+// and a nonzero difference is never -0; one 3-input OR then decides.
+// Equivalent to the reference's `r2 > 0` except for |dr| below 1e-19, where
+// the FP32 square underflows.
 __device__ __forceinline__ bool nonzero3(float a, float b, float c) {
-    return ((__float_as_uint(a) | __float_as_uint(b) | __float_as_uint(c)) << 1) != 0u;
+    return (__float_as_uint(a) | __float_as_uint(b) | __float_as_uint(c)) != 0u;
 }
 
 // ---------------------------------------------------------------------------

@@ -49,7 +49,7 @@ enum RecField {
 struct DsArgs {
     PairArgs p;
     const float4 *rec;   // packed j-records
-    double *part;        // [gridDim.x][2][NP][DS_THREADS]
+    double *part;        // [gridDim.x][2][IPT][NP][DS_THREADS]
     int *ticket;         // [NIT]
     long long nit, njt;  // i-tiles, j-tiles
 };
@@ -137,146 +137,136 @@ __device__ __forceinline__ float2 lo2(float4 q) { return make_float2(q.x, q.y); 
 __device__ __forceinline__ float2 hi2(float4 q) { return make_float2(q.z, q.w); }
 
 // ---------------------------------------------------------------------------
-// Kernels.  Each provides:
-//   JF, NQ (float4 per record pair), NO (outputs), NP (FP64 partials per i)
-//   St: per-thread state;  init(St&, args, i)
-//   step(St&, const float4* rec)   -- one record (two j)
-//   fold(St&)                      -- fold FP32 slots into compensated sums
-//   partials(const St&, double*)   -- per-thread FP64 partial values
-//   combine(double* acc, const double* p)  -- acc (+)= p
-//   store(const double* p, args, i)        -- final outputs from partials
-//   reset(St&)                     -- clear accumulators for a new i-tile
+// Kernels.  Each provides, for IPT i-particles per thread:
+//   IPT, JF (floats per j), NQ (float4 per record), NP (FP64 partials per i)
+//   IS                          per-i state (position, sums)
+//   load(IS&, args, i)          read and split one i-particle, clear sums
+//   step(IS (&)[IPT], rec)      one record (two j) against the IPT i-particles
+//   fold(IS&)                   fold the FP32 lane sums into compensated sums
+//   partials(const IS&, double*), combine(double*, const double*)
+//   store(const double*, args, i)   final outputs from the FP64 partials
+//   pack()                      j-record field list
 // ---------------------------------------------------------------------------
-template <bool REFINE>
+template <int IPT_, bool REFINE>
 struct AccDS {
-    static constexpr int JF = 8, NQ = 4, NO = 3, NP = 3, KID = K_ACC;
-    struct St { IPos q; float2 e; float2 a[3]; Comp c[3]; };
-    __device__ static void reset(St &s) {
-        for (int k = 0; k < 3; ++k) { s.a[k] = f2(0.f); s.c[k] = Comp{0.f, 0.f}; }
-    }
-    __device__ static void init(St &s, const PairArgs &a, size_t i) {
+    static constexpr int IPT = IPT_, JF = 8, NQ = 4, NP = 3;
+    struct IS { IPos q; float2 e; float2 a[3]; Comp c[3]; };
+    __device__ static void load(IS &s, const PairArgs &a, size_t i) {
         load_pos(a, i, s.q);
         s.e = f2(__double2float_rn(a.I.f[F_E2][i]));
-        reset(s);
+        for (int k = 0; k < 3; ++k) { s.a[k] = f2(0.f); s.c[k] = Comp{0.f, 0.f}; }
     }
-    // record: q0 = {xh, yh}, q1 = {zh, xl}, q2 = {yl, zl}, q3 = {m, e2}
-    __device__ __forceinline__ static void step(St &s, const float4 *R) {
+    // record: {xh,yh} {zh,xl} {yl,zl} {m,e2}
+    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R) {
         const float4 q0 = R[0], q1 = R[1], q2 = R[2], q3 = R[3];
-        float2 dx, dy, dz;
-        pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), dx, dy, dz);
-        const float2 e2 = add2(s.e, hi2(q3));
-        const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
-        const float2 y = inv_r<REFINE>(ss, dx, dy, dz);
-        const float2 y2 = mul2(y, y);
-        const float2 mr3 = mul2(mul2(lo2(q3), y), y2);
-        s.a[0] = fnma2(mr3, dx, s.a[0]);
-        s.a[1] = fnma2(mr3, dy, s.a[1]);
-        s.a[2] = fnma2(mr3, dz, s.a[2]);
-    }
-    __device__ static void fold(St &s) {
-        for (int k = 0; k < 3; ++k) {
-            comp_add(s.c[k], __fadd_rn(s.a[k].x, s.a[k].y));
-            s.a[k] = f2(0.f);
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+            IS &s = S[u];
+            float2 dx, dy, dz;
+            pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), dx, dy, dz);
+            const float2 e2 = add2(s.e, hi2(q3));
+            const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
+            const float2 y = inv_r<REFINE>(ss, dx, dy, dz);
+            const float2 y2 = mul2(y, y);
+            const float2 mr3 = mul2(mul2(lo2(q3), y), y2);
+            s.a[0] = fnma2(mr3, dx, s.a[0]);
+            s.a[1] = fnma2(mr3, dy, s.a[1]);
+            s.a[2] = fnma2(mr3, dz, s.a[2]);
         }
     }
-    __device__ static void partials(const St &s, double *p) {
-        for (int k = 0; k < 3; ++k) p[k] = comp_value(s.c[k]);
+    __device__ static void fold(IS &s) {
+        for (int k = 0; k < 3; ++k) { comp_add(s.c[k], __fadd_rn(s.a[k].x, s.a[k].y)); s.a[k] = f2(0.f); }
     }
-    __device__ static void combine(double *acc, const double *p) {
-        for (int k = 0; k < 3; ++k) acc[k] += p[k];
-    }
+    __device__ static void partials(const IS &s, double *p) { for (int k = 0; k < 3; ++k) p[k] = comp_value(s.c[k]); }
+    __device__ static void combine(double *acc, const double *p) { for (int k = 0; k < 3; ++k) acc[k] += p[k]; }
     __device__ static void store(const double *p, const PairArgs &a, size_t i) {
         for (int k = 0; k < 3; ++k) a.out[k][i] = p[k];
     }
     static PackSpec pack() { return PackSpec{8, 2, {F_M, F_E2}}; }
 };
 
-template <bool REFINE>
+template <int IPT_, bool REFINE>
 struct PhiDS {
-    static constexpr int JF = 8, NQ = 4, NO = 1, NP = 1, KID = K_PHI;
-    struct St { IPos q; float2 e; float2 p; Comp c; };
-    __device__ static void reset(St &s) { s.p = f2(0.f); s.c = Comp{0.f, 0.f}; }
-    __device__ static void init(St &s, const PairArgs &a, size_t i) {
+    static constexpr int IPT = IPT_, JF = 8, NQ = 4, NP = 1;
+    struct IS { IPos q; float2 e; float2 p; Comp c; };
+    __device__ static void load(IS &s, const PairArgs &a, size_t i) {
         load_pos(a, i, s.q);
         s.e = f2(__double2float_rn(a.I.f[F_E2][i]));
-        reset(s);
+        s.p = f2(0.f); s.c = Comp{0.f, 0.f};
     }
-    __device__ __forceinline__ static void step(St &s, const float4 *R) {
+    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R) {
         const float4 q0 = R[0], q1 = R[1], q2 = R[2], q3 = R[3];
-        float2 dx, dy, dz;
-        pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), dx, dy, dz);
-        const float2 e2 = add2(s.e, hi2(q3));
-        const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
-        const float2 y = inv_r<REFINE>(ss, dx, dy, dz);
-        s.p = fnma2(lo2(q3), y, s.p);
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+            IS &s = S[u];
+            float2 dx, dy, dz;
+            pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), dx, dy, dz);
+            const float2 e2 = add2(s.e, hi2(q3));
+            const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
+            const float2 y = inv_r<REFINE>(ss, dx, dy, dz);
+            s.p = fnma2(lo2(q3), y, s.p);
+        }
     }
-    __device__ static void fold(St &s) { comp_add(s.c, __fadd_rn(s.p.x, s.p.y)); s.p = f2(0.f); }
-    __device__ static void partials(const St &s, double *p) { p[0] = comp_value(s.c); }
+    __device__ static void fold(IS &s) { comp_add(s.c, __fadd_rn(s.p.x, s.p.y)); s.p = f2(0.f); }
+    __device__ static void partials(const IS &s, double *p) { p[0] = comp_value(s.c); }
     __device__ static void combine(double *acc, const double *p) { acc[0] += p[0]; }
     __device__ static void store(const double *p, const PairArgs &a, size_t i) { a.out[0][i] = p[0]; }
     static PackSpec pack() { return PackSpec{8, 2, {F_M, F_E2}}; }
 };
 
-template <bool REFINE>
+template <int IPT_, bool REFINE>
 struct AccJerkDS {
-    static constexpr int JF = 12, NQ = 6, NO = 6, NP = 6, KID = K_ACC_JERK;
-    struct St { IPos q; float2 u, v, w, e; float2 a[6]; Comp c[6]; };
-    __device__ static void reset(St &s) {
-        for (int k = 0; k < 6; ++k) { s.a[k] = f2(0.f); s.c[k] = Comp{0.f, 0.f}; }
-    }
-    __device__ static void init(St &s, const PairArgs &a, size_t i) {
+    static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 6;
+    struct IS { IPos q; float2 u, v, w, e; float2 a[6]; Comp c[6]; };
+    __device__ static void load(IS &s, const PairArgs &a, size_t i) {
         load_pos(a, i, s.q);
         s.u = f2(__double2float_rn(a.I.f[F_VX][i]));
         s.v = f2(__double2float_rn(a.I.f[F_VY][i]));
         s.w = f2(__double2float_rn(a.I.f[F_VZ][i]));
         s.e = f2(__double2float_rn(a.I.f[F_E2][i]));
-        reset(s);
+        for (int k = 0; k < 6; ++k) { s.a[k] = f2(0.f); s.c[k] = Comp{0.f, 0.f}; }
     }
     // record: {xh,yh} {zh,xl} {yl,zl} {vx,vy} {vz,m} {e2,pad}
-    __device__ __forceinline__ static void step(St &s, const float4 *R) {
+    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R) {
         const float4 q0 = R[0], q1 = R[1], q2 = R[2], q3 = R[3], q4 = R[4], q5 = R[5];
-        float2 dx, dy, dz;
-        pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), dx, dy, dz);
-        const float2 du = sub2(s.u, lo2(q3)), dv = sub2(s.v, hi2(q3)), dw = sub2(s.w, lo2(q4));
-        const float2 e2 = add2(s.e, lo2(q5));
-        const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
-        const float2 y = inv_r<REFINE>(ss, dx, dy, dz);
-        const float2 y2 = mul2(y, y);
-        const float2 mr3 = mul2(mul2(hi2(q4), y), y2);
-        const float2 rv = fma2(dx, du, fma2(dy, dv, mul2(dz, dw)));
-        const float2 al = mul2(mul2(rv, y2), f2(3.0f));
-        const float2 tu = fnma2(al, dx, du), tv = fnma2(al, dy, dv), tw = fnma2(al, dz, dw);
-        s.a[0] = fnma2(mr3, dx, s.a[0]);
-        s.a[1] = fnma2(mr3, dy, s.a[1]);
-        s.a[2] = fnma2(mr3, dz, s.a[2]);
-        s.a[3] = fnma2(mr3, tu, s.a[3]);
-        s.a[4] = fnma2(mr3, tv, s.a[4]);
-        s.a[5] = fnma2(mr3, tw, s.a[5]);
-    }
-    __device__ static void fold(St &s) {
-        for (int k = 0; k < 6; ++k) {
-            comp_add(s.c[k], __fadd_rn(s.a[k].x, s.a[k].y));
-            s.a[k] = f2(0.f);
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+            IS &s = S[u];
+            float2 dx, dy, dz;
+            pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), dx, dy, dz);
+            const float2 du = sub2(s.u, lo2(q3)), dv = sub2(s.v, hi2(q3)), dw = sub2(s.w, lo2(q4));
+            const float2 e2 = add2(s.e, lo2(q5));
+            const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
+            const float2 y = inv_r<REFINE>(ss, dx, dy, dz);
+            const float2 y2 = mul2(y, y);
+            const float2 mr3 = mul2(mul2(hi2(q4), y), y2);
+            const float2 rv = fma2(dx, du, fma2(dy, dv, mul2(dz, dw)));
+            const float2 al = mul2(mul2(rv, y2), f2(3.0f));
+            const float2 tu = fnma2(al, dx, du), tv = fnma2(al, dy, dv), tw = fnma2(al, dz, dw);
+            s.a[0] = fnma2(mr3, dx, s.a[0]);
+            s.a[1] = fnma2(mr3, dy, s.a[1]);
+            s.a[2] = fnma2(mr3, dz, s.a[2]);
+            s.a[3] = fnma2(mr3, tu, s.a[3]);
+            s.a[4] = fnma2(mr3, tv, s.a[4]);
+            s.a[5] = fnma2(mr3, tw, s.a[5]);
         }
     }
-    __device__ static void partials(const St &s, double *p) {
-        for (int k = 0; k < 6; ++k) p[k] = comp_value(s.c[k]);
+    __device__ static void fold(IS &s) {
+        for (int k = 0; k < 6; ++k) { comp_add(s.c[k], __fadd_rn(s.a[k].x, s.a[k].y)); s.a[k] = f2(0.f); }
     }
-    __device__ static void combine(double *acc, const double *p) {
-        for (int k = 0; k < 6; ++k) acc[k] += p[k];
-    }
+    __device__ static void partials(const IS &s, double *p) { for (int k = 0; k < 6; ++k) p[k] = comp_value(s.c[k]); }
+    __device__ static void combine(double *acc, const double *p) { for (int k = 0; k < 6; ++k) acc[k] += p[k]; }
     __device__ static void store(const double *p, const PairArgs &a, size_t i) {
         for (int k = 0; k < 6; ++k) a.out[k][i] = p[k];
     }
     static PackSpec pack() { return PackSpec{12, 6, {F_VX, F_VY, F_VZ, F_M, F_E2, -2}}; }
 };
 
-template <bool REFINE>
+template <int IPT_, bool REFINE>
 struct TstepDS {
-    static constexpr int JF = 12, NQ = 6, NO = 2, NP = 2, KID = K_TSTEP;
-    struct St { IPos q; float2 u, v, w, e, m; float eta; float2 ws; float wmax; Comp c; };
-    __device__ static void reset(St &s) { s.ws = f2(0.f); s.c = Comp{0.f, 0.f}; s.wmax = 0.f; }
-    __device__ static void init(St &s, const PairArgs &a, size_t i) {
+    static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 2;
+    struct IS { IPos q; float2 u, v, w, e, m; float eta; float2 ws; float wmax; Comp c; };
+    __device__ static void load(IS &s, const PairArgs &a, size_t i) {
         load_pos(a, i, s.q);
         s.u = f2(__double2float_rn(a.I.f[F_VX][i]));
         s.v = f2(__double2float_rn(a.I.f[F_VY][i]));
@@ -284,44 +274,41 @@ struct TstepDS {
         s.e = f2(__double2float_rn(a.I.f[F_E2][i]));
         s.m = f2(__double2float_rn(a.I.f[F_M][i]));
         s.eta = __double2float_rn(a.eta);
-        reset(s);
+        s.ws = f2(0.f); s.c = Comp{0.f, 0.f}; s.wmax = 0.f;
     }
     // record: {xh,yh} {zh,xl} {yl,zl} {vx,vy} {vz,m} {e2,valid}
-    __device__ __forceinline__ static void step(St &s, const float4 *R) {
+    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R) {
         const float4 q0 = R[0], q1 = R[1], q2 = R[2], q3 = R[3], q4 = R[4], q5 = R[5];
-        float2 dx, dy, dz;
-        pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), dx, dy, dz);
-        const float2 du = sub2(s.u, lo2(q3)), dv = sub2(s.v, hi2(q3)), dw = sub2(s.w, lo2(q4));
-        const float2 e2 = add2(s.e, lo2(q5));
-        const float2 m = add2(s.m, hi2(q4));
-        const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
-        const float2 rv = fma2(dx, du, fma2(dy, dv, mul2(dz, dw)));
-        const float2 v2 = fma2(du, du, fma2(dv, dv, mul2(dw, dw)));
-        const float2 y = inv_r<REFINE>(ss, dx, dy, dz);
-        const float2 q2v = mul2(y, y);
-        const float2 phi = mul2(m, y);
-        float2 w2 = mul2(q2v, fma2(f2(2.0f), phi, v2));
-        float2 gam = mul2(q2v, fma2(mul2(f2(2.0f), q2v), phi, w2));
-        float2 rw;
-        rw.x = rsqrt_hw(w2.x);
-        rw.y = rsqrt_hw(w2.y);
-        gam = mul2(gam, mul2(f2(s.eta), rw));
-        w2 = fnma2(gam, rv, w2);
-        const float vx = q5.z, vy = q5.w;    // valid flags
-        w2.x = (nonzero3(dx.x, dy.x, dz.x) && vx != 0.f) ? w2.x : 0.f;
-        w2.y = (nonzero3(dx.y, dy.y, dz.y) && vy != 0.f) ? w2.y : 0.f;
-        s.ws = add2(s.ws, w2);
-        s.wmax = fmaxf(fmaxf(w2.x, w2.y), s.wmax);
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+            IS &s = S[u];
+            float2 dx, dy, dz;
+            pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), dx, dy, dz);
+            const float2 du = sub2(s.u, lo2(q3)), dv = sub2(s.v, hi2(q3)), dw = sub2(s.w, lo2(q4));
+            const float2 e2 = add2(s.e, lo2(q5));
+            const float2 m = add2(s.m, hi2(q4));
+            const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
+            const float2 rv = fma2(dx, du, fma2(dy, dv, mul2(dz, dw)));
+            const float2 v2 = fma2(du, du, fma2(dv, dv, mul2(dw, dw)));
+            const float2 y = inv_r<REFINE>(ss, dx, dy, dz);
+            const float2 q2v = mul2(y, y);
+            const float2 phi = mul2(m, y);
+            float2 w2 = mul2(q2v, fma2(f2(2.0f), phi, v2));
+            float2 gam = mul2(q2v, fma2(mul2(f2(2.0f), q2v), phi, w2));
+            float2 rw;
+            rw.x = rsqrt_hw(w2.x);
+            rw.y = rsqrt_hw(w2.y);
+            gam = mul2(gam, mul2(f2(s.eta), rw));
+            w2 = fnma2(gam, rv, w2);
+            w2.x = (nonzero3(dx.x, dy.x, dz.x) && q5.z != 0.f) ? w2.x : 0.f;
+            w2.y = (nonzero3(dx.y, dy.y, dz.y) && q5.w != 0.f) ? w2.y : 0.f;
+            s.ws = add2(s.ws, w2);
+            s.wmax = fmaxf(fmaxf(w2.x, w2.y), s.wmax);
+        }
     }
-    __device__ static void fold(St &s) { comp_add(s.c, __fadd_rn(s.ws.x, s.ws.y)); s.ws = f2(0.f); }
-    __device__ static void partials(const St &s, double *p) {
-        p[0] = comp_value(s.c);
-        p[1] = (double)s.wmax;
-    }
-    __device__ static void combine(double *acc, const double *p) {
-        acc[0] += p[0];
-        acc[1] = fmax(p[1], acc[1]);
-    }
+    __device__ static void fold(IS &s) { comp_add(s.c, __fadd_rn(s.ws.x, s.ws.y)); s.ws = f2(0.f); }
+    __device__ static void partials(const IS &s, double *p) { p[0] = comp_value(s.c); p[1] = (double)s.wmax; }
+    __device__ static void combine(double *acc, const double *p) { acc[0] += p[0]; acc[1] = fmax(p[1], acc[1]); }
     __device__ static void store(const double *p, const PairArgs &a, size_t i) {
         a.out[0][i] = a.eta / sqrt(1.0 + p[0]);
         a.out[1][i] = a.eta / sqrt(1.0 + p[1]);
@@ -329,14 +316,11 @@ struct TstepDS {
     static PackSpec pack() { return PackSpec{12, 6, {F_VX, F_VY, F_VZ, F_M, F_E2, -1}}; }
 };
 
-template <bool REFINE>
+template <int IPT_, bool REFINE>
 struct SnapCrackleDS {
-    static constexpr int JF = 18, NQ = 9, NO = 6, NP = 6, KID = K_SNAP_CRACKLE;
-    struct St { IPos q; float2 v[3], A[3], J[3], e; float2 o[6]; Comp c[6]; };
-    __device__ static void reset(St &s) {
-        for (int k = 0; k < 6; ++k) { s.o[k] = f2(0.f); s.c[k] = Comp{0.f, 0.f}; }
-    }
-    __device__ static void init(St &s, const PairArgs &a, size_t i) {
+    static constexpr int IPT = IPT_, JF = 18, NQ = 9, NP = 6;
+    struct IS { IPos q; float2 v[3], A[3], J[3], e; float2 o[6]; Comp c[6]; };
+    __device__ static void load(IS &s, const PairArgs &a, size_t i) {
         load_pos(a, i, s.q);
         for (int k = 0; k < 3; ++k) {
             s.v[k] = f2(__double2float_rn(a.I.f[F_VX + k][i]));
@@ -344,57 +328,53 @@ struct SnapCrackleDS {
             s.J[k] = f2(__double2float_rn(a.I.f[F_JX + k][i]));
         }
         s.e = f2(__double2float_rn(a.I.f[F_E2][i]));
-        reset(s);
+        for (int k = 0; k < 6; ++k) { s.o[k] = f2(0.f); s.c[k] = Comp{0.f, 0.f}; }
     }
     // record: {xh,yh} {zh,xl} {yl,zl} {vx,vy} {vz,ax} {ay,az} {jx,jy} {jz,m} {e2,pad}
-    __device__ __forceinline__ static void step(St &s, const float4 *R) {
+    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R) {
         const float4 q0 = R[0], q1 = R[1], q2 = R[2], q3 = R[3], q4 = R[4];
         const float4 q5 = R[5], q6 = R[6], q7 = R[7], q8 = R[8];
-        float2 r[3];
-        pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), r[0], r[1], r[2]);
-        float2 v[3] = {sub2(s.v[0], lo2(q3)), sub2(s.v[1], hi2(q3)), sub2(s.v[2], lo2(q4))};
-        float2 A[3] = {sub2(s.A[0], hi2(q4)), sub2(s.A[1], lo2(q5)), sub2(s.A[2], hi2(q5))};
-        float2 J[3] = {sub2(s.J[0], lo2(q6)), sub2(s.J[1], hi2(q6)), sub2(s.J[2], lo2(q7))};
-        const float2 e2 = add2(s.e, lo2(q8));
-        const float2 ss = fma2(r[0], r[0], fma2(r[1], r[1], fma2(r[2], r[2], e2)));
-        const float2 rv = fma2(r[0], v[0], fma2(r[1], v[1], mul2(r[2], v[2])));
-        const float2 v2 = fma2(v[0], v[0], fma2(v[1], v[1], mul2(v[2], v[2])));
-        const float2 rJ = fma2(r[0], J[0], fma2(r[1], J[1], mul2(r[2], J[2])));
-        const float2 rA = fma2(r[0], A[0], fma2(r[1], A[1], mul2(r[2], A[2])));
-        const float2 vA = fma2(v[0], A[0], fma2(v[1], A[1], mul2(v[2], A[2])));
-        const float2 y = inv_r<REFINE>(ss, r[0], r[1], r[2]);
-        const float2 q2v = mul2(y, y);
-        float2 al = mul2(rv, q2v);
-        const float2 al2 = mul2(al, al);
-        float2 be = mul2(f2(3.0f), fma2(add2(v2, rA), q2v, al2));
-        float2 ga = fma2(fma2(f2(3.0f), vA, rJ), q2v, mul2(al, fnma2(f2(4.0f), al2, be)));
-        al = mul2(al, f2(3.0f));
-        ga = mul2(ga, f2(3.0f));
-        for (int k = 0; k < 3; ++k) v[k] = fnma2(al, r[k], v[k]);
-        const float2 two_al = mul2(f2(2.0f), al);
-        for (int k = 0; k < 3; ++k) A[k] = sub2(A[k], fma2(two_al, v[k], mul2(be, r[k])));
-        al = mul2(al, f2(3.0f));
-        be = mul2(be, f2(3.0f));
-        for (int k = 0; k < 3; ++k)
-            J[k] = sub2(J[k], fma2(al, A[k], fma2(be, v[k], mul2(ga, r[k]))));
-        const float2 mr3 = mul2(mul2(hi2(q7), y), q2v);
-        for (int k = 0; k < 3; ++k) {
-            s.o[k] = fnma2(mr3, A[k], s.o[k]);
-            s.o[3 + k] = fnma2(mr3, J[k], s.o[3 + k]);
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+            IS &s = S[u];
+            float2 r[3];
+            pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), r[0], r[1], r[2]);
+            float2 v[3] = {sub2(s.v[0], lo2(q3)), sub2(s.v[1], hi2(q3)), sub2(s.v[2], lo2(q4))};
+            float2 A[3] = {sub2(s.A[0], hi2(q4)), sub2(s.A[1], lo2(q5)), sub2(s.A[2], hi2(q5))};
+            float2 J[3] = {sub2(s.J[0], lo2(q6)), sub2(s.J[1], hi2(q6)), sub2(s.J[2], lo2(q7))};
+            const float2 e2 = add2(s.e, lo2(q8));
+            const float2 ss = fma2(r[0], r[0], fma2(r[1], r[1], fma2(r[2], r[2], e2)));
+            const float2 rv = fma2(r[0], v[0], fma2(r[1], v[1], mul2(r[2], v[2])));
+            const float2 v2 = fma2(v[0], v[0], fma2(v[1], v[1], mul2(v[2], v[2])));
+            const float2 rJ = fma2(r[0], J[0], fma2(r[1], J[1], mul2(r[2], J[2])));
+            const float2 rA = fma2(r[0], A[0], fma2(r[1], A[1], mul2(r[2], A[2])));
+            const float2 vA = fma2(v[0], A[0], fma2(v[1], A[1], mul2(v[2], A[2])));
+            const float2 y = inv_r<REFINE>(ss, r[0], r[1], r[2]);
+            const float2 q2v = mul2(y, y);
+            float2 al = mul2(rv, q2v);
+            const float2 al2 = mul2(al, al);
+            float2 be = mul2(f2(3.0f), fma2(add2(v2, rA), q2v, al2));
+            float2 ga = fma2(fma2(f2(3.0f), vA, rJ), q2v, mul2(al, fnma2(f2(4.0f), al2, be)));
+            al = mul2(al, f2(3.0f));
+            ga = mul2(ga, f2(3.0f));
+            for (int k = 0; k < 3; ++k) v[k] = fnma2(al, r[k], v[k]);
+            const float2 two_al = mul2(f2(2.0f), al);
+            for (int k = 0; k < 3; ++k) A[k] = sub2(A[k], fma2(two_al, v[k], mul2(be, r[k])));
+            al = mul2(al, f2(3.0f));
+            be = mul2(be, f2(3.0f));
+            for (int k = 0; k < 3; ++k) J[k] = sub2(J[k], fma2(al, A[k], fma2(be, v[k], mul2(ga, r[k]))));
+            const float2 mr3 = mul2(mul2(hi2(q7), y), q2v);
+            for (int k = 0; k < 3; ++k) {
+                s.o[k] = fnma2(mr3, A[k], s.o[k]);
+                s.o[3 + k] = fnma2(mr3, J[k], s.o[3 + k]);
+            }
         }
     }
-    __device__ static void fold(St &s) {
-        for (int k = 0; k < 6; ++k) {
-            comp_add(s.c[k], __fadd_rn(s.o[k].x, s.o[k].y));
-            s.o[k] = f2(0.f);
-        }
+    __device__ static void fold(IS &s) {
+        for (int k = 0; k < 6; ++k) { comp_add(s.c[k], __fadd_rn(s.o[k].x, s.o[k].y)); s.o[k] = f2(0.f); }
     }
-    __device__ static void partials(const St &s, double *p) {
-        for (int k = 0; k < 6; ++k) p[k] = comp_value(s.c[k]);
-    }
-    __device__ static void combine(double *acc, const double *p) {
-        for (int k = 0; k < 6; ++k) acc[k] += p[k];
-    }
+    __device__ static void partials(const IS &s, double *p) { for (int k = 0; k < 6; ++k) p[k] = comp_value(s.c[k]); }
+    __device__ static void combine(double *acc, const double *p) { for (int k = 0; k < 6; ++k) acc[k] += p[k]; }
     __device__ static void store(const double *p, const PairArgs &a, size_t i) {
         for (int k = 0; k < 6; ++k) a.out[k][i] = p[k];
     }
@@ -403,39 +383,34 @@ struct SnapCrackleDS {
     }
 };
 
-template <bool REFINE>
+template <int IPT_, bool REFINE>
 struct PNAccDS {
-    static constexpr int JF = 12, NQ = 6, NO = 3, NP = 3, KID = K_PNACC;
-    struct St {
-        IPos q; float2 u, v, w, e; float im, iv2; unsigned long order;
+    static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 3;
+    struct IS {
+        IPos q; float iu, iv, iw; float2 u, v, w, e; float im, iv2; unsigned long order;
         float inv2, inv4, inv5, inv6, inv7; float2 a[3]; Comp c[3];
     };
-    __device__ static void reset(St &s) {
-        for (int k = 0; k < 3; ++k) { s.a[k] = f2(0.f); s.c[k] = Comp{0.f, 0.f}; }
-    }
-    __device__ static void init(St &s, const PairArgs &a, size_t i) {
+    __device__ static void load(IS &s, const PairArgs &a, size_t i) {
         load_pos(a, i, s.q);
         const double u = a.I.f[F_VX][i], v = a.I.f[F_VY][i], w = a.I.f[F_VZ][i];
-        s.u = f2(__double2float_rn(u));
-        s.v = f2(__double2float_rn(v));
-        s.w = f2(__double2float_rn(w));
+        s.iu = __double2float_rn(u); s.iv = __double2float_rn(v); s.iw = __double2float_rn(w);
+        s.u = f2(s.iu); s.v = f2(s.iv); s.w = f2(s.iw);
         s.e = f2(__double2float_rn(a.I.f[F_E2][i]));
         s.im = __double2float_rn(a.I.f[F_M][i]);
         s.iv2 = __double2float_rn(u * u + v * v + w * w);
         s.order = a.order;
         s.inv2 = (float)a.inv[2]; s.inv4 = (float)a.inv[4]; s.inv5 = (float)a.inv[5];
         s.inv6 = (float)a.inv[6]; s.inv7 = (float)a.inv[7];
-        reset(s);
+        for (int k = 0; k < 3; ++k) { s.a[k] = f2(0.f); s.c[k] = Comp{0.f, 0.f}; }
     }
-    __device__ __forceinline__ static void lane(St &s, float dx, float dy, float dz, float du, float dv,
+    __device__ __forceinline__ static void lane(IS &s, float dx, float dy, float dz, float du, float dv,
                                                 float dw, float y, float ju, float jv, float jw,
                                                 float jm, float &ax, float &ay, float &az) {
         const float y2 = y * y;
         const float nx = dx * y, ny = dy * y, nz = dz * y;
-        const float iu = s.u.x, iv = s.v.x, iw = s.w.x;
         const float jv2 = ju * ju + jv * jv + jw * jw;
-        const float ivjv = iu * ju + iv * jv + iw * jw;
-        const float niv = nx * iu + ny * iv + nz * iw;
+        const float ivjv = s.iu * ju + s.iv * jv + s.iw * jw;
+        const float niv = nx * s.iu + ny * s.iv + nz * s.iw;
         const float njv = nx * ju + ny * jv + nz * jw;
         const float nv = nx * du + ny * dv + nz * dw;
         const float v2 = du * du + dv * dv + dw * dw;
@@ -448,31 +423,28 @@ struct PNAccDS {
         ay += A * dy + B * dv;
         az += A * dz + B * dw;
     }
-    __device__ __forceinline__ static void step(St &s, const float4 *R) {
+    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R) {
         const float4 q0 = R[0], q1 = R[1], q2 = R[2], q3 = R[3], q4 = R[4], q5 = R[5];
-        float2 dx, dy, dz;
-        pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), dx, dy, dz);
-        const float2 du = sub2(s.u, lo2(q3)), dv = sub2(s.v, hi2(q3)), dw = sub2(s.w, lo2(q4));
-        const float2 e2 = add2(s.e, lo2(q5));
-        const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
-        const float2 y = inv_r<REFINE>(ss, dx, dy, dz);
-        lane(s, dx.x, dy.x, dz.x, du.x, dv.x, dw.x, y.x, q3.x, q3.z, q4.x, q4.z,
-             s.a[0].x, s.a[1].x, s.a[2].x);
-        lane(s, dx.y, dy.y, dz.y, du.y, dv.y, dw.y, y.y, q3.y, q3.w, q4.y, q4.w,
-             s.a[0].y, s.a[1].y, s.a[2].y);
-    }
-    __device__ static void fold(St &s) {
-        for (int k = 0; k < 3; ++k) {
-            comp_add(s.c[k], __fadd_rn(s.a[k].x, s.a[k].y));
-            s.a[k] = f2(0.f);
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+            IS &s = S[u];
+            float2 dx, dy, dz;
+            pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), dx, dy, dz);
+            const float2 du = sub2(s.u, lo2(q3)), dv = sub2(s.v, hi2(q3)), dw = sub2(s.w, lo2(q4));
+            const float2 e2 = add2(s.e, lo2(q5));
+            const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
+            const float2 y = inv_r<REFINE>(ss, dx, dy, dz);
+            lane(s, dx.x, dy.x, dz.x, du.x, dv.x, dw.x, y.x, q3.x, q3.z, q4.x, q4.z,
+                 s.a[0].x, s.a[1].x, s.a[2].x);
+            lane(s, dx.y, dy.y, dz.y, du.y, dv.y, dw.y, y.y, q3.y, q3.w, q4.y, q4.w,
+                 s.a[0].y, s.a[1].y, s.a[2].y);
         }
     }
-    __device__ static void partials(const St &s, double *p) {
-        for (int k = 0; k < 3; ++k) p[k] = comp_value(s.c[k]);
+    __device__ static void fold(IS &s) {
+        for (int k = 0; k < 3; ++k) { comp_add(s.c[k], __fadd_rn(s.a[k].x, s.a[k].y)); s.a[k] = f2(0.f); }
     }
-    __device__ static void combine(double *acc, const double *p) {
-        for (int k = 0; k < 3; ++k) acc[k] += p[k];
-    }
+    __device__ static void partials(const IS &s, double *p) { for (int k = 0; k < 3; ++k) p[k] = comp_value(s.c[k]); }
+    __device__ static void combine(double *acc, const double *p) { for (int k = 0; k < 3; ++k) acc[k] += p[k]; }
     __device__ static void store(const double *p, const PairArgs &a, size_t i) {
         for (int k = 0; k < 3; ++k) a.out[k][i] = p[k];
     }
@@ -489,13 +461,18 @@ __device__ __forceinline__ long long unit_owner(long long u, long long U, long l
     return ((u + 1) * G - 1) / U;
 }
 
+#ifndef TG_DS32_MINB
+#define TG_DS32_MINB 1
+#endif
 template <class K>
-__global__ void __launch_bounds__(DS_THREADS) ds32_streamk(DsArgs a) {
+__global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs a) {
     extern __shared__ __align__(128) float4 ring[];   // [DS_STAGES][DS_PAIRS * NQ]
     __shared__ __align__(8) uint64_t full[DS_STAGES];
     __shared__ int s_last;
+    constexpr int IPT = K::IPT;
     constexpr int TILE_Q = DS_PAIRS * K::NQ;
     constexpr unsigned TILE_BYTES = TILE_Q * sizeof(float4);
+    constexpr int BI = DS_THREADS * IPT;   // i-particles per i-tile
 
     const long long U = a.nit * a.njt;
     const long long G = gridDim.x;
@@ -518,10 +495,14 @@ __global__ void __launch_bounds__(DS_THREADS) ds32_streamk(DsArgs a) {
         for (int s = 0; s < DS_STAGES && u0 + s < u1; ++s) issue(u0 + s, s);
     }
 
+    const size_t last = a.p.ni - 1;
     long long t = u0 / a.njt;
-    typename K::St st;
-    size_t i = (size_t)t * DS_THREADS + tid;
-    K::init(st, a.p, i < a.p.ni ? i : a.p.ni - 1);
+    typename K::IS st[IPT];
+#pragma unroll
+    for (int q = 0; q < IPT; ++q) {
+        const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
+        K::load(st[q], a.p, i < a.p.ni ? i : last);
+    }
     bool aborted = false;
     long long abort_u = u1;                  // first unit whose tile never arrived
     long long issued_to = (u0 + DS_STAGES < u1) ? u0 + DS_STAGES : u1;   // tid 0 only
@@ -538,9 +519,10 @@ __global__ void __launch_bounds__(DS_THREADS) ds32_streamk(DsArgs a) {
         const float4 *R = ring + s * TILE_Q;
 #pragma unroll 1
         for (int fb = 0; fb < DS_PAIRS; fb += DS_FOLD_PAIRS) {
-#pragma unroll 8
+#pragma unroll 4
             for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) K::step(st, R + (fb + pp) * K::NQ);
-            K::fold(st);
+#pragma unroll
+            for (int q = 0; q < IPT; ++q) K::fold(st[q]);
         }
         __syncthreads();   // stage s fully consumed
         if (tid == 0 && u + DS_STAGES < u1) {
@@ -551,15 +533,24 @@ __global__ void __launch_bounds__(DS_THREADS) ds32_streamk(DsArgs a) {
         if (tn == t) continue;
 
         // ---- i-tile t is done for this CTA: store or hand over partials ----
-        double p[K::NP];
-        K::partials(st, p);
         const long long ta = t * a.njt, tb = ta + a.njt;
         if (ta >= u0 && tb <= u1) {
-            if (i < a.p.ni) K::store(p, a.p, i);
+#pragma unroll
+            for (int q = 0; q < IPT; ++q) {
+                const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
+                double p[K::NP];
+                K::partials(st[q], p);
+                if (i < a.p.ni) K::store(p, a.p, i);
+            }
         } else {
             const int slot = (t == u0 / a.njt) ? 0 : 1;
-            double *mine = a.part + ((k * 2 + slot) * K::NP) * DS_THREADS;
-            for (int q = 0; q < K::NP; ++q) mine[q * DS_THREADS + tid] = p[q];
+            double *mine = a.part + ((k * 2 + slot) * IPT * K::NP) * DS_THREADS;
+#pragma unroll
+            for (int q = 0; q < IPT; ++q) {
+                double p[K::NP];
+                K::partials(st[q], p);
+                for (int v = 0; v < K::NP; ++v) mine[(q * K::NP + v) * DS_THREADS + tid] = p[v];
+            }
             __threadfence();
             __syncthreads();
             const long long klo = unit_owner(ta, U, G), khi = unit_owner(tb - 1, U, G);
@@ -570,27 +561,31 @@ __global__ void __launch_bounds__(DS_THREADS) ds32_streamk(DsArgs a) {
             __syncthreads();
             if (s_last) {
                 __threadfence();
-                double acc[K::NP];
-                bool first = true;
-                for (long long kk = klo; kk <= khi; ++kk) {
-                    const int sl = (t == unit_start(kk, U, G) / a.njt) ? 0 : 1;
-                    const double *src = a.part + ((kk * 2 + sl) * K::NP) * DS_THREADS;
-                    double q[K::NP];
-                    for (int v = 0; v < K::NP; ++v) q[v] = __ldcg(src + v * DS_THREADS + tid);
-                    if (first) {
-                        for (int v = 0; v < K::NP; ++v) acc[v] = q[v];
-                        first = false;
-                    } else {
-                        K::combine(acc, q);
+                for (int q = 0; q < IPT; ++q) {
+                    double acc[K::NP];
+                    for (long long kk = klo; kk <= khi; ++kk) {
+                        const int sl = (t == unit_start(kk, U, G) / a.njt) ? 0 : 1;
+                        const double *src = a.part + ((kk * 2 + sl) * IPT * K::NP) * DS_THREADS;
+                        double v[K::NP];
+                        for (int w = 0; w < K::NP; ++w) v[w] = __ldcg(src + (q * K::NP + w) * DS_THREADS + tid);
+                        if (kk == klo) {
+                            for (int w = 0; w < K::NP; ++w) acc[w] = v[w];
+                        } else {
+                            K::combine(acc, v);
+                        }
                     }
+                    const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
+                    if (i < a.p.ni) K::store(acc, a.p, i);
                 }
-                if (i < a.p.ni) K::store(acc, a.p, i);
             }
         }
         if (tn >= 0) {
             t = tn;
-            i = (size_t)t * DS_THREADS + tid;
-            K::init(st, a.p, i < a.p.ni ? i : a.p.ni - 1);
+#pragma unroll
+            for (int q = 0; q < IPT; ++q) {
+                const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
+                K::load(st[q], a.p, i < a.p.ni ? i : last);
+            }
         }
     }
 
@@ -632,13 +627,14 @@ static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 template <class K>
 static Geometry geometry(size_t ni, size_t nj, int sms) {
     Geometry g;
-    g.nit = (long long)((ni + DS_THREADS - 1) / DS_THREADS);
+    const size_t bi = (size_t)DS_THREADS * K::IPT;
+    g.nit = (long long)((ni + bi - 1) / bi);
     g.njt = (long long)((nj + DS_TILE - 1) / DS_TILE);
     g.units = g.nit * g.njt;
     const long long slots = (long long)sms * ctas_per_sm<K>();
     g.grid = g.units < slots ? g.units : slots;
     g.rec_bytes = align_up((size_t)g.njt * DS_PAIRS * K::NQ * sizeof(float4), 256);
-    g.part_bytes = align_up((size_t)g.grid * 2 * K::NP * DS_THREADS * sizeof(double), 256);
+    g.part_bytes = align_up((size_t)g.grid * 2 * K::IPT * K::NP * DS_THREADS * sizeof(double), 256);
     g.ticket_bytes = align_up((size_t)g.nit * sizeof(int), 256);
     return g;
 }
@@ -673,32 +669,36 @@ static cudaError_t run_ds(const PairArgs &p, void *ws, size_t ws_bytes, int sms,
 }
 
 #ifndef TG_DS32_REFINE
-#define TG_DS32_REFINE 1
+#define TG_DS32_REFINE 0
+#endif
+#ifndef TG_DS32_IPT
+#define TG_DS32_IPT 2
 #endif
 constexpr bool REF = TG_DS32_REFINE != 0;
+constexpr int IPT2 = TG_DS32_IPT;
 
 bool ds32_supported(int kernel) { return kernel != K_SAKURA && kernel >= 0 && kernel < K_COUNT; }
 
 size_t ds32_workspace_bytes(int kernel, size_t ni, size_t nj, int sms) {
     switch (kernel) {
-        case K_PHI: return ws_bytes_for<PhiDS<REF>>(ni, nj, sms);
-        case K_ACC: return ws_bytes_for<AccDS<REF>>(ni, nj, sms);
-        case K_ACC_JERK: return ws_bytes_for<AccJerkDS<REF>>(ni, nj, sms);
-        case K_SNAP_CRACKLE: return ws_bytes_for<SnapCrackleDS<REF>>(ni, nj, sms);
-        case K_TSTEP: return ws_bytes_for<TstepDS<REF>>(ni, nj, sms);
-        case K_PNACC: return ws_bytes_for<PNAccDS<REF>>(ni, nj, sms);
+        case K_PHI: return ws_bytes_for<PhiDS<IPT2, REF>>(ni, nj, sms);
+        case K_ACC: return ws_bytes_for<AccDS<IPT2, REF>>(ni, nj, sms);
+        case K_ACC_JERK: return ws_bytes_for<AccJerkDS<IPT2, REF>>(ni, nj, sms);
+        case K_SNAP_CRACKLE: return ws_bytes_for<SnapCrackleDS<1, REF>>(ni, nj, sms);
+        case K_TSTEP: return ws_bytes_for<TstepDS<IPT2, REF>>(ni, nj, sms);
+        case K_PNACC: return ws_bytes_for<PNAccDS<1, REF>>(ni, nj, sms);
         default: return 0;
     }
 }
 
 cudaError_t launch_ds32(int kernel, const PairArgs &a, void *ws, size_t ws_bytes, int sms, cudaStream_t s) {
     switch (kernel) {
-        case K_PHI: return run_ds<PhiDS<REF>>(a, ws, ws_bytes, sms, s);
-        case K_ACC: return run_ds<AccDS<REF>>(a, ws, ws_bytes, sms, s);
-        case K_ACC_JERK: return run_ds<AccJerkDS<REF>>(a, ws, ws_bytes, sms, s);
-        case K_SNAP_CRACKLE: return run_ds<SnapCrackleDS<REF>>(a, ws, ws_bytes, sms, s);
-        case K_TSTEP: return run_ds<TstepDS<REF>>(a, ws, ws_bytes, sms, s);
-        case K_PNACC: return run_ds<PNAccDS<REF>>(a, ws, ws_bytes, sms, s);
+        case K_PHI: return run_ds<PhiDS<IPT2, REF>>(a, ws, ws_bytes, sms, s);
+        case K_ACC: return run_ds<AccDS<IPT2, REF>>(a, ws, ws_bytes, sms, s);
+        case K_ACC_JERK: return run_ds<AccJerkDS<IPT2, REF>>(a, ws, ws_bytes, sms, s);
+        case K_SNAP_CRACKLE: return run_ds<SnapCrackleDS<1, REF>>(a, ws, ws_bytes, sms, s);
+        case K_TSTEP: return run_ds<TstepDS<IPT2, REF>>(a, ws, ws_bytes, sms, s);
+        case K_PNACC: return run_ds<PNAccDS<1, REF>>(a, ws, ws_bytes, sms, s);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -26,6 +26,28 @@ __global__ void probe_fp32(float *sink, int iters, float a, float b) {
     if (s == 12345.678f) sink[blockIdx.x] = s;   // keeps the chains alive
 }
 
+// Packed FFMA2 chains interleaved with as many scalar FFMA chains: shows
+// whether scalar FP32 work can overlap packed work on the FMA pipes.
+__global__ void probe_fp32_mixed(float *sink, int iters, float a, float b) {
+    float2 acc[NCHAIN];
+    float sc[NCHAIN];
+    for (int k = 0; k < NCHAIN; ++k) {
+        acc[k] = make_float2(threadIdx.x * 1e-7f + k, k * 1e-3f);
+        sc[k] = k * 2e-3f;
+    }
+    const float2 va = make_float2(a, a), vb = make_float2(b, b);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int k = 0; k < NCHAIN; ++k) {
+            acc[k] = __ffma2_rn(acc[k], va, vb);
+            sc[k] = fmaf(sc[k], a, b);
+        }
+    }
+    float s = 0.f;
+    for (int k = 0; k < NCHAIN; ++k) s += acc[k].x + acc[k].y + sc[k];
+    if (s == 12345.678f) sink[blockIdx.x] = s;
+}
+
 __global__ void probe_fp64(double *sink, int iters, double a, double b) {
     double acc[NCHAIN];
     for (int k = 0; k < NCHAIN; ++k) acc[k] = threadIdx.x * 1e-7 + k;
@@ -60,13 +82,15 @@ double tg_probe_fma_tflops(int which, int iters, void *stream) {
         cudaEventRecord(e0, s);
         if (which == 0)
             probe_fp32<<<blocks, threads, 0, s>>>(static_cast<float *>(sink), iters, 0.999999f, 1e-6f);
+        else if (which == 2)
+            probe_fp32_mixed<<<blocks, threads, 0, s>>>(static_cast<float *>(sink), iters, 0.999999f, 1e-6f);
         else
             probe_fp64<<<blocks, threads, 0, s>>>(static_cast<double *>(sink), iters, 0.999999, 1e-6);
         cudaEventRecord(e1, s);
         if (cudaEventSynchronize(e1) != cudaSuccess) { best = -1.0; break; }
         float ms = 0.f;
         cudaEventElapsedTime(&ms, e0, e1);
-        const double fmas = (double)blocks * threads * iters * NCHAIN * (which == 0 ? 2.0 : 1.0);
+        const double fmas = (double)blocks * threads * iters * NCHAIN * (which == 0 ? 2.0 : which == 2 ? 3.0 : 1.0);
         const double tf = 2.0 * fmas / (ms * 1e-3) / 1e12;
         if (rep > 0 && tf > best) best = tf;   // first launch is warm-up
     }
