@@ -57,6 +57,14 @@ __device__ __forceinline__ float rsqrt_hw(float s) {
     return y;
 }
 
+// Hardware reciprocal (MUFU.RCP, ~1 ulp): 1/s from the XU pipe instead of
+// y*y on the FMA pipe.
+__device__ __forceinline__ float rcp_hw(float s) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(s));
+    return y;
+}
+
 // Pair exclusion: lane is kept when r != 0, i.e. any of dx, dy, dz is
 // nonzero.  The split-FP32 kernels store every coordinate with -0 turned
 // into +0, so the difference of two equal coordinates is +0 (all bits zero)

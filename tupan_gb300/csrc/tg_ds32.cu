@@ -32,7 +32,10 @@
 
 namespace tg {
 
-constexpr int DS_THREADS = 128;   // i-particles per tile (one per thread)
+#ifndef TG_DS32_THREADS
+#define TG_DS32_THREADS 256
+#endif
+constexpr int DS_THREADS = TG_DS32_THREADS;   // threads per CTA
 constexpr int DS_TILE = 256;      // j-particles per tile
 constexpr int DS_PAIRS = DS_TILE / 2;
 constexpr int DS_STAGES = 3;
@@ -119,6 +122,16 @@ __device__ __forceinline__ void pair_dr(const IPos &q, float2 jxh, float2 jyh, f
     dz = add2(sub2(q.zh, jzh), sub2(q.zl, jzl));
 }
 // Masked, Newton-refined 1/sqrt(s) per lane; zero where dr == 0.
+// 1/sqrt(s) and 1/s per lane from the XU pipe; both zero where dr == 0
+// (the excluded lane gets s = +inf, whose reciprocal and rsqrt are 0).
+__device__ __forceinline__ void inv_r_r2(float2 s, float2 dx, float2 dy, float2 dz, float2 &y, float2 &y2) {
+    const float inf = __int_as_float(0x7f800000);
+    const float sx = nonzero3(dx.x, dy.x, dz.x) ? s.x : inf;
+    const float sy = nonzero3(dx.y, dy.y, dz.y) ? s.y : inf;
+    y = make_float2(rsqrt_hw(sx), rsqrt_hw(sy));
+    y2 = make_float2(rcp_hw(sx), rcp_hw(sy));
+}
+
 template <bool REFINE>
 __device__ __forceinline__ float2 inv_r(float2 s, float2 dx, float2 dy, float2 dz) {
     float2 y;
@@ -166,8 +179,9 @@ struct AccDS {
             pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), dx, dy, dz);
             const float2 e2 = add2(s.e, hi2(q3));
             const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
-            const float2 y = inv_r<REFINE>(ss, dx, dy, dz);
-            const float2 y2 = mul2(y, y);
+            float2 y, y2;
+            if (REFINE) { y = inv_r<true>(ss, dx, dy, dz); y2 = mul2(y, y); }
+            else inv_r_r2(ss, dx, dy, dz, y, y2);
             const float2 mr3 = mul2(mul2(lo2(q3), y), y2);
             s.a[0] = fnma2(mr3, dx, s.a[0]);
             s.a[1] = fnma2(mr3, dy, s.a[1]);
@@ -237,8 +251,9 @@ struct AccJerkDS {
             const float2 du = sub2(s.u, lo2(q3)), dv = sub2(s.v, hi2(q3)), dw = sub2(s.w, lo2(q4));
             const float2 e2 = add2(s.e, lo2(q5));
             const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
-            const float2 y = inv_r<REFINE>(ss, dx, dy, dz);
-            const float2 y2 = mul2(y, y);
+            float2 y, y2;
+            if (REFINE) { y = inv_r<true>(ss, dx, dy, dz); y2 = mul2(y, y); }
+            else inv_r_r2(ss, dx, dy, dz, y, y2);
             const float2 mr3 = mul2(mul2(hi2(q4), y), y2);
             const float2 rv = fma2(dx, du, fma2(dy, dv, mul2(dz, dw)));
             const float2 al = mul2(mul2(rv, y2), f2(3.0f));
@@ -462,8 +477,12 @@ __device__ __forceinline__ long long unit_owner(long long u, long long U, long l
 }
 
 #ifndef TG_DS32_MINB
-#define TG_DS32_MINB 1
+#define TG_DS32_MINB 2
 #endif
+#ifndef TG_DS32_UNROLL
+#define TG_DS32_UNROLL 4
+#endif
+constexpr int DS_UNROLL = TG_DS32_UNROLL;
 template <class K>
 __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs a) {
     extern __shared__ __align__(128) float4 ring[];   // [DS_STAGES][DS_PAIRS * NQ]
@@ -519,7 +538,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
         const float4 *R = ring + s * TILE_Q;
 #pragma unroll 1
         for (int fb = 0; fb < DS_PAIRS; fb += DS_FOLD_PAIRS) {
-#pragma unroll 4
+#pragma unroll DS_UNROLL
             for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) K::step(st, R + (fb + pp) * K::NQ);
 #pragma unroll
             for (int q = 0; q < IPT; ++q) K::fold(st[q]);
