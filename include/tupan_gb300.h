@@ -9,7 +9,7 @@
  *    unsigned long, INT is long, REAL is double).  They take HOST pointers,
  *    copy inputs to the GPU, run, copy outputs back and return when done, so
  *    the reference's cffi backend can load this library in place of its own
- *    build (see INTEGRATION.md).  The arithmetic precision is chosen with
+ *    build.  The arithmetic precision is chosen with
  *    tg_set_host_precision() (default TG_PREC_FP64).
  *
  * 2. Device entry points tg_<kernel>(...) with the same argument order but

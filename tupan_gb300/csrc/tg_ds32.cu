@@ -25,7 +25,7 @@
 // Arithmetic: one i-particle per thread, two j-particles per packed f32x2
 // instruction (FADD2/FMUL2/FFMA2); 1/sqrt is MUFU.RSQ plus one Newton step;
 // per-thread sums run in FP32 over 64 j and are then folded into Kahan-
-// compensated accumulators.  The roofline is the FP32 pipe: see the design doc.
+// compensated accumulators.  The roofline is the FP32 pipe (FFMA2 issue).
 #include "tg_device.cuh"
 #include "tg_internal.h"
 #include "tg_pn_terms.cuh"
