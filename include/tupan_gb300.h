@@ -145,6 +145,25 @@ int tg_sakura(size_t ni, const double *im, const double *irx, const double *iry,
               double *idrx, double *idry, double *idrz,
               double *idvx, double *idvy, double *idvz, int prec, void *stream);
 
+/* No counterpart in the reference.  Split-FP32 AccJerk (same arithmetic as
+ * tg_acc_jerk with TG_PREC_DS32) for callers that cannot let a library
+ * allocate GPU memory -- applications whose own pool owns the GPU's memory,
+ * or loops that must not stall other streams on cudaMalloc/cudaFree.  It
+ * calls no allocator: its scratch is a fixed 24 MiB __device__ array that
+ * every GPU loading the library holds until exit.  Limits: ni <= 2^20,
+ * nj <= 2^17 (else TG_EINVAL).  The first call on a device looks up the
+ * array's address with that device current; make it before any stream
+ * capture.  Calls share the array, so calls that overlap on the GPU race:
+ * order them on one stream.  Device pointers, asynchronous on `stream`. */
+int tg_acc_jerk_noalloc(size_t ni, const double *im, const double *irx, const double *iry,
+                        const double *irz, const double *ie2,
+                        const double *ivx, const double *ivy, const double *ivz,
+                        size_t nj, const double *jm, const double *jrx, const double *jry,
+                        const double *jrz, const double *je2,
+                        const double *jvx, const double *jvy, const double *jvz,
+                        double *iax, double *iay, double *iaz,
+                        double *ijx, double *ijy, double *ijz, void *stream);
+
 /* ---------------------------------------------------------------------- */
 /* Drop-in host entry points: exact libtupan.h signatures (float64 build)  */
 /* ---------------------------------------------------------------------- */

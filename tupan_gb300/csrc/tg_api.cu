@@ -202,6 +202,10 @@ void host_call(const HostCall &h, F launch) {
 
 }  // namespace
 
+namespace tg {
+void set_last_error(const char *msg) { g_err = msg; }
+}  // namespace tg
+
 extern "C" {
 
 const char *tg_version(void) { return "tupan_gb300 0.1.0 (sm_103a)"; }

@@ -687,6 +687,41 @@ static cudaError_t run_ds(const PairArgs &p, void *ws, size_t ws_bytes, int sms,
     return cudaGetLastError();
 }
 
+// Same launch as run_ds with the grid limited to max_grid CTAs.
+template <class K>
+static Geometry geometry_capped(size_t ni, size_t nj, int sms, long long max_grid) {
+    Geometry g = geometry<K>(ni, nj, sms);
+    if (max_grid > 0 && g.grid > max_grid) {
+        g.grid = max_grid;
+        g.part_bytes = align_up((size_t)g.grid * 2 * K::IPT * K::NP * DS_THREADS * sizeof(double), 256);
+    }
+    return g;
+}
+
+template <class K>
+static cudaError_t run_ds_capped(const PairArgs &p, void *ws, size_t ws_bytes, int sms,
+                                 long long max_grid, cudaStream_t s) {
+    const Geometry g = geometry_capped<K>(p.ni, p.nj, sms, max_grid);
+    if (g.rec_bytes + g.part_bytes + g.ticket_bytes > ws_bytes) return cudaErrorInvalidValue;
+    char *base = static_cast<char *>(ws);
+    DsArgs a;
+    a.p = p;
+    a.rec = reinterpret_cast<const float4 *>(base);
+    a.part = reinterpret_cast<double *>(base + g.rec_bytes);
+    a.ticket = reinterpret_cast<int *>(base + g.rec_bytes + g.part_bytes);
+    a.nit = g.nit;
+    a.njt = g.njt;
+    const size_t npairs = (size_t)g.njt * DS_PAIRS;
+    const PackSpec spec = K::pack();
+    const unsigned pack_blocks = (unsigned)((npairs * 2 + 255) / 256);
+    ds32_pack<<<pack_blocks, 256, 0, s>>>(p.J, p.nj, npairs, spec, reinterpret_cast<float *>(base));
+    cudaError_t e = cudaMemsetAsync(a.ticket, 0, g.ticket_bytes, s);
+    if (e != cudaSuccess) return e;
+    const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
+    ds32_streamk<K><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
 #ifndef TG_DS32_REFINE
 #define TG_DS32_REFINE 0
 #endif
@@ -720,6 +755,18 @@ cudaError_t launch_ds32(int kernel, const PairArgs &a, void *ws, size_t ws_bytes
         case K_PNACC: return run_ds<PNAccDS<1, REF>>(a, ws, ws_bytes, sms, s);
         default: return cudaErrorInvalidValue;
     }
+}
+
+size_t ds32_workspace_bytes_capped(int kernel, size_t ni, size_t nj, int sms, long long max_grid) {
+    if (kernel != K_ACC_JERK) return 0;
+    const Geometry g = geometry_capped<AccJerkDS<IPT2, REF>>(ni, nj, sms, max_grid);
+    return g.rec_bytes + g.part_bytes + g.ticket_bytes;
+}
+
+cudaError_t launch_ds32_capped(int kernel, const PairArgs &a, void *ws, size_t ws_bytes, int sms,
+                               long long max_grid, cudaStream_t s) {
+    if (kernel != K_ACC_JERK) return cudaErrorInvalidValue;
+    return run_ds_capped<AccJerkDS<IPT2, REF>>(a, ws, ws_bytes, sms, max_grid, s);
 }
 
 }  // namespace tg

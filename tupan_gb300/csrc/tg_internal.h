@@ -52,4 +52,13 @@ cudaError_t launch_ds32(int kernel, const PairArgs &a, void *ws, size_t ws_bytes
                         cudaStream_t s);
 bool ds32_supported(int kernel);
 
+// Record `msg` as this thread's tg_last_error() text.
+void set_last_error(const char *msg);
+
+// Split-FP32 launch on caller-provided scratch with the grid limited to
+// `max_grid` CTAs (the caller sizes its scratch for that many).
+size_t ds32_workspace_bytes_capped(int kernel, size_t ni, size_t nj, int sms, long long max_grid);
+cudaError_t launch_ds32_capped(int kernel, const PairArgs &a, void *ws, size_t ws_bytes, int sms,
+                               long long max_grid, cudaStream_t s);
+
 }  // namespace tg
