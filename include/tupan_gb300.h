@@ -145,6 +145,36 @@ int tg_sakura(size_t ni, const double *im, const double *irx, const double *iry,
               double *idrx, double *idry, double *idrz,
               double *idvx, double *idvy, double *idvz, int prec, void *stream);
 
+/* ---------------------------------------------------------------------- */
+/* Integrator updates (device pointers, FP64, asynchronous on `stream`).   */
+/* Fused forms of the reference integrators' numpy updates, evaluated in   */
+/* numpy's operation order so FP64 trajectories match bit for bit.         */
+/* ---------------------------------------------------------------------- */
+
+/* r += v * tau (drift_n, tupan/integrator/sia.py:64-73) */
+int tg_drift(size_t n, double *rx, double *ry, double *rz, const double *vx, const double *vy,
+             const double *vz, double tau, void *stream);
+/* v += a * tau (kick_n, tupan/integrator/sia.py:77-86) */
+int tg_kick(size_t n, double *vx, double *vy, double *vz, const double *ax, const double *ay,
+            const double *az, double tau, void *stream);
+/* r += dr, v += dv (sakura_step, tupan/integrator/sakura.py:30-44) */
+int tg_add_increments(size_t n, double *rx, double *ry, double *rz, double *vx, double *vy, double *vz,
+                      const double *drx, const double *dry, const double *drz, const double *dvx,
+                      const double *dvy, const double *dvz, void *stream);
+/* Hermite predictor of order 2/4/6/8 (H2/H4/H6/H8.epredict,
+ * tupan/integrator/hermite.py:24-36, 75-90, 127-157, 200-235): updates
+ * rv = {rx, ry, rz, vx, vy, vz} in place from deriv = {ax, ay, az, jx, ...,
+ * cz} (3 * order/2 arrays: a, then j, s, c as the order needs). */
+int tg_hermite_predict(int order, size_t n, double tau, double *const *rv, const double *const *deriv,
+                       void *stream);
+/* Hermite corrector of order 2/4/6/8 (H2..H8.ecorrect, hermite.py:39-53,
+ * 93-119, 160-196, 238-283): rv1 = corrected {r, v} from the start state
+ * rv0 = {r0, v0}, its derivatives deriv0 and the derivatives deriv1 at the
+ * predicted state (same layouts as tg_hermite_predict). */
+int tg_hermite_correct(int order, size_t n, double tau, const double *const *rv0,
+                       const double *const *deriv0, const double *const *deriv1, double *const *rv1,
+                       void *stream);
+
 /* No counterpart in the reference.  Split-FP32 AccJerk (same arithmetic as
  * tg_acc_jerk with TG_PREC_DS32) for callers that cannot let a library
  * allocate GPU memory -- applications whose own pool owns the GPU's memory,

@@ -141,5 +141,67 @@ def main():
         print("wrote", path, os.path.getsize(path), "bytes,", len(calls), "calls")
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and "--integrators" not in sys.argv:
     main()
+
+
+# ---------------------------------------------------------------------------
+# Integrator trajectories from the reference integrators themselves.
+# ---------------------------------------------------------------------------
+INTEGRATOR_RUNS = (
+    # method, eta, t_end, eps2
+    ("ahermite2", 0.01, 1.0 / 64, 1e-3),
+    ("ahermite4", 0.01, 1.0 / 32, 1e-3),
+    ("hermite6", 1.0 / 128, 1.0 / 32, 1e-3),
+    ("hermite8", 1.0 / 128, 1.0 / 64, 1e-3),
+    ("sia21s.kdk", 1.0 / 256, 1.0 / 32, 1e-3),
+    ("sia21s.dkd", 1.0 / 256, 1.0 / 32, 1e-3),
+    ("sia21a.kdk", 0.01, 1.0 / 32, 1e-3),
+    ("sakura", 1.0 / 128, 1.0 / 64, 0.0),
+    ("asakura", 0.01, 1.0 / 64, 0.0),
+)
+
+
+def integrator_ics(n=48, seed=7):
+    rng = np.random.default_rng(seed)
+    d = {"mass": rng.random(n) / n}
+    for c in "xyz":
+        d["r" + c] = rng.normal(size=n)
+        d["v" + c] = rng.normal(size=n) * 0.3
+    return d
+
+
+def reference_trajectories(ref_root="/root/reference"):
+    """Run the reference integrators (imported from the reference tree, with
+    HOME redirected for its cffi build cache) on the same initial state."""
+    import tempfile
+    os.environ["HOME"] = tempfile.mkdtemp(prefix="tupan_home_")
+    sys.path.insert(0, ref_root)
+    from tupan.integrator import Integrator
+    from tupan.particles.allparticles import ParticleSystem
+    ics = integrator_ics()
+    n = len(ics["mass"])
+    store = {"ic_" + k: v for k, v in ics.items()}
+    for method, eta, t_end, eps2 in INTEGRATOR_RUNS:
+        ps = ParticleSystem(n)
+        for k, v in ics.items():
+            getattr(ps, k)[...] = v
+        ps.eps2[...] = eps2
+        integ = Integrator(eta, 0.0, ps, method=method)
+        steps = 0
+        while abs(integ.time) < abs(t_end):
+            integ.evolve_step(t_end)
+            steps += 1
+        out = integ.particle_system
+        key = method.replace(".", "_")
+        store["cfg_" + key] = np.array([eta, t_end, eps2, steps, integ.time])
+        for f in ("rx", "ry", "rz", "vx", "vy", "vz"):
+            store["end_%s_%s" % (key, f)] = np.array(getattr(out, f))
+        print(method, steps, "steps to", integ.time)
+    path = os.path.join(HERE, "golden_integrators.npz")
+    np.savez_compressed(path, **store)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__" and "--integrators" in sys.argv:
+    reference_trajectories()

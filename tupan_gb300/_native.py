@@ -70,6 +70,16 @@ def _load():
     lib.tg_set_host_precision.restype = ctypes.c_int
     lib.tg_get_host_precision.restype = ctypes.c_int
     lib.tg_device_sms.restype = ctypes.c_int
+    for nm in ("tg_drift", "tg_kick"):
+        getattr(lib, nm).restype = ctypes.c_int
+        getattr(lib, nm).argtypes = [ctypes.c_size_t] + [_DP] * 6 + [ctypes.c_double, _DP]
+    lib.tg_add_increments.restype = ctypes.c_int
+    lib.tg_add_increments.argtypes = [ctypes.c_size_t] + [_DP] * 12 + [_DP]
+    PP = ctypes.POINTER(ctypes.c_void_p)
+    lib.tg_hermite_predict.restype = ctypes.c_int
+    lib.tg_hermite_predict.argtypes = [ctypes.c_int, ctypes.c_size_t, ctypes.c_double, PP, PP, _DP]
+    lib.tg_hermite_correct.restype = ctypes.c_int
+    lib.tg_hermite_correct.argtypes = [ctypes.c_int, ctypes.c_size_t, ctypes.c_double, PP, PP, PP, PP, _DP]
     lib.tg_probe_fma_tflops.restype = ctypes.c_double
     lib.tg_probe_fma_tflops.argtypes = [ctypes.c_int, ctypes.c_int, _DP]
     return lib
@@ -100,3 +110,9 @@ def sync_status(stream=None):
     if rc < 0:
         raise TupanGB300Error("tg_sync_status failed: %s" % last_error())
     return rc
+
+
+def ptr_array(tensors):
+    """A host array of device pointers (for the tg_hermite_* entry points)."""
+    arr = (ctypes.c_void_p * len(tensors))(*[t.data_ptr() for t in tensors])
+    return arr

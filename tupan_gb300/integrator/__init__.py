@@ -1,0 +1,118 @@
+"""Integrators driving the GPU kernels, mirroring tupan/integrator.
+
+Base and Integrator follow tupan/integrator/__init__.py:13-157 (base time
+step, power-of-two block step commensurate with the current time,
+evolve_step); Hermite (hermite2..8, ahermite2..8), SIA21 (sia21s/sia21a,
+kdk/dkd) and Sakura (sakura, asakura) are in the submodules.  All particle
+state stays on the GPU; the element-wise updates are the fused FP64 kernels
+of libtupan_gb300 (tg_drift, tg_kick, tg_hermite_predict, ...), evaluated in
+the reference's operation order.
+"""
+import math
+import sys
+
+import numpy as np
+
+from ..lib import extensions
+
+
+class Base(object):
+    def __init__(self, eta, time, ps, **kwargs):
+        self.eta = eta
+        self.ps = ps
+        self.t_curr = float(time)
+        ps.t_curr = self.t_curr
+        self.is_initialized = False
+        pn_order = kwargs.pop("pn_order", 0)
+        clight = kwargs.pop("clight", None)
+        if pn_order > 0:
+            if clight is None:
+                raise TypeError("'clight' is not defined. Please set the speed of light "
+                                "argument 'clight' when using 'pn_order' > 0.")
+            extensions.clight.pn_order = pn_order
+            extensions.clight.clight = clight
+        self.reporter = kwargs.pop("reporter", None)
+        if kwargs:
+            raise TypeError("%s.__init__ received unexpected keyword arguments: %s."
+                            % (type(self).__name__, ", ".join(kwargs.keys())))
+
+    def initialize(self, t_end):
+        if self.reporter:
+            self.reporter.diagnostic_report(self.ps)
+        self.is_initialized = True
+
+    def finalize(self, t_end):
+        pass
+
+    def get_base_tstep(self, t_end):
+        """integrator/__init__.py:49-57"""
+        dt = min(abs(t_end) - abs(self.t_curr), abs(self.eta))
+        dt = max(dt, abs(t_end) * (2 * sys.float_info.epsilon))
+        return math.copysign(dt, self.eta)
+
+    def get_min_block_tstep(self, ps, tau):
+        """Power-of-two step not above the smallest particle step and
+        commensurate with the current time (integrator/__init__.py:59-78)."""
+        min_ts = ps.min_tstep()
+        power = int(np.log2(min_ts) - 1)
+        min_bts = 2.0 ** power
+        t_next = self.t_curr + min_bts
+        while t_next % min_bts != 0:
+            min_bts /= 2
+        min_bts = math.copysign(min_bts, tau)
+        if abs(min_bts) > abs(tau):
+            min_bts = tau
+        return min_bts
+
+    def advance_time(self, ps, tau):
+        self.t_curr += tau
+        ps.t_curr = self.t_curr
+        ps.tstep.fill_(tau)
+        ps.time += tau
+        ps.nstep += 1
+
+    def evolve_step(self, t_end):
+        if not self.is_initialized:
+            self.initialize(t_end)
+        tau = self.get_base_tstep(t_end)
+        self.ps = self.do_step(self.ps, tau)
+        if self.reporter:
+            self.reporter.diagnostic_report(self.ps)
+
+
+from . import hermite, sakura, sia  # noqa: E402
+
+
+class Integrator(object):
+    """Method dispatcher (integrator/__init__.py:108-157)."""
+    PROVIDED_METHODS = (sia.SIA.PROVIDED_METHODS + sakura.Sakura.PROVIDED_METHODS
+                        + hermite.Hermite.PROVIDED_METHODS)
+
+    def __init__(self, eta, time, ps, **kwargs):
+        method = kwargs.pop("method", None)
+        if method in sia.SIA.PROVIDED_METHODS:
+            self.integrator = sia.SIA(eta, time, ps, method, **kwargs)
+        elif method in sakura.Sakura.PROVIDED_METHODS:
+            self.integrator = sakura.Sakura(eta, time, ps, method, **kwargs)
+        elif method in hermite.Hermite.PROVIDED_METHODS:
+            self.integrator = hermite.Hermite(eta, time, ps, method, **kwargs)
+        else:
+            raise ValueError("Unexpected integration method: %r. Provided methods: %s"
+                             % (method, list(self.PROVIDED_METHODS)))
+
+    def initialize(self, t_end):
+        self.integrator.initialize(t_end)
+
+    def finalize(self, t_end):
+        self.integrator.finalize(t_end)
+
+    def evolve_step(self, t_end):
+        self.integrator.evolve_step(t_end)
+
+    @property
+    def time(self):
+        return self.integrator.t_curr
+
+    @property
+    def particle_system(self):
+        return self.integrator.ps
