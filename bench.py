@@ -233,6 +233,7 @@ def ours(args, rank, world, dist):
         dist.barrier()
     torch.cuda.synchronize()
     wall0 = time.perf_counter()
+    torch.cuda.nvtx.range_push("bench_timed")   # ncu --nvtx-include bench_timed/
     for s in range(args.steps):
         flush.zero_()
         ev[s][0].record(stream)
@@ -240,6 +241,7 @@ def ours(args, rank, world, dist):
         ev[s][1].record(stream)
         acc_jerk(DS, outs[3:])
         ev[s][2].record(stream)
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
     if dist:

@@ -145,6 +145,16 @@ int tg_sakura(size_t ni, const double *im, const double *irx, const double *iry,
               double *idrx, double *idry, double *idrz,
               double *idvx, double *idvy, double *idvz, int prec, void *stream);
 
+/* No counterpart in the reference: vector-Jacobian product of acc_kernel
+ * for one particle set (i-set = j-set).  Given the upstream gradient
+ * g = dL/da, returns dL/dr (rb) and dL/dm (mb):
+ *   rb_k = sum_j T_kj (m_k g_j - m_j g_k),  T = s^-3/2 I - 3 s^-5/2 r r^T,
+ *   mb_k = sum_j g_j . (r_k - r_j) s^-3/2,  r = r_k - r_j, s = r^2 + e2_k + e2_j.
+ * Same tiling and precisions as tg_acc. */
+int tg_acc_vjp(size_t n, const double *m, const double *rx, const double *ry, const double *rz,
+               const double *e2, const double *gx, const double *gy, const double *gz,
+               double *rbx, double *rby, double *rbz, double *mb, int prec, void *stream);
+
 /* ---------------------------------------------------------------------- */
 /* Integrator updates (device pointers, FP64, asynchronous on `stream`).   */
 /* Fused forms of the reference integrators' numpy updates, evaluated in   */

@@ -55,14 +55,15 @@ def test_gpu_integrator_matches_reference_trajectory(modules, method):
         assert np.array_equal(got, want), method
 
 
-def test_config1_ahermite4_plummer_4096_matches_oracle(modules):
-    from oracle import integrators as oi
+def test_config1_ahermite4_plummer_4096_full_run(modules):
+    """Configuration 1 at full size against tests/golden/golden_config1.npz
+    (made by tests/golden/make_config1.py with the CPU restatement of the
+    reference integrator): same step count, bit-identical final state."""
+    import os
+    from golden_io import GOLDEN
     from tupan_gb300.ics import plummer_arrays
-    d = plummer_arrays(4096, eps=0.01, seed=4096)
-    d["eps2"] = np.full(4096, 0.5e-4)          # pair softening e2 = 1e-4
-    n, t, got = run_gpu(modules, d, "ahermite4", 0.01, 0.125)
-    ref = oi.integrator("ahermite4", 0.01, oi.make_ps(d), oi.Kernels(nthreads=16))
-    ref.run(0.125)
-    want = np.stack([ref.ps[f] for f in RV])
-    assert t == ref.t_curr
-    assert np.array_equal(got, want)
+    g = np.load(os.path.join(GOLDEN, "golden_config1.npz"))
+    d = plummer_arrays(int(g["n"]), float(g["eps"]), seed=int(g["seed"]))
+    n, t, got = run_gpu(modules, d, "ahermite4", float(g["eta"]), float(g["t_end"]))
+    assert n == int(g["steps"]) and t == float(g["t_final"])
+    assert np.array_equal(got, np.stack([g[f] for f in RV]))

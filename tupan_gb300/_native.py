@@ -80,6 +80,8 @@ def _load():
     lib.tg_hermite_predict.argtypes = [ctypes.c_int, ctypes.c_size_t, ctypes.c_double, PP, PP, _DP]
     lib.tg_hermite_correct.restype = ctypes.c_int
     lib.tg_hermite_correct.argtypes = [ctypes.c_int, ctypes.c_size_t, ctypes.c_double, PP, PP, PP, PP, _DP]
+    lib.tg_acc_vjp.restype = ctypes.c_int
+    lib.tg_acc_vjp.argtypes = [ctypes.c_size_t] + [_DP] * 12 + [ctypes.c_int, _DP]
     lib.tg_probe_fma_tflops.restype = ctypes.c_double
     lib.tg_probe_fma_tflops.argtypes = [ctypes.c_int, ctypes.c_int, _DP]
     return lib

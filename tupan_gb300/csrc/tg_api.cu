@@ -101,7 +101,7 @@ int run(int kernel, tg::PairArgs &a, int prec, void *stream) {
     a.status = c->status;
     cudaError_t e;
     if (prec == TG_PREC_FP64 || !tg::ds32_supported(kernel) || a.nj == 0) {
-        e = tg::launch_fp64(kernel, a, s);
+        e = tg::launch_fp64(kernel, a, c->sms, s);
     } else {
         std::lock_guard<std::mutex> lk(c->mu);
         const size_t need = tg::ds32_workspace_bytes(kernel, a.ni, a.nj, c->sms);
@@ -336,6 +336,21 @@ int tg_sakura(size_t ni, const double *im, const double *irx, const double *iry,
     a.out[0] = idrx; a.out[1] = idry; a.out[2] = idrz; a.out[3] = idvx; a.out[4] = idvy; a.out[5] = idvz;
     (void)prec;
     return run(tg::K_SAKURA, a, TG_PREC_FP64, stream);
+}
+
+int tg_acc_vjp(size_t n, const double *m, const double *rx, const double *ry, const double *rz,
+               const double *e2, const double *gx, const double *gy, const double *gz, double *rbx,
+               double *rby, double *rbz, double *mb, int prec, void *stream) {
+    tg::PairArgs a = blank();
+    set5(a.I, m, rx, ry, rz, e2);
+    // every field slot the kernel family validates must be non-null
+    setv(a.I, rx, ry, rz);
+    a.I.f[tg::F_AX] = gx; a.I.f[tg::F_AY] = gy; a.I.f[tg::F_AZ] = gz;
+    a.I.f[tg::F_JX] = gx; a.I.f[tg::F_JY] = gy; a.I.f[tg::F_JZ] = gz;
+    a.J = a.I;
+    a.ni = n; a.nj = n;
+    a.out[0] = rbx; a.out[1] = rby; a.out[2] = rbz; a.out[3] = mb;
+    return run(tg::K_ACC_VJP, a, prec, stream);
 }
 
 // ---------------------------------------------------------------------------

@@ -466,6 +466,54 @@ struct PNAccDS {
     static PackSpec pack() { return PackSpec{12, 6, {F_VX, F_VY, F_VZ, F_M, F_E2, -2}}; }
 };
 
+// Vector-Jacobian product of Acc (see AccVjp64 in tg_fp64.cu for the
+// formulas); the upstream gradient g travels in the acceleration slots.
+template <int IPT_, bool REFINE>
+struct AccVjpDS {
+    static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 4;
+    struct IS { IPos q; float2 e, m, g[3]; float2 o[4]; Comp c[4]; };
+    __device__ static void load(IS &s, const PairArgs &a, size_t i) {
+        load_pos(a, i, s.q);
+        s.e = f2(__double2float_rn(a.I.f[F_E2][i]));
+        s.m = f2(__double2float_rn(a.I.f[F_M][i]));
+        for (int k = 0; k < 3; ++k) s.g[k] = f2(__double2float_rn(a.I.f[F_AX + k][i]));
+        for (int k = 0; k < 4; ++k) { s.o[k] = f2(0.f); s.c[k] = Comp{0.f, 0.f}; }
+    }
+    // record: {xh,yh} {zh,xl} {yl,zl} {m,e2} {gx,gy} {gz,pad}
+    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R) {
+        const float4 q0 = R[0], q1 = R[1], q2 = R[2], q3 = R[3], q4 = R[4], q5 = R[5];
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+            IS &s = S[u];
+            float2 r[3];
+            pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), r[0], r[1], r[2]);
+            const float2 e2 = add2(s.e, hi2(q3));
+            const float2 ss = fma2(r[0], r[0], fma2(r[1], r[1], fma2(r[2], r[2], e2)));
+            float2 y, y2;
+            inv_r_r2(ss, r[0], r[1], r[2], y, y2);
+            const float2 y3 = mul2(y, y2);
+            const float2 mj = lo2(q3);
+            const float2 gj[3] = {lo2(q4), hi2(q4), lo2(q5)};
+            float2 w[3];
+            for (int k = 0; k < 3; ++k) w[k] = fnma2(mj, s.g[k], mul2(s.m, gj[k]));
+            const float2 rw = fma2(r[0], w[0], fma2(r[1], w[1], mul2(r[2], w[2])));
+            const float2 c = mul2(mul2(mul2(y3, y2), f2(3.0f)), rw);
+            for (int k = 0; k < 3; ++k) s.o[k] = fnma2(c, r[k], fma2(y3, w[k], s.o[k]));
+            const float2 gr = fma2(gj[0], r[0], fma2(gj[1], r[1], mul2(gj[2], r[2])));
+            s.o[3] = fma2(gr, y3, s.o[3]);
+        }
+    }
+    __device__ static void fold(IS &s) {
+        for (int k = 0; k < 4; ++k) { comp_add(s.c[k], __fadd_rn(s.o[k].x, s.o[k].y)); s.o[k] = f2(0.f); }
+    }
+    __device__ static void partials(const IS &s, double *p) { for (int k = 0; k < 4; ++k) p[k] = comp_value(s.c[k]); }
+    __device__ static void combine(double *acc, const double *p) { for (int k = 0; k < 4; ++k) acc[k] += p[k]; }
+    __device__ static void store(const double *p, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 4; ++k) a.out[k][i] = p[k];
+    }
+    static PackSpec pack() { return PackSpec{12, 6, {F_M, F_E2, F_AX, F_AY, F_AZ, -2}}; }
+};
+
 // ---------------------------------------------------------------------------
 // Stream-K geometry helpers.
 // ---------------------------------------------------------------------------
@@ -741,6 +789,7 @@ size_t ds32_workspace_bytes(int kernel, size_t ni, size_t nj, int sms) {
         case K_SNAP_CRACKLE: return ws_bytes_for<SnapCrackleDS<1, REF>>(ni, nj, sms);
         case K_TSTEP: return ws_bytes_for<TstepDS<IPT2, REF>>(ni, nj, sms);
         case K_PNACC: return ws_bytes_for<PNAccDS<1, REF>>(ni, nj, sms);
+        case K_ACC_VJP: return ws_bytes_for<AccVjpDS<IPT2, REF>>(ni, nj, sms);
         default: return 0;
     }
 }
@@ -753,6 +802,7 @@ cudaError_t launch_ds32(int kernel, const PairArgs &a, void *ws, size_t ws_bytes
         case K_SNAP_CRACKLE: return run_ds<SnapCrackleDS<1, REF>>(a, ws, ws_bytes, sms, s);
         case K_TSTEP: return run_ds<TstepDS<IPT2, REF>>(a, ws, ws_bytes, sms, s);
         case K_PNACC: return run_ds<PNAccDS<1, REF>>(a, ws, ws_bytes, sms, s);
+        case K_ACC_VJP: return run_ds<AccVjpDS<IPT2, REF>>(a, ws, ws_bytes, sms, s);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -250,19 +250,55 @@ struct Sakura64 {
     }
 };
 
+// Vector-Jacobian product of Acc for one particle set (i-set == j-set):
+//   r-bar_k = sum_j T_kj (m_k g_j - m_j g_k),  T = s^-3/2 I - 3 s^-5/2 r r^T
+//   m-bar_k = sum_j g_j . r_kj s^-3/2,          r = r_k - r_j, s = r^2 + e2
+// with g the upstream gradient dL/da; pairs with r2 = 0 contribute nothing.
+struct AccVjp64 {
+    static constexpr int NF = 14, NO = 4;
+    struct St { double m, x, y, z, e, g[3], rb[3], mb; };
+    __device__ static void init(St &s, const PairArgs &a, size_t i) {
+        s.m = a.I.f[F_M][i]; s.x = a.I.f[F_RX][i]; s.y = a.I.f[F_RY][i]; s.z = a.I.f[F_RZ][i];
+        s.e = a.I.f[F_E2][i];
+        for (int k = 0; k < 3; ++k) { s.g[k] = a.I.f[F_AX + k][i]; s.rb[k] = 0.0; }
+        s.mb = 0.0;
+    }
+    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &) {
+        const double r[3] = {s.x - sj[F_RX][jj], s.y - sj[F_RY][jj], s.z - sj[F_RZ][jj]};
+        const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+        if (!(r2 > 0)) return;
+        const double q2 = 1.0 / (r2 + s.e + sj[F_E2][jj]);
+        const double q3 = q2 * sqrt(q2);
+        const double mj = sj[F_M][jj];
+        double w[3], gj[3];
+        for (int k = 0; k < 3; ++k) {
+            gj[k] = sj[F_AX + k][jj];
+            w[k] = s.m * gj[k] - mj * s.g[k];
+        }
+        const double rw = r[0] * w[0] + r[1] * w[1] + r[2] * w[2];
+        const double c = 3.0 * q3 * q2 * rw;
+        for (int k = 0; k < 3; ++k) s.rb[k] += q3 * w[k] - c * r[k];
+        s.mb += (gj[0] * r[0] + gj[1] * r[1] + gj[2] * r[2]) * q3;
+    }
+    __device__ static void store(const St &s, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 3; ++k) a.out[k][i] = s.rb[k];
+        a.out[3][i] = s.mb;
+    }
+};
+
 // ---------------------------------------------------------------------------
 // Generic sequential-j engine.
 // ---------------------------------------------------------------------------
 template <class K>
 __global__ void __launch_bounds__(F64_THREADS) fp64_pairwise(PairArgs a) {
     __shared__ double sj[K::NF][F64_TILE];
-    const size_t i = (size_t)blockIdx.x * F64_THREADS + threadIdx.x;
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < a.ni;
     typename K::St st;
     K::init(st, a, live ? i : 0);
     for (size_t j0 = 0; j0 < a.nj; j0 += F64_TILE) {
         const int nt = (int)((a.nj - j0) < (size_t)F64_TILE ? (a.nj - j0) : F64_TILE);
-        for (int q = threadIdx.x; q < K::NF * F64_TILE; q += F64_THREADS) {
+        for (int q = threadIdx.x; q < K::NF * F64_TILE; q += blockDim.x) {
             const int f = q / F64_TILE, jj = q % F64_TILE;
             if (jj < nt) sj[f][jj] = a.J.f[f][j0 + jj];
         }
@@ -273,22 +309,32 @@ __global__ void __launch_bounds__(F64_THREADS) fp64_pairwise(PairArgs a) {
     if (live) K::store(st, a, i);
 }
 
+// The FP64 pipe, not occupancy, bounds these kernels, so a few warps per SM
+// suffice; small i-sets use narrower CTAs to spread over more SMs.
+static unsigned fp64_threads(size_t ni, int sms) {
+    for (unsigned t = F64_THREADS; t > 32; t /= 2)
+        if ((ni + t - 1) / t >= (size_t)(sms > 0 ? sms : 1)) return t;
+    return 32;
+}
+
 template <class K>
-static cudaError_t run(const PairArgs &a, cudaStream_t s) {
-    const size_t blocks = (a.ni + F64_THREADS - 1) / F64_THREADS;
-    fp64_pairwise<K><<<(unsigned)blocks, F64_THREADS, 0, s>>>(a);
+static cudaError_t run(const PairArgs &a, int sms, cudaStream_t s) {
+    const unsigned t = fp64_threads(a.ni, sms);
+    const size_t blocks = (a.ni + t - 1) / t;
+    fp64_pairwise<K><<<(unsigned)blocks, t, 0, s>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_fp64(int kernel, const PairArgs &a, cudaStream_t s) {
+cudaError_t launch_fp64(int kernel, const PairArgs &a, int sms, cudaStream_t s) {
     switch (kernel) {
-        case K_PHI: return run<Phi64>(a, s);
-        case K_ACC: return run<Acc64>(a, s);
-        case K_ACC_JERK: return run<AccJerk64>(a, s);
-        case K_SNAP_CRACKLE: return run<SnapCrackle64>(a, s);
-        case K_TSTEP: return run<Tstep64>(a, s);
-        case K_PNACC: return run<PNAcc64>(a, s);
-        case K_SAKURA: return run<Sakura64>(a, s);
+        case K_PHI: return run<Phi64>(a, sms, s);
+        case K_ACC: return run<Acc64>(a, sms, s);
+        case K_ACC_JERK: return run<AccJerk64>(a, sms, s);
+        case K_SNAP_CRACKLE: return run<SnapCrackle64>(a, sms, s);
+        case K_TSTEP: return run<Tstep64>(a, sms, s);
+        case K_PNACC: return run<PNAcc64>(a, sms, s);
+        case K_SAKURA: return run<Sakura64>(a, sms, s);
+        case K_ACC_VJP: return run<AccVjp64>(a, sms, s);
         default: return cudaErrorInvalidValue;
     }
 }

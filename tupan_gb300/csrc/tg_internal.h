@@ -13,15 +13,18 @@ enum Field : int {
     F_AX, F_AY, F_AZ, F_JX, F_JY, F_JZ, F_COUNT
 };
 
-enum Kernel : int { K_PHI = 0, K_ACC, K_ACC_JERK, K_SNAP_CRACKLE, K_TSTEP, K_PNACC, K_SAKURA, K_COUNT };
+enum Kernel : int { K_PHI = 0, K_ACC, K_ACC_JERK, K_SNAP_CRACKLE, K_TSTEP, K_PNACC, K_SAKURA,
+                    K_ACC_VJP, K_COUNT };
+// K_ACC_VJP reads the upstream gradient of the acceleration from the
+// F_AX..F_AZ slots of the particle set and writes r-bar (3) and m-bar (1).
 
 // Number of per-particle input fields each kernel reads (libtupan.h:2-246).
 constexpr int kernel_fields(int k) {
-    return k == K_PHI || k == K_ACC ? 5 : (k == K_SNAP_CRACKLE ? 14 : 8);
+    return k == K_PHI || k == K_ACC ? 5 : (k == K_SNAP_CRACKLE || k == K_ACC_VJP ? 14 : 8);
 }
 // Number of output arrays.
 constexpr int kernel_outputs(int k) {
-    return k == K_PHI ? 1 : (k == K_ACC || k == K_PNACC ? 3 : (k == K_TSTEP ? 2 : 6));
+    return k == K_PHI ? 1 : (k == K_ACC || k == K_PNACC ? 3 : (k == K_TSTEP ? 2 : (k == K_ACC_VJP ? 4 : 6)));
 }
 
 struct PSet {
@@ -41,7 +44,7 @@ struct PairArgs {
 };
 
 // Launchers (stream-ordered, asynchronous).  Return a cudaError_t.
-cudaError_t launch_fp64(int kernel, const PairArgs &a, cudaStream_t s);
+cudaError_t launch_fp64(int kernel, const PairArgs &a, int sms, cudaStream_t s);
 
 // Split-FP32 path: packs j-records into `ws` and runs the stream-K kernel.
 struct Ds32Plan {

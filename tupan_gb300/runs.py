@@ -1,0 +1,232 @@
+"""Named workload runs: the precision, differentiation and binary-cluster
+configurations, each reporting a JSON summary.
+
+    python -m tupan_gb300.runs precision      # Plummer-Salpeter N=65536 SIA21
+    python -m tupan_gb300.runs adjoint        # N=16384 leapfrog gradients
+    python -m tupan_gb300.runs binaries       # 2048 + 64 binaries, PN + Sakura
+
+All inputs are seeded synthetic Plummer spheres (tupan_gb300.ics).
+"""
+import argparse
+import json
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import _native, autodiff
+from .ics import Salpeter, make_binary, plummer_arrays
+from .integrator import Integrator
+from .lib import extensions
+from .particles import ParticleSystem
+
+RV = ("rx", "ry", "rz", "vx", "vy", "vz")
+
+
+def energy(ps):
+    """Total energy K + U with the FP64 Phi kernel (body.py:259-306)."""
+    extensions.Phi("CUDA", "float64").calc(ps, ps)
+    k = 0.5 * float((ps.mass * (ps.vx ** 2 + ps.vy ** 2 + ps.vz ** 2)).sum())
+    u = 0.5 * float((ps.mass * ps.phi).sum())
+    return k + u
+
+
+def force_error(ps):
+    """Per-particle |a_ds32 - a_fp64| / |a_fp64| on the current positions."""
+    a64 = np.stack([o.cpu().numpy() for o in extensions.Acc("CUDA", "float64").calc(ps, ps)])
+    a32 = np.stack([o.cpu().numpy() for o in extensions.Acc("CUDA", "ds32").calc(ps, ps)])
+    r = np.sqrt(((a32 - a64) ** 2).sum(0)) / np.sqrt((a64 ** 2).sum(0))
+    return {"max": float(r.max()), "p999": float(np.percentile(r, 99.9)),
+            "p99": float(np.percentile(r, 99)), "median": float(np.median(r))}
+
+
+def precision_run(n=65536, steps=128, dt=1.0 / 1024, seed=20261203, probe_every=32):
+    """Shared-step SIA21 kdk leapfrog, split FP32 against FP64."""
+    d = plummer_arrays(n, 1e-3, imf=Salpeter(0.1, 100.0), seed=seed)
+    out = {"config": {"n": n, "imf": "salpeter [0.1,100]", "eps2_pair": 1e-6, "method": "sia21s.kdk",
+                      "dt": dt, "steps": steps, "tstep_eta": dt}}
+    for prec in ("ds32", "float64"):
+        extensions.set_precision(prec)
+        ps = ParticleSystem.from_arrays(**d)
+        e0 = energy(ps)
+        integ = Integrator(dt, 0.0, ps, method="sia21s.kdk")
+        probes = []
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for s in range(steps):
+            integ.evolve_step((s + 1) * dt)
+            integ.particle_system.set_tstep(integ.particle_system, dt)
+            if prec == "ds32" and (s + 1) % probe_every == 0:
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                probes.append({"step": s + 1, "force_error": force_error(integ.particle_system)})
+                t0 += time.perf_counter() - t1
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        ps = integ.particle_system
+        e1 = energy(ps)
+        out[prec] = {"e0": e0, "e1": e1, "rel_energy_error": abs((e1 - e0) / e0),
+                     "ms_per_step": 1e3 * wall / steps,
+                     "min_tstep_last": float(ps.tstep.abs().min()),
+                     "final": {f: getattr(ps, f).cpu().numpy() for f in RV}}
+        if probes:
+            out[prec]["force_error_probes"] = probes
+    extensions.set_precision("float64")
+    ps0 = ParticleSystem.from_arrays(**d)
+    out["force_error_step0"] = force_error(ps0)
+    fa, fb = out["ds32"].pop("final"), out["float64"].pop("final")
+    dpos = np.sqrt(sum((fa[f] - fb[f]) ** 2 for f in ("rx", "ry", "rz")))
+    out["trajectory_difference"] = {"max_abs_position": float(dpos.max()), "median": float(np.median(dpos))}
+    out["energy_drift_ratio_ds32_over_fp64"] = out["ds32"]["rel_energy_error"] / max(out["float64"]["rel_energy_error"], 1e-300)
+    return out
+
+
+def adjoint_run(n=16384, steps=64, dt=1.0 / 256, seed=16384, checkpoint_every=8, ncoords=32):
+    """Gradients of a trajectory loss by the Acc adjoint, checked by FP64
+    central finite differences."""
+    d = plummer_arrays(n, 0.01, seed=seed)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    r0 = torch.tensor(np.stack([d["rx"], d["ry"], d["rz"]]), dtype=torch.float64, device=dev)
+    v0 = torch.tensor(np.stack([d["vx"], d["vy"], d["vz"]]), dtype=torch.float64, device=dev)
+    m0 = torch.tensor(d["mass"], dtype=torch.float64, device=dev)
+    e2 = torch.tensor(d["eps2"], dtype=torch.float64, device=dev)
+    rng = np.random.default_rng(seed)
+    noise = torch.tensor(rng.lognormal(0.0, 0.01, n), dtype=torch.float64, device=dev)
+    with torch.no_grad():
+        target, _ = autodiff.leapfrog(r0, v0, m0 * noise, e2, dt, steps, "float64", 0)
+
+    def loss(r, v, m, prec, ck):
+        rf, _ = autodiff.leapfrog(r, v, m, e2, dt, steps, prec, ck)
+        return autodiff.loss_to_target(rf, target)
+
+    out = {"config": {"n": n, "steps": steps, "dt": dt, "eps2_pair": 1e-4, "checkpoint_every": checkpoint_every,
+                      "target": "same ICs, masses x lognormal(sigma=0.01), not renormalised, FP64 run"}}
+    grads = {}
+    for prec in ("ds32", "float64"):
+        r = r0.clone().requires_grad_(True)
+        v = v0.clone().requires_grad_(True)
+        m = m0.clone().requires_grad_(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        L = loss(r, v, m, prec, checkpoint_every)
+        L.backward()
+        torch.cuda.synchronize()
+        grads[prec] = (r.grad, v.grad, m.grad)
+        out[prec] = {"loss": float(L), "seconds_forward_backward": time.perf_counter() - t0,
+                     "peak_mem_mb": torch.cuda.max_memory_allocated() / 2 ** 20}
+    rel = [float((a - b).norm() / b.norm()) for a, b in zip(grads["ds32"], grads["float64"])]
+    out["ds32_vs_fp64_adjoint_rel_norm"] = {"r": rel[0], "v": rel[1], "m": rel[2]}
+    worst64, worst32, checks = 0.0, 0.0, []
+    with torch.no_grad():
+        for q in range(ncoords):
+            which = ("r", "v", "m")[q % 3]
+            base = {"r": r0, "v": v0, "m": m0}[which]
+            idx = tuple(int(rng.integers(0, s)) for s in base.shape)
+            h = 1e-6 * max(abs(float(base[idx])), 1e-3) if which != "m" else 1e-6 * float(base[idx])
+            args_p = {"r": r0, "v": v0, "m": m0}
+            args_m = dict(args_p)
+            bp, bm = base.clone(), base.clone()
+            bp[idx] += h
+            bm[idx] -= h
+            args_p[which], args_m[which] = bp, bm
+            fd = float(loss(args_p["r"], args_p["v"], args_p["m"], "float64", 0)
+                       - loss(args_m["r"], args_m["v"], args_m["m"], "float64", 0)) / (2 * h)
+            k = "rvm".index(which)
+            g64, g32 = float(grads["float64"][k][idx]), float(grads["ds32"][k][idx])
+            scale = max(abs(fd), 1e-12)
+            e64, e32 = abs(g64 - fd) / scale, abs(g32 - fd) / scale
+            worst64, worst32 = max(worst64, e64), max(worst32, e32)
+            checks.append({"coord": which + str(idx), "fd": fd, "adjoint_fp64": g64, "adjoint_ds32": g32})
+    out["finite_difference"] = {"coordinates": ncoords, "max_rel_error_fp64_adjoint": worst64,
+                                "max_rel_error_ds32_adjoint": worst32, "samples": checks[:6]}
+    return out
+
+
+def binaries_run(nbg=2048, nbin=64, t_end=1.0 / 16, dt=1.0 / 1024, clight=1e4, pn_order=5, seed=2176):
+    """Plummer background plus hard binaries: Sakura Kepler-drift steps (FP64)
+    with a post-Newtonian kick (split FP32 PNAcc) split around them
+    (kick tau/2, Sakura step tau, kick tau/2)."""
+    from .integrator.sakura import sakura_step
+    d = plummer_arrays(nbg, 0.0, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    host = rng.choice(nbg, nbin, replace=False)
+    cols = {k: list(d[k]) for k in ("mass", "rx", "ry", "rz", "vx", "vy", "vz")}
+    mpart = 1.0 / (nbg + nbin)
+    for k in range(nbg):
+        cols["mass"][k] = mpart
+    semis, eccs = [], []
+    for h in host:
+        a = math.exp(rng.uniform(math.log(1e-4), math.log(1e-3)))
+        e = 0.9 * math.sqrt(rng.random())
+        ms, rr, vv = make_binary(mpart, mpart, a, e, rng)
+        semis.append(a)
+        eccs.append(e)
+        com_r = np.array([d["rx"][h], d["ry"][h], d["rz"][h]])
+        com_v = np.array([d["vx"][h], d["vy"][h], d["vz"][h]])
+        for c, ax in enumerate("xyz"):
+            cols["r" + ax][h] = com_r[c] + rr[0][c]
+            cols["v" + ax][h] = com_v[c] + vv[0][c]
+            cols["r" + ax].append(com_r[c] + rr[1][c])
+            cols["v" + ax].append(com_v[c] + vv[1][c])
+        cols["mass"].append(mpart)
+    n = nbg + nbin
+    arrays = {k: np.array(v) for k, v in cols.items()}
+    arrays["eps2"] = np.zeros(n)
+    extensions.set_precision("float64")
+    extensions.clight.pn_order = pn_order
+    extensions.clight.clight = clight
+    pn = extensions.PNAcc("CUDA", "ds32")
+    ps = ParticleSystem.from_arrays(**arrays)
+    e0 = energy(ps)
+
+    def pn_kick(ps, tau):
+        pn.calc(ps, ps)
+        ps.vx += ps.pnax * tau
+        ps.vy += ps.pnay * tau
+        ps.vz += ps.pnaz * tau
+
+    steps = int(round(t_end / dt))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        pn_kick(ps, dt / 2)
+        ps = sakura_step(ps, dt)
+        pn_kick(ps, dt / 2)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    status = _native.sync_status(torch.cuda.current_stream().cuda_stream)
+    e1 = energy(ps)
+    # binary separations after the run
+    sep = []
+    for k, h in enumerate(host):
+        j = nbg + k
+        dx = [float(getattr(ps, "r" + ax)[h] - getattr(ps, "r" + ax)[j]) for ax in "xyz"]
+        sep.append(math.sqrt(sum(x * x for x in dx)))
+    return {"config": {"background": nbg, "binaries": nbin, "n": n, "a_range": [1e-4, 1e-3],
+                       "e": "0.9*sqrt(u)", "eps2": 0.0, "pn_order": pn_order, "clight": clight,
+                       "dt": dt, "t_end": t_end, "scheme": "PN kick dt/2, sakura_step dt, PN kick dt/2",
+                       "pnacc_precision": "ds32", "sakura_precision": "float64"},
+            "steps": steps, "ms_per_step": 1e3 * wall / steps, "kepler_status": status,
+            "rel_energy_error_newtonian": abs((e1 - e0) / e0),
+            "binary_separation_over_a": {"min": float(min(s / a for s, a in zip(sep, semis))),
+                                         "max": float(max(s / a for s, a in zip(sep, semis)))}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("which", choices=["precision", "adjoint", "binaries"])
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--n", type=int, default=None)
+    args = ap.parse_args()
+    kw = {}
+    if args.steps:
+        kw["steps"] = args.steps
+    if args.n:
+        kw["n"] = args.n
+    fn = {"precision": precision_run, "adjoint": adjoint_run, "binaries": binaries_run}[args.which]
+    print(json.dumps(fn(**kw), default=float))
+
+
+if __name__ == "__main__":
+    main()
