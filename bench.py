@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--particles", type=int, default=N_DEFAULT)
     ap.add_argument("--cpu-seconds", type=float, default=3.0,
                     help="target wall time of each CPU baseline sample")
     ap.add_argument("--no-fp64", action="store_true")
@@ -112,7 +112,7 @@ def reference_arm(args, rank, world):
         return
     from oracle import oracle as om
     om.build()
-    d = workload(args.n, 0)
+    d = workload(args.particles, 0)
     threads = os.cpu_count() or 1
     for _ in range(max(args.warmup, 0)):
         cpu_sample(d, min(args.cpu_seconds, 1.0), threads)
@@ -124,7 +124,7 @@ def reference_arm(args, rank, world):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Gint/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / len(vals),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": config(args.n), "cpu_baseline": base,
+            "data": "synthetic", "config": config(args.particles), "cpu_baseline": base,
             "e2e": {"value": v, "unit": "Gint/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -201,7 +201,7 @@ def ours(args, rank, world, dist):
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
-    n = args.n
+    n = args.particles
     d = workload(n, rank)
     T = {k: torch.tensor(d[k], dtype=torch.float64, device=dev) for k in P8}
     outs = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(9)]
