@@ -46,6 +46,9 @@ EPS = 1e-3
 SEED = 20261203
 FLOP_ACC = 20       # tupan/lib/src/acc_kernel_common.h:38
 FLOP_ACC_JERK = 42  # tupan/lib/src/acc_jerk_kernel_common.h:56
+# DRAM bytes (read + write) of one split-FP32 AccJerk launch on this workload,
+# from an ncu capture (profiles/ds32_acc_jerk_n65536.txt)
+TRAFFIC_ACC_JERK_N65536 = 6.86e6
 METRIC = "Gint/s Acc+AccJerk split-FP32 (N=65536 Plummer-Salpeter, eps2=1e-6)"
 P5 = ("mass", "rx", "ry", "rz", "eps2")
 P8 = P5 + ("vx", "vy", "vz")
@@ -276,7 +279,9 @@ def ours(args, rank, world, dist):
                         "acc_jerk_ds32": {"ms": aj_ms, "gint_s": n * n / (aj_ms * 1e-3) / 1e9}},
             "roofline": {"bound": "fp32", "kernel": "ds32_streamk<AccJerkDS>",
                          "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
-                         "frac": achieved / peak32 if peak32 > 0 else None, "traffic": None,
+                         "frac": achieved / peak32 if peak32 > 0 else None,
+                         "traffic": TRAFFIC_ACC_JERK_N65536 if n == N_DEFAULT else None,
+                         "traffic_source": "ncu dram__bytes_read+write of one AccJerk launch at N=65536",
                          "flop_per_interaction": FLOP_ACC_JERK,
                          "peak_source": "measured: tg_probe_fma_tflops (FFMA2 chains, this GPU)",
                          "peak_fp64_tflops": peak64,

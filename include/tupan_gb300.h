@@ -145,6 +145,37 @@ int tg_sakura(size_t ni, const double *im, const double *irx, const double *iry,
               double *idrx, double *idry, double *idrz,
               double *idvx, double *idvy, double *idvz, int prec, void *stream);
 
+/* ---------------------------------------------------------------------- */
+/* Ensembles: many independent clusters in one launch.  No counterpart in  */
+/* the reference (which calls its kernels once per particle set).          */
+/* Cluster k is particles [start[k], start[k] + count[k]) of the arrays     */
+/* passed to the segmented calls and interacts only with itself; results   */
+/* per cluster equal the single-set calls (bit for bit in FP64).  The      */
+/* split-FP32 form runs all clusters' (i-tile, j-tile) units as one         */
+/* stream-K launch; its first call per kernel times a few tile/grid        */
+/* variants on the stream and keeps the fastest (make it before any stream */
+/* capture).  Later calls are capturable in a CUDA graph.                  */
+/* ---------------------------------------------------------------------- */
+typedef struct tg_segments tg_segments;
+/* host arrays; segments must not overlap; NULL on error (tg_last_error) */
+tg_segments *tg_segments_create(size_t nseg, const long long *start, const long long *count);
+void tg_segments_destroy(tg_segments *seg);
+int tg_phi_segmented(tg_segments *seg, const double *m, const double *rx, const double *ry,
+                     const double *rz, const double *e2, double *phi, int prec, void *stream);
+int tg_acc_segmented(tg_segments *seg, const double *m, const double *rx, const double *ry,
+                     const double *rz, const double *e2, double *ax, double *ay, double *az,
+                     int prec, void *stream);
+int tg_acc_jerk_segmented(tg_segments *seg, const double *m, const double *rx, const double *ry,
+                          const double *rz, const double *e2, const double *vx, const double *vy,
+                          const double *vz, double *ax, double *ay, double *az,
+                          double *jx, double *jy, double *jz, int prec, void *stream);
+int tg_snap_crackle_segmented(tg_segments *seg, const double *m, const double *rx, const double *ry,
+                              const double *rz, const double *e2, const double *vx, const double *vy,
+                              const double *vz, const double *ax, const double *ay, const double *az,
+                              const double *jx, const double *jy, const double *jz,
+                              double *sx, double *sy, double *sz, double *cx, double *cy, double *cz,
+                              int prec, void *stream);
+
 /* No counterpart in the reference: vector-Jacobian product of acc_kernel
  * for one particle set (i-set = j-set).  Given the upstream gradient
  * g = dL/da, returns dL/dr (rb) and dL/dm (mb):

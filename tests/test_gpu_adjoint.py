@@ -37,7 +37,7 @@ def naive_acc(r, m, e2):
     s = r2 + e2[:, None] + e2[None, :]
     mask = r2 > 0
     q3 = torch.where(mask, s ** -1.5, torch.zeros_like(s))
-    return -(d * (m[None, None, :] * q3)[None]).sum(2)
+    return -(d * (m[None, :] * q3)[None]).sum(2)
 
 
 @pytest.mark.parametrize("prec,tol", [("float64", 1e-10), ("ds32", 1e-4)])

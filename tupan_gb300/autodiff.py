@@ -91,7 +91,7 @@ def leapfrog(r, v, m, e2, dt, steps, prec="ds32", checkpoint_every=8):
     a = acc(r, m, e2, prec)
     done = 0
     while done < steps:
-        k = min(checkpoint_every, steps - done)
+        k = min(checkpoint_every, steps - done) if checkpoint_every else steps - done
         if checkpoint_every and torch.is_grad_enabled():
             r, v, a = checkpoint(_kdk_block, r, v, a, m, e2, dt, k, prec, use_reentrant=False)
         else:

@@ -6,7 +6,10 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <algorithm>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "../../include/tupan_gb300.h"
 #include "tg_device.cuh"
@@ -487,6 +490,249 @@ void sakura_kernel(const unsigned long ni, const double *_im, const double *_irx
                          j[3], j[4], j[5], j[6], j[7], dt, flag, o[0], o[1], o[2], o[3], o[4], o[5],
                          TG_PREC_FP64, s);
     });
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Segmented (ensemble) entry points.
+// ---------------------------------------------------------------------------
+struct tg_segments {
+    int dev = 0;
+    long long C = 0, n_total = 0;
+    std::vector<long long> start, count;
+    long long *d_tab[2] = {nullptr, nullptr};   // ds32 tables for 1 and 2 i-particles per thread
+    tg::SegGeometry geo[2];
+    long long *d_fp64 = nullptr;                // block_off[C+1], seg_start[C], seg_n[C]
+    long long fp64_blocks = 0;
+    int fp64_threads = 128;
+    struct Tune { int ipt = 0, mult = 0; };
+    Tune tune[tg::K_COUNT];
+};
+
+namespace {
+
+long long cdiv(long long a, long long b) { return (a + b - 1) / b; }
+
+int upload(long long **dst, const std::vector<long long> &v) {
+    if (cudaMalloc(dst, v.size() * sizeof(long long)) != cudaSuccess) return TG_ENOMEM;
+    if (cudaMemcpy(*dst, v.data(), v.size() * sizeof(long long), cudaMemcpyHostToDevice) != cudaSuccess)
+        return TG_ECUDA;
+    return TG_OK;
+}
+
+// Candidates (i-particles per thread, grid multiple) timed on the first
+// call outside stream capture; the fastest is kept for this ensemble.
+const int TUNE_IPT[2] = {2, 1};
+const int TUNE_MULT[2] = {1, 2};
+
+int run_segmented(int kernel, tg_segments *sg, tg::PairArgs &a, int prec, void *stream) {
+    g_err.clear();
+    if (!sg) return fail(TG_EINVAL, "null segment table");
+    if (prec != TG_PREC_FP64 && prec != TG_PREC_DS32) return fail(TG_EINVAL, "unknown precision");
+    const int nf = tg::kernel_fields(kernel), no = tg::kernel_outputs(kernel);
+    if (sg->n_total > 0) {
+        for (int f = 0; f < nf; ++f)
+            if (!a.I.f[f]) return fail(TG_EINVAL, "null particle pointer");
+        for (int o = 0; o < no; ++o)
+            if (!a.out[o]) return fail(TG_EINVAL, "null output pointer");
+    }
+    a.J = a.I;
+    a.ni = a.nj = (size_t)sg->n_total;
+    if (sg->n_total == 0) return TG_OK;
+    DevCtx *c = nullptr;
+    int rc = current_ctx(&c);
+    if (rc != TG_OK) return rc;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev != sg->dev) return fail(TG_EINVAL, "segment table was created on another device");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    a.status = c->status;
+    cudaError_t e;
+    if (prec == TG_PREC_FP64) {
+        const long long *t = sg->d_fp64;
+        e = tg::launch_fp64_seg(kernel, a, sg->C, sg->fp64_blocks, sg->fp64_threads, t, t + sg->C + 1,
+                                t + 2 * sg->C + 1, s);
+        if (e != cudaSuccess) return fail(TG_ECUDA, "segmented kernel launch", e);
+        return TG_OK;
+    }
+    std::lock_guard<std::mutex> lk(c->mu);
+    const int nipt = kernel == tg::K_SNAP_CRACKLE ? 1 : 2;
+    size_t need = 0;
+    for (int q = 0; q < nipt; ++q) {
+        const int ipt = kernel == tg::K_SNAP_CRACKLE ? 1 : TUNE_IPT[q];
+        for (int m = 0; m < 2; ++m) {
+            const size_t b = tg::ds32_seg_workspace_bytes(kernel, ipt, sg->geo[ipt - 1], c->sms, TUNE_MULT[m]);
+            need = b > need ? b : need;
+        }
+    }
+    rc = ensure_ws(*c, need, s);
+    if (rc != TG_OK) return rc;
+    tg_segments::Tune &tu = sg->tune[kernel];
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &cs);
+    if (tu.ipt == 0 && cs == cudaStreamCaptureStatusNone) {
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        float best = 1e30f;
+        for (int q = 0; q < nipt; ++q) {
+            const int ipt = kernel == tg::K_SNAP_CRACKLE ? 1 : TUNE_IPT[q];
+            for (int m = 0; m < 2; ++m) {
+                e = tg::launch_ds32_seg(kernel, ipt, a, sg->geo[ipt - 1], c->ws, c->ws_bytes, c->sms,
+                                        TUNE_MULT[m], s);   // warm-up
+                cudaEventRecord(e0, s);
+                for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep)
+                    e = tg::launch_ds32_seg(kernel, ipt, a, sg->geo[ipt - 1], c->ws, c->ws_bytes, c->sms,
+                                            TUNE_MULT[m], s);
+                cudaEventRecord(e1, s);
+                if (e != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+                    cudaEventDestroy(e0);
+                    cudaEventDestroy(e1);
+                    return fail(TG_ECUDA, "segmented autotune launch", e);
+                }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms < best) { best = ms; tu.ipt = ipt; tu.mult = TUNE_MULT[m]; }
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    const int ipt = tu.ipt ? tu.ipt : (kernel == tg::K_SNAP_CRACKLE ? 1 : 2);
+    const int mult = tu.mult ? tu.mult : 1;
+    e = tg::launch_ds32_seg(kernel, ipt, a, sg->geo[ipt - 1], c->ws, c->ws_bytes, c->sms, mult, s);
+    if (e != cudaSuccess) return fail(TG_ECUDA, "segmented kernel launch", e);
+    return TG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+tg_segments *tg_segments_create(size_t nseg, const long long *start, const long long *count) {
+    g_err.clear();
+    if (nseg > 0 && (!start || !count)) { fail(TG_EINVAL, "null segment arrays"); return nullptr; }
+    std::vector<std::pair<long long, long long>> iv;
+    long long n_total = 0;
+    for (size_t k = 0; k < nseg; ++k) {
+        if (start[k] < 0 || count[k] < 0 || count[k] > (1LL << 31)) {
+            fail(TG_EINVAL, "segment start/count out of range");
+            return nullptr;
+        }
+        iv.push_back({start[k], start[k] + count[k]});
+        n_total = std::max(n_total, start[k] + count[k]);
+    }
+    std::vector<std::pair<long long, long long>> sorted = iv;
+    std::sort(sorted.begin(), sorted.end());
+    long long max_end = 0;
+    for (const auto &r : sorted) {
+        if (r.second == r.first) continue;   // empty segments overlap nothing
+        if (r.first < max_end) {
+            fail(TG_EINVAL, "segments overlap");
+            return nullptr;
+        }
+        max_end = std::max(max_end, r.second);
+    }
+    DevCtx *c = nullptr;
+    if (current_ctx(&c) != TG_OK) return nullptr;
+    tg_segments *sg = new tg_segments();
+    cudaGetDevice(&sg->dev);
+    sg->C = (long long)nseg;
+    sg->n_total = n_total;
+    sg->start.assign(start, start + nseg);
+    sg->count.assign(count, count + nseg);
+    const long long C = sg->C, TJ = tg::ds32_tile_j();
+    int rc = TG_OK;
+    for (int q = 0; q < 2 && rc == TG_OK; ++q) {
+        const long long BI = tg::ds32_tile_i(tg::K_ACC_JERK, q + 1);
+        std::vector<long long> tab;
+        tab.reserve(5 * C + 3);
+        long long u = 0, it = 0, rt = 0;
+        std::vector<long long> uo(1, 0), io(1, 0), ro(1, 0);
+        for (long long k = 0; k < C; ++k) {
+            const long long n = sg->count[k];
+            const long long nit = cdiv(n, BI), njt = cdiv(n, TJ);
+            u += nit * njt; it += nit; rt += njt;
+            uo.push_back(u); io.push_back(it); ro.push_back(rt);
+        }
+        tab.insert(tab.end(), uo.begin(), uo.end());
+        tab.insert(tab.end(), io.begin(), io.end());
+        tab.insert(tab.end(), ro.begin(), ro.end());
+        tab.insert(tab.end(), sg->start.begin(), sg->start.end());
+        tab.insert(tab.end(), sg->count.begin(), sg->count.end());
+        rc = upload(&sg->d_tab[q], tab);
+        sg->geo[q] = tg::SegGeometry{C, u, it, rt, sg->d_tab[q]};
+    }
+    // FP64: narrow CTAs while the ensemble would leave SMs idle
+    int t = 128;
+    auto blocks_for = [&](int th) {
+        long long b = 0;
+        for (long long k = 0; k < C; ++k) b += cdiv(sg->count[k], th);
+        return b;
+    };
+    while (t > 32 && blocks_for(t) < c->sms) t /= 2;
+    sg->fp64_threads = t;
+    std::vector<long long> ft(1, 0);
+    for (long long k = 0; k < C; ++k) ft.push_back(ft.back() + cdiv(sg->count[k], t));
+    sg->fp64_blocks = ft.back();
+    ft.insert(ft.end(), sg->start.begin(), sg->start.end());
+    ft.insert(ft.end(), sg->count.begin(), sg->count.end());
+    if (rc == TG_OK) rc = upload(&sg->d_fp64, ft);
+    if (rc != TG_OK) {
+        fail(rc, "segment table upload failed");
+        tg_segments_destroy(sg);
+        return nullptr;
+    }
+    return sg;
+}
+
+void tg_segments_destroy(tg_segments *sg) {
+    if (!sg) return;
+    for (int q = 0; q < 2; ++q)
+        if (sg->d_tab[q]) cudaFree(sg->d_tab[q]);
+    if (sg->d_fp64) cudaFree(sg->d_fp64);
+    delete sg;
+}
+
+int tg_phi_segmented(tg_segments *sg, const double *m, const double *rx, const double *ry,
+                     const double *rz, const double *e2, double *phi, int prec, void *stream) {
+    tg::PairArgs a = blank();
+    set5(a.I, m, rx, ry, rz, e2);
+    a.out[0] = phi;
+    return run_segmented(tg::K_PHI, sg, a, prec, stream);
+}
+
+int tg_acc_segmented(tg_segments *sg, const double *m, const double *rx, const double *ry,
+                     const double *rz, const double *e2, double *ax, double *ay, double *az, int prec,
+                     void *stream) {
+    tg::PairArgs a = blank();
+    set5(a.I, m, rx, ry, rz, e2);
+    a.out[0] = ax; a.out[1] = ay; a.out[2] = az;
+    return run_segmented(tg::K_ACC, sg, a, prec, stream);
+}
+
+int tg_acc_jerk_segmented(tg_segments *sg, const double *m, const double *rx, const double *ry,
+                          const double *rz, const double *e2, const double *vx, const double *vy,
+                          const double *vz, double *ax, double *ay, double *az, double *jx, double *jy,
+                          double *jz, int prec, void *stream) {
+    tg::PairArgs a = blank();
+    set5(a.I, m, rx, ry, rz, e2); setv(a.I, vx, vy, vz);
+    a.out[0] = ax; a.out[1] = ay; a.out[2] = az; a.out[3] = jx; a.out[4] = jy; a.out[5] = jz;
+    return run_segmented(tg::K_ACC_JERK, sg, a, prec, stream);
+}
+
+int tg_snap_crackle_segmented(tg_segments *sg, const double *m, const double *rx, const double *ry,
+                              const double *rz, const double *e2, const double *vx, const double *vy,
+                              const double *vz, const double *ax, const double *ay, const double *az,
+                              const double *jx, const double *jy, const double *jz, double *sx, double *sy,
+                              double *sz, double *cx, double *cy, double *cz, int prec, void *stream) {
+    tg::PairArgs a = blank();
+    set5(a.I, m, rx, ry, rz, e2); setv(a.I, vx, vy, vz);
+    a.I.f[tg::F_AX] = ax; a.I.f[tg::F_AY] = ay; a.I.f[tg::F_AZ] = az;
+    a.I.f[tg::F_JX] = jx; a.I.f[tg::F_JY] = jy; a.I.f[tg::F_JZ] = jz;
+    a.out[0] = sx; a.out[1] = sy; a.out[2] = sz; a.out[3] = cx; a.out[4] = cy; a.out[5] = cz;
+    return run_segmented(tg::K_SNAP_CRACKLE, sg, a, prec, stream);
 }
 
 }  // extern "C"

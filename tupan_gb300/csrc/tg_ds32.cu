@@ -179,9 +179,10 @@ struct AccDS {
             pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), dx, dy, dz);
             const float2 e2 = add2(s.e, hi2(q3));
             const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
-            float2 y, y2;
-            if (REFINE) { y = inv_r<true>(ss, dx, dy, dz); y2 = mul2(y, y); }
-            else inv_r_r2(ss, dx, dy, dz, y, y2);
+            // 1/r^2 from y*y here: with one more MUFU per pair Acc would be
+            // XU-bound (18 packed FP32 ops vs 4 MUFU per two pairs)
+            const float2 y = inv_r<REFINE>(ss, dx, dy, dz);
+            const float2 y2 = mul2(y, y);
             const float2 mr3 = mul2(mul2(lo2(q3), y), y2);
             s.a[0] = fnma2(mr3, dx, s.a[0]);
             s.a[1] = fnma2(mr3, dy, s.a[1]);
@@ -667,6 +668,215 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// Segmented (ensemble) form: many independent clusters in one launch.
+// Cluster c owns particles [seg_start[c], seg_start[c] + seg_n[c]) and
+// interacts only with itself.  Its (i-tile x j-tile) units are numbered
+// after those of the previous clusters (unit_off), so the stream-K split
+// runs over all clusters at once; its j-records start at record tile
+// rec_tile_off[c]; its i-tiles are numbered itile_off[c] + t for the
+// tickets.  A CTA's unit range may span clusters.
+// ---------------------------------------------------------------------------
+struct DsSegArgs {
+    PairArgs p;
+    const float4 *rec;
+    double *part;
+    int *ticket;
+    const long long *unit_off, *itile_off, *rec_tile_off, *seg_start, *seg_n;
+    long long C, U;
+};
+
+// largest c in [0, C) with off[c] <= u (off nondecreasing, off[C] > u)
+__device__ __forceinline__ long long seg_find(const long long *off, long long C, long long u) {
+    long long lo = 0, hi = C;
+    while (hi - lo > 1) {
+        const long long mid = (lo + hi) >> 1;
+        if (__ldg(off + mid) <= u) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void ds32_pack_seg(PSet J, const long long *rec_tile_off, const long long *seg_start,
+                              const long long *seg_n, long long C, size_t npairs, PackSpec ps, float *rec) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= npairs * 2) return;
+    const size_t p = t >> 1;
+    const int lane = (int)(t & 1);
+    const long long c = seg_find(rec_tile_off, C, (long long)(p / DS_PAIRS));
+    const long long lj = 2 * ((long long)p - rec_tile_off[c] * DS_PAIRS) + lane;
+    const bool valid = lj < seg_n[c];
+    const size_t j = (size_t)(seg_start[c] + (valid ? lj : 0));
+    float *r = rec + p * (size_t)(2 * ps.jf);
+    float h, l;
+    for (int q = 0; q < 3; ++q) {
+        split_ds(valid ? J.f[F_RX + q][j] : 0.0, h, l);
+        r[2 * (R_XH + q) + lane] = h;
+        r[2 * (R_XL + q) + lane] = l;
+    }
+    for (int q = 0; q < ps.nextra; ++q) {
+        const int f = ps.extra[q];
+        float v;
+        if (f == -1) v = valid ? 1.0f : 0.0f;
+        else if (f == -2) v = 0.0f;
+        else if (f == F_E2) v = valid ? __double2float_rn(J.f[f][j]) : 1.0f;
+        else v = valid ? __double2float_rn(J.f[f][j]) : 0.0f;
+        r[2 * (6 + q) + lane] = v;
+    }
+}
+
+template <class K>
+__global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsSegArgs a) {
+    extern __shared__ __align__(128) float4 ring[];
+    __shared__ __align__(8) uint64_t full[DS_STAGES];
+    __shared__ int s_last;
+    constexpr int IPT = K::IPT;
+    constexpr int TILE_Q = DS_PAIRS * K::NQ;
+    constexpr unsigned TILE_BYTES = TILE_Q * sizeof(float4);
+    constexpr int BI = DS_THREADS * IPT;
+
+    const long long U = a.U;
+    const long long G = gridDim.x;
+    const long long k = blockIdx.x;
+    const long long u0 = unit_start(k, U, G), u1 = unit_start(k + 1, U, G);
+    if (u0 >= u1) return;
+    const int tid = threadIdx.x;
+
+    if (tid == 0) {
+        for (int s = 0; s < DS_STAGES; ++s) mbar_init(&full[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    long long pc = seg_find(a.unit_off, a.C, u0);   // producer's cluster cursor (tid 0)
+    auto issue = [&](long long u, int s) {
+        while (a.unit_off[pc + 1] <= u) ++pc;
+        const long long njt = a.rec_tile_off[pc + 1] - a.rec_tile_off[pc];
+        const long long jt = (u - a.unit_off[pc]) % njt;
+        mbar_expect_tx(&full[s], TILE_BYTES);
+        bulk_g2s(ring + s * TILE_Q, a.rec + (a.rec_tile_off[pc] + jt) * TILE_Q, TILE_BYTES, &full[s]);
+    };
+    if (tid == 0) {
+        for (int s = 0; s < DS_STAGES && u0 + s < u1; ++s) issue(u0 + s, s);
+    }
+
+    // the unit's cluster, local i-tile and global i-tile
+    long long c = seg_find(a.unit_off, a.C, u0);
+    auto tile_of = [&](long long cl, long long u) {
+        const long long njt = a.rec_tile_off[cl + 1] - a.rec_tile_off[cl];
+        return (u - a.unit_off[cl]) / njt;
+    };
+    long long t = tile_of(c, u0);
+    const long long git_first = a.itile_off[c] + t;
+    typename K::IS st[IPT];
+    auto load_tile = [&](long long cl, long long tt) {
+#pragma unroll
+        for (int q = 0; q < IPT; ++q) {
+            const long long li = tt * BI + q * DS_THREADS + tid;
+            const size_t i = (size_t)(a.seg_start[cl] + (li < a.seg_n[cl] ? li : 0));
+            K::load(st[q], a.p, i);
+        }
+    };
+    load_tile(c, t);
+    bool aborted = false;
+    long long abort_u = u1;
+    long long issued_to = (u0 + DS_STAGES < u1) ? u0 + DS_STAGES : u1;
+
+    for (long long u = u0, it = 0; u < u1; ++u, ++it) {
+        const int s = (int)(it % DS_STAGES);
+        const uint32_t parity = (uint32_t)((it / DS_STAGES) & 1);
+        if (!mbar_wait(&full[s], parity)) aborted = true;
+        if (__syncthreads_or(aborted)) {
+            aborted = true;
+            abort_u = u;
+            break;
+        }
+        const float4 *R = ring + s * TILE_Q;
+#pragma unroll 1
+        for (int fb = 0; fb < DS_PAIRS; fb += DS_FOLD_PAIRS) {
+#pragma unroll DS_UNROLL
+            for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) K::step(st, R + (fb + pp) * K::NQ);
+#pragma unroll
+            for (int q = 0; q < IPT; ++q) K::fold(st[q]);
+        }
+        __syncthreads();
+        if (tid == 0 && u + DS_STAGES < u1) {
+            issue(u + DS_STAGES, s);
+            issued_to = u + DS_STAGES + 1;
+        }
+        // next unit's cluster and tile
+        long long cn = c, tn = -1;
+        if (u + 1 < u1) {
+            while (a.unit_off[cn + 1] <= u + 1) ++cn;
+            tn = tile_of(cn, u + 1);
+        }
+        if (cn == c && tn == t) continue;
+
+        const long long njt = a.rec_tile_off[c + 1] - a.rec_tile_off[c];
+        const long long ta = a.unit_off[c] + t * njt, tb = ta + njt;
+        const long long git = a.itile_off[c] + t;
+        if (ta >= u0 && tb <= u1) {
+#pragma unroll
+            for (int q = 0; q < IPT; ++q) {
+                const long long li = t * BI + q * DS_THREADS + tid;
+                double p[K::NP];
+                K::partials(st[q], p);
+                if (li < a.seg_n[c]) K::store(p, a.p, (size_t)(a.seg_start[c] + li));
+            }
+        } else {
+            const int slot = (git == git_first) ? 0 : 1;
+            double *mine = a.part + ((k * 2 + slot) * IPT * K::NP) * DS_THREADS;
+#pragma unroll
+            for (int q = 0; q < IPT; ++q) {
+                double p[K::NP];
+                K::partials(st[q], p);
+                for (int v = 0; v < K::NP; ++v) mine[(q * K::NP + v) * DS_THREADS + tid] = p[v];
+            }
+            __threadfence();
+            __syncthreads();
+            const long long klo = unit_owner(ta, U, G), khi = unit_owner(tb - 1, U, G);
+            if (tid == 0) {
+                const int prev = atomicAdd(&a.ticket[git], 1);
+                s_last = (prev == (int)(khi - klo));
+            }
+            __syncthreads();
+            if (s_last) {
+                __threadfence();
+                for (int q = 0; q < IPT; ++q) {
+                    double acc[K::NP];
+                    for (long long kk = klo; kk <= khi; ++kk) {
+                        const long long us = unit_start(kk, U, G);
+                        const long long ck = seg_find(a.unit_off, a.C, us);
+                        const int sl = (git == a.itile_off[ck] + tile_of(ck, us)) ? 0 : 1;
+                        const double *src = a.part + ((kk * 2 + sl) * IPT * K::NP) * DS_THREADS;
+                        double v[K::NP];
+                        for (int w = 0; w < K::NP; ++w) v[w] = __ldcg(src + (q * K::NP + w) * DS_THREADS + tid);
+                        if (kk == klo) {
+                            for (int w = 0; w < K::NP; ++w) acc[w] = v[w];
+                        } else {
+                            K::combine(acc, v);
+                        }
+                    }
+                    const long long li = t * BI + q * DS_THREADS + tid;
+                    if (li < a.seg_n[c]) K::store(acc, a.p, (size_t)(a.seg_start[c] + li));
+                }
+            }
+        }
+        if (tn >= 0) {
+            c = cn;
+            t = tn;
+            load_tile(c, t);
+        }
+    }
+
+    if (aborted && tid == 0) {
+        atomicOr(a.p.status, ST_MBAR_TIMEOUT);
+        for (long long u = abort_u; u < issued_to; ++u) {
+            const long long it = u - u0;
+            mbar_wait(&full[it % DS_STAGES], (uint32_t)((it / DS_STAGES) & 1));
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Host side.
 // ---------------------------------------------------------------------------
@@ -770,6 +980,73 @@ static cudaError_t run_ds_capped(const PairArgs &p, void *ws, size_t ws_bytes, i
     return cudaGetLastError();
 }
 
+
+// ---------------------------------------------------------------------------
+// Segmented launch.  Host tables (per cluster, nondecreasing prefixes) are
+// built by the caller for this kernel's i-tile size; `dev` points to the
+// same tables on the device in the order unit_off[C+1], itile_off[C+1],
+// rec_tile_off[C+1], seg_start[C], seg_n[C].
+// ---------------------------------------------------------------------------
+template <class K>
+static int ds32_bi() { return DS_THREADS * K::IPT; }
+
+template <class K>
+static int ctas_per_sm_seg() {
+    static int cached = -1;
+    if (cached < 0) {
+        const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
+        cudaFuncSetAttribute(ds32_streamk_seg<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ds32_streamk_seg<K>, DS_THREADS, smem) != cudaSuccess || n < 1)
+            n = 1;
+        cached = n;
+    }
+    return cached;
+}
+
+template <class K>
+static size_t seg_ws_bytes(long long U, long long NIT, long long NJT, int sms, int grid_mult) {
+    const long long slots = (long long)sms * ctas_per_sm_seg<K>() * (grid_mult > 0 ? grid_mult : 1);
+    const long long grid = U < slots ? U : slots;
+    return align_up((size_t)NJT * DS_PAIRS * K::NQ * sizeof(float4), 256) +
+           align_up((size_t)grid * 2 * K::IPT * K::NP * DS_THREADS * sizeof(double), 256) +
+           align_up((size_t)NIT * sizeof(int), 256);
+}
+
+template <class K>
+static cudaError_t run_ds_seg(const PairArgs &p, const SegGeometry &g, void *ws, size_t ws_bytes, int sms,
+                              int grid_mult, cudaStream_t s) {
+    if (g.U == 0) return cudaSuccess;
+    const long long slots = (long long)sms * ctas_per_sm_seg<K>() * (grid_mult > 0 ? grid_mult : 1);
+    const long long grid = g.U < slots ? g.U : slots;
+    const size_t rec_bytes = align_up((size_t)g.NJT * DS_PAIRS * K::NQ * sizeof(float4), 256);
+    const size_t part_bytes = align_up((size_t)grid * 2 * K::IPT * K::NP * DS_THREADS * sizeof(double), 256);
+    const size_t ticket_bytes = align_up((size_t)g.NIT * sizeof(int), 256);
+    if (rec_bytes + part_bytes + ticket_bytes > ws_bytes) return cudaErrorInvalidValue;
+    char *base = static_cast<char *>(ws);
+    DsSegArgs a;
+    a.p = p;
+    a.rec = reinterpret_cast<const float4 *>(base);
+    a.part = reinterpret_cast<double *>(base + rec_bytes);
+    a.ticket = reinterpret_cast<int *>(base + rec_bytes + part_bytes);
+    a.C = g.C;
+    a.U = g.U;
+    a.unit_off = g.dev;
+    a.itile_off = g.dev + (g.C + 1);
+    a.rec_tile_off = g.dev + 2 * (g.C + 1);
+    a.seg_start = g.dev + 3 * (g.C + 1);
+    a.seg_n = g.dev + 3 * (g.C + 1) + g.C;
+    const size_t npairs = (size_t)g.NJT * DS_PAIRS;
+    const unsigned pack_blocks = (unsigned)((npairs * 2 + 255) / 256);
+    ds32_pack_seg<<<pack_blocks, 256, 0, s>>>(p.J, a.rec_tile_off, a.seg_start, a.seg_n, g.C, npairs,
+                                              K::pack(), reinterpret_cast<float *>(base));
+    cudaError_t e = cudaMemsetAsync(a.ticket, 0, ticket_bytes, s);
+    if (e != cudaSuccess) return e;
+    const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
+    ds32_streamk_seg<K><<<(unsigned)grid, DS_THREADS, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
 #ifndef TG_DS32_REFINE
 #define TG_DS32_REFINE 0
 #endif
@@ -817,6 +1094,44 @@ cudaError_t launch_ds32_capped(int kernel, const PairArgs &a, void *ws, size_t w
                                long long max_grid, cudaStream_t s) {
     if (kernel != K_ACC_JERK) return cudaErrorInvalidValue;
     return run_ds_capped<AccJerkDS<IPT2, REF>>(a, ws, ws_bytes, sms, max_grid, s);
+}
+
+// i-particles per thread of the segmented instances: 1 or 2 (2 is the
+// default of the single-set kernels); SnapCrackle always uses 1.
+int ds32_tile_i(int kernel, int ipt) {
+    if (kernel == K_SNAP_CRACKLE) return ds32_bi<SnapCrackleDS<1, REF>>();
+    return ipt == 1 ? DS_THREADS : DS_THREADS * 2;
+}
+
+int ds32_tile_j() { return DS_TILE; }
+
+size_t ds32_seg_workspace_bytes(int kernel, int ipt, const SegGeometry &g, int sms, int grid_mult) {
+    const bool one = ipt == 1;
+    switch (kernel) {
+        case K_PHI: return one ? seg_ws_bytes<PhiDS<1, REF>>(g.U, g.NIT, g.NJT, sms, grid_mult)
+                               : seg_ws_bytes<PhiDS<2, REF>>(g.U, g.NIT, g.NJT, sms, grid_mult);
+        case K_ACC: return one ? seg_ws_bytes<AccDS<1, REF>>(g.U, g.NIT, g.NJT, sms, grid_mult)
+                               : seg_ws_bytes<AccDS<2, REF>>(g.U, g.NIT, g.NJT, sms, grid_mult);
+        case K_ACC_JERK: return one ? seg_ws_bytes<AccJerkDS<1, REF>>(g.U, g.NIT, g.NJT, sms, grid_mult)
+                                    : seg_ws_bytes<AccJerkDS<2, REF>>(g.U, g.NIT, g.NJT, sms, grid_mult);
+        case K_SNAP_CRACKLE: return seg_ws_bytes<SnapCrackleDS<1, REF>>(g.U, g.NIT, g.NJT, sms, grid_mult);
+        default: return 0;
+    }
+}
+
+cudaError_t launch_ds32_seg(int kernel, int ipt, const PairArgs &a, const SegGeometry &g, void *ws,
+                            size_t ws_bytes, int sms, int grid_mult, cudaStream_t s) {
+    const bool one = ipt == 1;
+    switch (kernel) {
+        case K_PHI: return one ? run_ds_seg<PhiDS<1, REF>>(a, g, ws, ws_bytes, sms, grid_mult, s)
+                               : run_ds_seg<PhiDS<2, REF>>(a, g, ws, ws_bytes, sms, grid_mult, s);
+        case K_ACC: return one ? run_ds_seg<AccDS<1, REF>>(a, g, ws, ws_bytes, sms, grid_mult, s)
+                               : run_ds_seg<AccDS<2, REF>>(a, g, ws, ws_bytes, sms, grid_mult, s);
+        case K_ACC_JERK: return one ? run_ds_seg<AccJerkDS<1, REF>>(a, g, ws, ws_bytes, sms, grid_mult, s)
+                                    : run_ds_seg<AccJerkDS<2, REF>>(a, g, ws, ws_bytes, sms, grid_mult, s);
+        case K_SNAP_CRACKLE: return run_ds_seg<SnapCrackleDS<1, REF>>(a, g, ws, ws_bytes, sms, grid_mult, s);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace tg

@@ -317,6 +317,63 @@ static unsigned fp64_threads(size_t ni, int sms) {
     return 32;
 }
 
+// Segmented form: CTA b works on cluster c with block_off[c] <= b <
+// block_off[c+1]; its threads walk that cluster's j-range in order, so each
+// cluster's results are the single-set results bit for bit.
+__device__ __forceinline__ long long seg_find64(const long long *off, long long C, long long u) {
+    long long lo = 0, hi = C;
+    while (hi - lo > 1) {
+        const long long mid = (lo + hi) >> 1;
+        if (off[mid] <= u) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+template <class K>
+__global__ void __launch_bounds__(F64_THREADS) fp64_pairwise_seg(PairArgs a, const long long *block_off,
+                                                                 const long long *seg_start,
+                                                                 const long long *seg_n, long long C) {
+    __shared__ double sj[K::NF][F64_TILE];
+    const long long c = seg_find64(block_off, C, (long long)blockIdx.x);
+    const long long li = ((long long)blockIdx.x - block_off[c]) * blockDim.x + threadIdx.x;
+    const long long n = seg_n[c], s0 = seg_start[c];
+    const bool live = li < n;
+    typename K::St st;
+    K::init(st, a, (size_t)(s0 + (live ? li : 0)));
+    for (long long j0 = 0; j0 < n; j0 += F64_TILE) {
+        const int nt = (int)((n - j0) < F64_TILE ? (n - j0) : F64_TILE);
+        for (int q = threadIdx.x; q < K::NF * F64_TILE; q += blockDim.x) {
+            const int f = q / F64_TILE, jj = q % F64_TILE;
+            if (jj < nt) sj[f][jj] = a.J.f[f][s0 + j0 + jj];
+        }
+        __syncthreads();
+        for (int jj = 0; jj < nt; ++jj) K::pair(st, sj, jj, a);
+        __syncthreads();
+    }
+    if (live) K::store(st, a, (size_t)(s0 + li));
+}
+
+template <class K>
+static cudaError_t run_seg(const PairArgs &a, long long C, long long nblocks, int threads,
+                           const long long *block_off, const long long *seg_start, const long long *seg_n,
+                           cudaStream_t s) {
+    if (nblocks == 0) return cudaSuccess;
+    fp64_pairwise_seg<K><<<(unsigned)nblocks, threads, 0, s>>>(a, block_off, seg_start, seg_n, C);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fp64_seg(int kernel, const PairArgs &a, long long C, long long nblocks, int threads,
+                            const long long *block_off, const long long *seg_start, const long long *seg_n,
+                            cudaStream_t s) {
+    switch (kernel) {
+        case K_PHI: return run_seg<Phi64>(a, C, nblocks, threads, block_off, seg_start, seg_n, s);
+        case K_ACC: return run_seg<Acc64>(a, C, nblocks, threads, block_off, seg_start, seg_n, s);
+        case K_ACC_JERK: return run_seg<AccJerk64>(a, C, nblocks, threads, block_off, seg_start, seg_n, s);
+        case K_SNAP_CRACKLE: return run_seg<SnapCrackle64>(a, C, nblocks, threads, block_off, seg_start, seg_n, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
 template <class K>
 static cudaError_t run(const PairArgs &a, int sms, cudaStream_t s) {
     const unsigned t = fp64_threads(a.ni, sms);

@@ -55,6 +55,24 @@ cudaError_t launch_ds32(int kernel, const PairArgs &a, void *ws, size_t ws_bytes
                         cudaStream_t s);
 bool ds32_supported(int kernel);
 
+// Segmented (ensemble) geometry for one kernel's i-tile size: C clusters,
+// U units, NIT i-tiles, NJT j-tiles in total; `dev` holds the device tables
+// unit_off[C+1], itile_off[C+1], rec_tile_off[C+1], seg_start[C], seg_n[C].
+struct SegGeometry {
+    long long C, U, NIT, NJT;
+    const long long *dev;
+};
+int ds32_tile_i(int kernel, int ipt);
+int ds32_tile_j();
+size_t ds32_seg_workspace_bytes(int kernel, int ipt, const SegGeometry &g, int sms, int grid_mult);
+cudaError_t launch_ds32_seg(int kernel, int ipt, const PairArgs &a, const SegGeometry &g, void *ws,
+                            size_t ws_bytes, int sms, int grid_mult, cudaStream_t s);
+// FP64 segmented launch: block_off[C+1] (device) maps CTAs of `threads`
+// threads to clusters; seg_start/seg_n as above.
+cudaError_t launch_fp64_seg(int kernel, const PairArgs &a, long long C, long long nblocks, int threads,
+                            const long long *block_off, const long long *seg_start, const long long *seg_n,
+                            cudaStream_t s);
+
 // Record `msg` as this thread's tg_last_error() text.
 void set_last_error(const char *msg);
 

@@ -4,6 +4,7 @@ configurations, each reporting a JSON summary.
     python -m tupan_gb300.runs precision      # Plummer-Salpeter N=65536 SIA21
     python -m tupan_gb300.runs adjoint        # N=16384 leapfrog gradients
     python -m tupan_gb300.runs binaries       # 2048 + 64 binaries, PN + Sakura
+    python -m tupan_gb300.runs ensemble       # 512 clusters, Hermite-6, CUDA graph
 
 All inputs are seeded synthetic Plummer spheres (tupan_gb300.ics).
 """
@@ -213,9 +214,54 @@ def binaries_run(nbg=2048, nbin=64, t_end=1.0 / 16, dt=1.0 / 1024, clight=1e4, p
                                          "max": float(max(s / a for s, a in zip(sep, semis)))}}
 
 
+def ensemble_run(nclusters=512, steps=16, dt=1.0 / 1024, base_seed=512):
+    """512 Plummer clusters (N log-uniform in [64, 8192]), 6th-order Hermite
+    with a shared step, every force evaluation one segmented launch, one
+    step captured in a CUDA graph and replayed."""
+    from .ensemble import Ensemble, random_ensemble
+    cl = random_ensemble(nclusters, base_seed=base_seed)
+    ens = Ensemble(cl, prec="ds32")
+    e0 = ens.energy()
+    # per-kernel throughput (after the autotuning first calls)
+    ens.acc_jerk()
+    ens.snap_crackle()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record()
+    ens.acc_jerk()
+    ev[1].record()
+    ens.snap_crackle()
+    ev[2].record()
+    torch.cuda.synchronize()
+    aj_ms, sc_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    # eager steps
+    t0 = time.perf_counter()
+    for _ in range(2):
+        ens.hermite_step(dt)
+    torch.cuda.synchronize()
+    eager_ms = 1e3 * (time.perf_counter() - t0) / 2
+    ens.capture(dt)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ens.replay(steps)
+    torch.cuda.synchronize()
+    graph_ms = 1e3 * (time.perf_counter() - t0) / steps
+    e1 = ens.energy()
+    de = np.abs((e1 - e0) / e0)
+    total_steps = steps + 3
+    return {"config": {"clusters": nclusters, "n_range": [64, 8192], "total_particles": int(ens.ps.n),
+                       "sum_n2": ens.interactions, "eps2_pair": 1e-4, "method": "hermite6 shared step",
+                       "dt": dt, "steps": total_steps, "precision": "ds32"},
+            "acc_jerk": {"ms": aj_ms, "gint_s": ens.interactions / (aj_ms * 1e-3) / 1e9},
+            "snap_crackle": {"ms": sc_ms, "gint_s": ens.interactions / (sc_ms * 1e-3) / 1e9},
+            "ms_per_step_eager": eager_ms, "ms_per_step_graph": graph_ms,
+            "gint_s_per_step_graph": 3 * 2 * ens.interactions / (graph_ms * 1e-3) / 1e9,
+            "energy_error": {"median": float(np.median(de)), "max": float(de.max())}}
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("which", choices=["precision", "adjoint", "binaries"])
+    ap.add_argument("which", choices=["precision", "adjoint", "binaries", "ensemble"])
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--n", type=int, default=None)
     args = ap.parse_args()
@@ -224,7 +270,8 @@ def main():
         kw["steps"] = args.steps
     if args.n:
         kw["n"] = args.n
-    fn = {"precision": precision_run, "adjoint": adjoint_run, "binaries": binaries_run}[args.which]
+    fn = {"precision": precision_run, "adjoint": adjoint_run, "binaries": binaries_run,
+          "ensemble": ensemble_run}[args.which]
     print(json.dumps(fn(**kw), default=float))
 
 
