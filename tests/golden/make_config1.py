@@ -25,6 +25,8 @@ N, EPS, SEED, ETA, T_END = 4096, 0.01, 4096, 0.01, 0.125
 
 
 def main():
+    # The initial state is stored too: numpy's sin/cos/power differ in the last
+    # bits between CPU architectures, and 4500 chaotic steps amplify that.
     d = plummer_arrays(N, EPS, seed=SEED)
     integ = oi.integrator("ahermite4", ETA, oi.make_ps(d), oi.Kernels(nthreads=os.cpu_count() or 4))
     t0 = time.time()
@@ -33,6 +35,7 @@ def main():
         integ.evolve_step(T_END)
         steps += 1
     out = {f: integ.ps[f] for f in ("rx", "ry", "rz", "vx", "vy", "vz")}
+    out.update({"ic_" + k: v for k, v in d.items()})
     np.savez_compressed(os.path.join(HERE, "golden_config1.npz"), steps=steps, t_final=integ.t_curr,
                         n=N, eps=EPS, seed=SEED, eta=ETA, t_end=T_END, **out)
     print("steps", steps, "seconds", time.time() - t0)

@@ -61,9 +61,8 @@ def test_config1_ahermite4_plummer_4096_full_run(modules):
     reference integrator): same step count, bit-identical final state."""
     import os
     from golden_io import GOLDEN
-    from tupan_gb300.ics import plummer_arrays
     g = np.load(os.path.join(GOLDEN, "golden_config1.npz"))
-    d = plummer_arrays(int(g["n"]), float(g["eps"]), seed=int(g["seed"]))
+    d = {k[3:]: g[k] for k in g.files if k.startswith("ic_")}   # stored: see make_config1.py
     n, t, got = run_gpu(modules, d, "ahermite4", float(g["eta"]), float(g["t_end"]))
     assert n == int(g["steps"]) and t == float(g["t_final"])
     assert np.array_equal(got, np.stack([g[f] for f in RV]))
