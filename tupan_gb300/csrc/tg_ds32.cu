@@ -36,10 +36,19 @@ namespace tg {
 #define TG_DS32_THREADS 256
 #endif
 constexpr int DS_THREADS = TG_DS32_THREADS;   // threads per CTA
-constexpr int DS_TILE = 256;      // j-particles per tile
+#ifndef TG_DS32_TILE
+#define TG_DS32_TILE 512
+#endif
+#ifndef TG_DS32_STAGES
+#define TG_DS32_STAGES 3
+#endif
+#ifndef TG_DS32_FOLD
+#define TG_DS32_FOLD 64
+#endif
+constexpr int DS_TILE = TG_DS32_TILE;     // j-particles per tile
 constexpr int DS_PAIRS = DS_TILE / 2;
-constexpr int DS_STAGES = 3;
-constexpr int DS_FOLD = 64;       // j per compensated fold
+constexpr int DS_STAGES = TG_DS32_STAGES;
+constexpr int DS_FOLD = TG_DS32_FOLD;     // j per compensated fold
 constexpr int DS_FOLD_PAIRS = DS_FOLD / 2;
 
 // ---------------------------------------------------------------------------
