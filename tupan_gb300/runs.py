@@ -5,6 +5,7 @@ configurations, each reporting a JSON summary.
     python -m tupan_gb300.runs adjoint        # N=16384 leapfrog gradients
     python -m tupan_gb300.runs binaries       # 2048 + 64 binaries, PN + Sakura
     python -m tupan_gb300.runs ensemble       # 512 clusters, Hermite-6, CUDA graph
+    python -m tupan_gb300.runs kernels --n N  # per-kernel device time, ds32 and FP64
 
 All inputs are seeded synthetic Plummer spheres (tupan_gb300.ics).
 """
@@ -266,19 +267,78 @@ def ensemble_run(nclusters=512, steps=16, dt=1.0 / 1024, base_seed=512):
             "energy_error": {"median": float(np.median(de)), "max": float(de.max())}}
 
 
+KERNEL_SCALARS = {"tstep": (1.0 / 1024,), "sakura": (1.0 / 1024, 1)}
+# reference flop counts per interaction (<kernel>_kernel_common.h, last line of each core)
+KERNEL_FLOP = {"phi": 14, "acc": 20, "acc_jerk": 42, "snap_crackle": 114, "tstep": 42}
+
+
+def kernels_run(n=65536, reps=5, kernels="phi,acc,acc_jerk,snap_crackle,tstep,pnacc",
+                precisions="ds32,float64", seed=20261203):
+    """Per-kernel device time on a Plummer-Salpeter sphere (eps = 1e-3,
+    Salpeter masses in [0.1, 100]): one untimed call, then `reps` calls each
+    bracketed by CUDA events on the launching stream; median ms and Gint/s.
+    Inputs of SnapCrackle (a, j) come from one FP64 AccJerk call.  PNAcc runs
+    at order 5 with c = 1e4, Tstep with eta = 1/1024, Sakura with dt = 1/1024."""
+    d = plummer_arrays(n, 1e-3, imf=Salpeter(0.1, 100.0), seed=seed)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    T = {k: torch.tensor(v, dtype=torch.float64, device=dev) for k, v in d.items()}
+    for k in ("ax", "ay", "az", "jx", "jy", "jz"):
+        T[k] = torch.empty(n, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream().cuda_stream
+    ptr = lambda names: [T[k].data_ptr() for k in names]  # noqa: E731
+    _native.call_device("acc_jerk", n, ptr(_native.P8), n, ptr(_native.P8), (),
+                        ptr(("ax", "ay", "az", "jx", "jy", "jz")), _native.PREC_FP64, stream)
+    clight = extensions.Clight()
+    clight.pn_order, clight.clight = 5, 1e4
+    scal = dict(KERNEL_SCALARS)
+    scal["pnacc"] = (clight.pn_order,) + tuple(getattr(clight, "inv%d" % k) for k in range(1, 8))
+    out = {"config": {"n": n, "interactions": n * n, "reps": reps, "imf": "salpeter [0.1,100]",
+                      "eps2_pair": 1e-6, "seed": seed}, "kernels": {}}
+    for name in kernels.split(","):
+        fields, _, outs = _native.SPECS[name]
+        o = [torch.empty(n, dtype=torch.float64, device=dev) for _ in outs]
+        for p in precisions.split(","):
+            prec = autodiff.PREC[p]
+
+            def call():
+                _native.call_device(name, n, ptr(fields), n, ptr(fields), scal.get(name, ()),
+                                    [x.data_ptr() for x in o], prec, stream)
+            call()
+            ms = []
+            for _ in range(reps):
+                ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+                ev[0].record()
+                call()
+                ev[1].record()
+                ev[1].synchronize()
+                ms.append(ev[0].elapsed_time(ev[1]))
+            med = float(np.median(ms))
+            rec = {"ms": med, "gint_s": n * n / (med * 1e-3) / 1e9}
+            if name in KERNEL_FLOP:
+                rec["tflops_ref_counted"] = rec["gint_s"] * KERNEL_FLOP[name] / 1e3
+            out["kernels"]["%s_%s" % (name, p)] = rec
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("which", choices=["precision", "adjoint", "binaries", "ensemble"])
+    ap.add_argument("which", choices=["precision", "adjoint", "binaries", "ensemble", "kernels"])
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--n", type=int, default=None)
+    ap.add_argument("--reps", type=int, default=None, help="kernels: timed calls per kernel")
+    ap.add_argument("--kernels", default=None, help="kernels: comma-separated kernel names")
+    ap.add_argument("--precisions", default=None, help="kernels: comma-separated, ds32/float64")
     args = ap.parse_args()
     kw = {}
     if args.steps:
         kw["steps"] = args.steps
     if args.n:
         kw["n"] = args.n
+    for k in ("reps", "kernels", "precisions"):
+        if getattr(args, k) is not None:
+            kw[k] = getattr(args, k)
     fn = {"precision": precision_run, "adjoint": adjoint_run, "binaries": binaries_run,
-          "ensemble": ensemble_run}[args.which]
+          "ensemble": ensemble_run, "kernels": kernels_run}[args.which]
     print(json.dumps(fn(**kw), default=float))
 
 
