@@ -145,6 +145,43 @@ int tg_sakura(size_t ni, const double *im, const double *irx, const double *iry,
               double *idrx, double *idry, double *idrz,
               double *idvx, double *idvy, double *idvz, int prec, void *stream);
 
+/* replaces nreg_Xkernel, tupan/lib/src/libtupan.h:152-178.  The pair
+ * separation r_ij + v_ij dt feeds imr = sum m_j r_ij, the softened
+ * acceleration and iu = m_i sum m_j / r_ij.  Always FP64 (the outputs are
+ * positions, not small increments); prec is checked and otherwise ignored. */
+int tg_nreg_x(size_t ni, const double *im, const double *irx, const double *iry,
+              const double *irz, const double *ie2,
+              const double *ivx, const double *ivy, const double *ivz,
+              size_t nj, const double *jm, const double *jrx, const double *jry,
+              const double *jrz, const double *je2,
+              const double *jvx, const double *jvy, const double *jvz,
+              double dt, double *imrx, double *imry, double *imrz,
+              double *iax, double *iay, double *iaz, double *iu, int prec, void *stream);
+
+/* replaces nreg_Vkernel, tupan/lib/src/libtupan.h:180-201.  The pair
+ * velocity v_ij + a_ij dt feeds imv = sum m_j v_ij and
+ * ik = m_i sum m_j |v_ij|^2.  Always FP64, like tg_nreg_x. */
+int tg_nreg_v(size_t ni, const double *im, const double *ivx, const double *ivy,
+              const double *ivz, const double *iax, const double *iay, const double *iaz,
+              size_t nj, const double *jm, const double *jvx, const double *jvy,
+              const double *jvz, const double *jax, const double *jay, const double *jaz,
+              double dt, double *imvx, double *imvy, double *imvz, double *ik,
+              int prec, void *stream);
+
+/* replaces kepler_solver_kernel, tupan/lib/src/libtupan.h:231-246, for
+ * npairs pairs at once (the reference call is npairs = 1): pair p is
+ * particles 2p and 2p+1; after dt their centre of mass has drifted freely
+ * and their relative orbit follows the universal-variable Kepler solver.
+ * FP64.  The outputs may alias the inputs (in-place update, as the
+ * reference's callers do).  The solver's retry loops are bounded (at most
+ * 1024 sub-steps per retry loop and 65536 Kepler solves per pair); a pair
+ * that reaches a bound keeps its last iterate and raises
+ * TG_ST_KEPLER_CAP. */
+int tg_kepler_solver(size_t npairs, const double *m, const double *rx, const double *ry,
+                     const double *rz, const double *e2, const double *vx, const double *vy,
+                     const double *vz, double dt, double *r1x, double *r1y, double *r1z,
+                     double *v1x, double *v1y, double *v1z, void *stream);
+
 /* ---------------------------------------------------------------------- */
 /* Ensembles: many independent clusters in one launch.  No counterpart in  */
 /* the reference (which calls its kernels once per particle set).          */
@@ -191,6 +228,20 @@ int tg_acc_vjp(size_t n, const double *m, const double *rx, const double *ry, co
 /* Fused forms of the reference integrators' numpy updates, evaluated in   */
 /* numpy's operation order so FP64 trajectories match bit for bit.         */
 /* ---------------------------------------------------------------------- */
+
+/* *out = sum of x[0..n) in numpy's float64 order (pairwise blocks of at
+ * most 128 elements with eight interleaved accumulators, halves split at
+ * multiples of 8), so reductions that steer the integrators (total mass,
+ * energies, the NREG integrator's U, W and K) equal numpy.sum bit for bit.
+ * n == 0 stores 0.  No counterpart in the reference's C library (numpy's
+ * reduction in its Python layer). */
+int tg_sum(size_t n, const double *x, double *out, void *stream);
+
+/* x = mx / d, y = my / d, z = mz / d with IEEE division (the NREG
+ * integrator's r = mr / M and v = mv / M, tupan/integrator/nreg.py:27-29,
+ * 50-52); the outputs may alias the inputs. */
+int tg_div3(size_t n, double *x, double *y, double *z, const double *mx, const double *my,
+            const double *mz, double d, void *stream);
 
 /* r += v * tau (drift_n, tupan/integrator/sia.py:64-73) */
 int tg_drift(size_t n, double *rx, double *ry, double *rz, const double *vx, const double *vy,
@@ -302,6 +353,31 @@ void sakura_kernel(const unsigned long ni, const double *_im, const double *_irx
                    const double dt, const long flag,
                    double *_idrx, double *_idry, double *_idrz,
                    double *_idvx, double *_idvy, double *_idvz);
+/* tupan/lib/src/libtupan.h:152-178 */
+void nreg_Xkernel(const unsigned long ni, const double *_im, const double *_irx,
+                  const double *_iry, const double *_irz, const double *_ie2,
+                  const double *_ivx, const double *_ivy, const double *_ivz,
+                  const unsigned long nj, const double *_jm, const double *_jrx,
+                  const double *_jry, const double *_jrz, const double *_je2,
+                  const double *_jvx, const double *_jvy, const double *_jvz,
+                  const double dt, double *_idrx, double *_idry, double *_idrz,
+                  double *_iax, double *_iay, double *_iaz, double *_iu);
+/* tupan/lib/src/libtupan.h:180-201 */
+void nreg_Vkernel(const unsigned long ni, const double *_im, const double *_ivx,
+                  const double *_ivy, const double *_ivz, const double *_iax,
+                  const double *_iay, const double *_iaz,
+                  const unsigned long nj, const double *_jm, const double *_jvx,
+                  const double *_jvy, const double *_jvz, const double *_jax,
+                  const double *_jay, const double *_jaz,
+                  const double dt, double *_idvx, double *_idvy, double *_idvz, double *_ik);
+
+/* tupan/lib/src/libtupan.h:231-246: two particles; the outputs may alias
+ * the inputs */
+void kepler_solver_kernel(const double *_im, const double *_irx, const double *_iry,
+                          const double *_irz, const double *_ie2, const double *_ivx,
+                          const double *_ivy, const double *_ivz, const double dt,
+                          double *_ir1x, double *_ir1y, double *_ir1z,
+                          double *_iv1x, double *_iv1y, double *_iv1z);
 
 #ifdef __cplusplus
 }

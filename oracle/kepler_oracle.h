@@ -14,10 +14,11 @@
  * that results are bit-identical to the reference on the same machine.
  *
  * Deviation: the reference retries without bound (halving at :483-500,
- * doubling at :580-606).  Here the halving stops after ORC_SPLIT_CAP
- * doublings, the energy loop after ORC_ENERGY_CAP, and a pair evolution
- * after ORC_SOLVE_BUDGET Kepler solves, keeping the last iterate (the same
- * bounds as the GPU kernel).  Within the bounds the steps are the reference's;
+ * doubling at :580-606).  Here the halving stops after orc_split_cap
+ * doublings, the energy loop after orc_energy_cap, and a pair evolution
+ * after orc_solve_budget Kepler solves, keeping the last iterate (the same
+ * bounds as the GPU kernels: ORC_* for Sakura, ORC_PAIR_* for the Kepler
+ * pair solver).  Within the bounds the steps are the reference's;
  * the bounds are reached only for inputs (radial free fall with v = 0, or
  * softened close pairs whose energy test never passes) on which the
  * reference itself never returns.
@@ -29,9 +30,20 @@
 
 #define ORC_TOL 2.2737367544323205948e-13 /* 2^-42 */
 #define ORC_MAXITER 64
+/* Bounds for Sakura's pairwise kernel (many pairs per call)... */
 #define ORC_SPLIT_CAP 6      /* up to 64 sub-steps after solver failures */
 #define ORC_ENERGY_CAP 4     /* up to 16 sub-steps for the energy test */
 #define ORC_SOLVE_BUDGET 1024
+/* ...and for the Kepler pair solver (a few pairs per call). */
+#ifndef ORC_PAIR_SPLIT_CAP
+#define ORC_PAIR_SPLIT_CAP 10
+#endif
+#ifndef ORC_PAIR_ENERGY_CAP
+#define ORC_PAIR_ENERGY_CAP 10
+#endif
+#ifndef ORC_PAIR_SOLVE_BUDGET
+#define ORC_PAIR_SOLVE_BUDGET 65536
+#endif
 #define ORC_PI 3.141592653589793
 
 static inline int orc_sign(double x) { return (x > 0) - (x < 0); }
@@ -110,8 +122,21 @@ static int orc_laguerre(double s0, double *s, const struct orc_kep *k)
     return 0;
 }
 
-/* Kepler solves spent on the current pair evolution (per thread). */
+/* Kepler solves spent on the current pair evolution, and the bounds in
+ * force (per thread; set by the caller before each pair). */
 static __thread int orc_solves;
+static __thread int orc_split_cap = ORC_SPLIT_CAP;
+static __thread int orc_energy_cap = ORC_ENERGY_CAP;
+static __thread int orc_solve_budget = ORC_SOLVE_BUDGET;
+/* Set when a bound was reached during the current pair evolution. */
+static __thread int orc_capped;
+
+static inline void orc_set_caps(int split_cap, int energy_cap, int solve_budget)
+{
+    orc_split_cap = split_cap;
+    orc_energy_cap = energy_cap;
+    orc_solve_budget = solve_budget;
+}
 
 /* One Kepler solve over dt0; r,v updated in place only on success. */
 static int orc_kepler_once(double dt0, double m, double e2, double r[3], double v[3])
@@ -168,10 +193,11 @@ static void orc_kepler_split(double dt, double m, double e2,
         for (int q = 0; q < 3; ++q) { r[q] = r0[q]; v[q] = v0[q]; }
         int failed = 0;
         for (long i = 0; i < n; ++i) {
-            if (orc_solves >= ORC_SOLVE_BUDGET) return;
+            if (orc_solves >= orc_solve_budget) { orc_capped = 1; return; }
             if (orc_kepler_once(dt / n, m, e2, r, v) != 0) { failed = 1; break; }
         }
-        if (!failed || tries >= ORC_SPLIT_CAP) return;
+        if (!failed) return;
+        if (tries >= orc_split_cap) { orc_capped = 1; return; }
         n *= 2;
     }
 }
@@ -206,7 +232,7 @@ static void orc_kepler(double dt, double m, double e2,
     if (2 * err < tol * (u1 + u0)) return;
 
     long n = 1;
-    for (int tries = 0; tries < ORC_ENERGY_CAP; ++tries) {
+    for (int tries = 0; tries < orc_energy_cap; ++tries) {
         n *= 2;
         for (int q = 0; q < 3; ++q) { r[q] = r0[q]; v[q] = v0[q]; }
         int bad = 0;
@@ -216,10 +242,11 @@ static void orc_kepler(double dt, double m, double e2,
             orc_energy(m, e2, r, v, &u1, &en1);
             err = fabs(en1 - en0);
             if (2 * err > tol * (u1 + u0)) { bad = 1; break; }
-            if (orc_solves >= ORC_SOLVE_BUDGET) return;
+            if (orc_capped) return;
         }
         if (!bad) return;
     }
+    orc_capped = 1;
 }
 
 /* Softened Newtonian acceleration of the relative orbit. */

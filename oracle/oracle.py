@@ -40,7 +40,12 @@ SPECS = {
     "tstep": (P8, ("real",), ("tstep", "tstepij")),
     "pnacc": (P8, ("uint",) + ("real",) * 7, ("pnax", "pnay", "pnaz")),
     "sakura": (P8, ("real", "int"), ("drx", "dry", "drz", "dvx", "dvy", "dvz")),
+    "nreg_x": (P8, ("real",), ("mrx", "mry", "mrz", "ax", "ay", "az", "u")),
+    "nreg_v": (("mass", "vx", "vy", "vz", "ax", "ay", "az"), ("real",), ("mvx", "mvy", "mvz", "mk")),
 }
+# kernels whose reference symbol is not <name>_kernel (libtupan.h:152-201)
+REF_SYMBOLS = {"nreg_x": "nreg_Xkernel", "nreg_v": "nreg_Vkernel"}
+KEPLER_OUT = ("rx", "ry", "rz", "vx", "vy", "vz")
 
 _DP = ctypes.POINTER(ctypes.c_double)
 
@@ -92,10 +97,24 @@ class _CLib:
         args += [r.ctypes.data_as(_DP) for r in res]
         if self.threaded:
             args.append(ctypes.c_int(int(nthreads)))
-        fn = getattr(self.lib, self.prefix + name + self.suffix)
+        fn = getattr(self.lib, self.symbol(name))
         fn.restype = None
         fn(*args)
         return res
+
+    def symbol(self, name):
+        return self.prefix + name + self.suffix
+
+    def _kepler_args(self, ps, dt, npairs):
+        keep, res = [], tuple(np.zeros(2 * npairs) for _ in KEPLER_OUT)
+        for f in P8:
+            a = _as_f64(ps[f])
+            if a.shape != (2 * npairs,):
+                raise ValueError("kepler: %s must hold 2 x npairs values" % f)
+            keep.append(a)
+        args = [a.ctypes.data_as(_DP) for a in keep] + [ctypes.c_double(float(dt))]
+        args += [r.ctypes.data_as(_DP) for r in res]
+        return keep, res, args
 
 
 class Oracle(_CLib):
@@ -103,6 +122,22 @@ class Oracle(_CLib):
     prefix = "orc_"
     suffix = ""
     threaded = True
+
+    def kepler(self, ps, dt, nthreads=1, capped=None):
+        """Kepler pair solver over consecutive pairs (2p, 2p+1) of `ps`;
+        returns (rx, ry, rz, vx, vy, vz) after dt
+        (kepler_solver_kernel_common.h:8-81).  If `capped` is a list, it
+        receives one flag per pair: True where a retry bound was reached."""
+        npairs = len(ps["mass"]) // 2
+        keep, res, args = self._kepler_args(ps, dt, npairs)
+        flags = np.zeros(npairs, dtype=np.intc)
+        fn = self.lib.orc_kepler_solver
+        fn.restype = None
+        fn(ctypes.c_size_t(npairs), *args, flags.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+           ctypes.c_int(int(nthreads)))
+        if capped is not None:
+            capped[:] = [bool(x) for x in flags]
+        return res
 
     def __init__(self, path=None):
         if path is None:
@@ -128,6 +163,23 @@ class ReferenceLib(_CLib):
     def _scalar(self, kind, value):
         # FP64 build of the reference: UINT = unsigned long, INT = long
         return super()._scalar(kind, value)
+
+    def symbol(self, name):
+        return REF_SYMBOLS.get(name, name + self.suffix)
+
+    def kepler(self, ps, dt, nthreads=1):
+        """The reference kepler_solver_kernel, one call per pair."""
+        npairs = len(ps["mass"]) // 2
+        res = tuple(np.zeros(2 * npairs) for _ in KEPLER_OUT)
+        fn = self.lib.kepler_solver_kernel
+        fn.restype = None
+        for p in range(npairs):
+            sub = {f: _as_f64(ps[f])[2 * p:2 * p + 2].copy() for f in P8}
+            _, out, args = self._kepler_args(sub, dt, 1)
+            fn(*args)
+            for r, o in zip(res, out):
+                r[2 * p:2 * p + 2] = o
+        return res
 
 
 def reference_available():

@@ -90,7 +90,7 @@ struct pset {
 struct call {
     struct pset I, J;
     size_t nj;
-    real *o[6];
+    real *o[8];
     real eta, dt;
     long flag;
     unsigned long order;
@@ -344,6 +344,7 @@ static void sakura_range(void *p, size_t i0, size_t i1)
 {
     struct call *c = (struct call *)p;
     const struct pset *I = &c->I, *J = &c->J;
+    orc_set_caps(ORC_SPLIT_CAP, ORC_ENERGY_CAP, ORC_SOLVE_BUDGET);
     for (size_t i = i0; i < i1; ++i) {
         real d[6] = {0, 0, 0, 0, 0, 0};
         for (size_t j = 0; j < c->nj; ++j) {
@@ -360,6 +361,126 @@ static void sakura_range(void *p, size_t i0, size_t i1)
             }
         }
         for (int k = 0; k < 6; ++k) c->o[k][i] = d[k];
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* NREG_X: nreg_kernels_common.h:7-60, nreg_kernels.c:5-67.                  */
+/* The pair separation is drifted by dt with the relative velocity before    */
+/* use; outputs are sum m_j r_ij (mr), the softened acceleration and         */
+/* u_i = m_i sum m_j / r_ij.                                                 */
+/* ------------------------------------------------------------------------ */
+static void nreg_x_range(void *p, size_t i0, size_t i1)
+{
+    struct call *c = (struct call *)p;
+    const struct pset *I = &c->I, *J = &c->J;
+    const real dt = c->dt;
+    for (size_t i = i0; i < i1; ++i) {
+        real mrx = 0, mry = 0, mrz = 0, ax = 0, ay = 0, az = 0, u = 0;
+        for (size_t j = 0; j < c->nj; ++j) {
+            real rx = I->rx[i] - J->rx[j];
+            real ry = I->ry[i] - J->ry[j];
+            real rz = I->rz[i] - J->rz[j];
+            real e2 = I->e2[i] + J->e2[j];
+            real vx = I->vx[i] - J->vx[j];
+            real vy = I->vy[i] - J->vy[j];
+            real vz = I->vz[i] - J->vz[j];
+            rx += vx * dt;
+            ry += vy * dt;
+            rz += vz * dt;
+            real r2 = rx * rx + ry * ry + rz * rz;
+            real q2 = soft_inv_r2(r2, e2);
+            real q1 = sqrt(q2);
+            real q3 = q2 * q1;
+            q3 *= J->m[j];
+            mrx += J->m[j] * rx;
+            mry += J->m[j] * ry;
+            mrz += J->m[j] * rz;
+            ax -= q3 * rx;
+            ay -= q3 * ry;
+            az -= q3 * rz;
+            u += J->m[j] * q1;
+        }
+        c->o[0][i] = mrx; c->o[1][i] = mry; c->o[2][i] = mrz;
+        c->o[3][i] = ax; c->o[4][i] = ay; c->o[5][i] = az;
+        c->o[6][i] = I->m[i] * u;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* NREG_V: nreg_kernels_common.h:62-102, nreg_kernels.c:70-116.              */
+/* The relative velocity is kicked by dt with the relative acceleration;     */
+/* outputs are sum m_j v_ij (mv) and k_i = m_i sum m_j |v_ij|^2.             */
+/* ------------------------------------------------------------------------ */
+static void nreg_v_range(void *p, size_t i0, size_t i1)
+{
+    struct call *c = (struct call *)p;
+    const struct pset *I = &c->I, *J = &c->J;
+    const real dt = c->dt;
+    for (size_t i = i0; i < i1; ++i) {
+        real mvx = 0, mvy = 0, mvz = 0, k = 0;
+        for (size_t j = 0; j < c->nj; ++j) {
+            real vx = I->vx[i] - J->vx[j];
+            real vy = I->vy[i] - J->vy[j];
+            real vz = I->vz[i] - J->vz[j];
+            real ax = I->ax[i] - J->ax[j];
+            real ay = I->ay[i] - J->ay[j];
+            real az = I->az[i] - J->az[j];
+            vx += ax * dt;
+            vy += ay * dt;
+            vz += az * dt;
+            real v2 = vx * vx + vy * vy + vz * vz;
+            mvx += J->m[j] * vx;
+            mvy += J->m[j] * vy;
+            mvz += J->m[j] * vz;
+            k += J->m[j] * v2;
+        }
+        c->o[0][i] = mvx; c->o[1][i] = mvy; c->o[2][i] = mvz;
+        c->o[3][i] = I->m[i] * k;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Kepler pair solver: kepler_solver_kernel_common.h:8-81 and                */
+/* kepler_solver_kernel.c.  Pair p is elements 2p (i) and 2p+1 (j); the      */
+/* centre of mass drifts freely and the relative orbit follows the bounded   */
+/* universal-variable solver.  Outputs may alias the inputs.                 */
+/* ------------------------------------------------------------------------ */
+struct kcall {
+    const real *m, *rx, *ry, *rz, *e2, *vx, *vy, *vz;
+    real dt;
+    real *o[6];
+    int *capped;    /* per pair: 1 when a retry bound was reached (may be NULL) */
+};
+
+static void kepler_range(void *p, size_t k0, size_t k1)
+{
+    struct kcall *c = (struct kcall *)p;
+    for (size_t k = k0; k < k1; ++k) {
+        const size_t a = 2 * k, b = 2 * k + 1;
+        real im = c->m[a], jm = c->m[b];
+        real ir[3] = {c->rx[a], c->ry[a], c->rz[a]}, jr[3] = {c->rx[b], c->ry[b], c->rz[b]};
+        real iv[3] = {c->vx[a], c->vy[a], c->vz[a]}, jv[3] = {c->vx[b], c->vy[b], c->vz[b]};
+        real r0[3], v0[3], rcm[3], vcm[3], r1[3], v1[3];
+        for (int q = 0; q < 3; ++q) { r0[q] = ir[q] - jr[q]; }
+        real e2 = c->e2[a] + c->e2[b];
+        for (int q = 0; q < 3; ++q) { v0[q] = iv[q] - jv[q]; }
+        real m = im + jm;
+        real imu = im / m, jmu = jm / m;
+        for (int q = 0; q < 3; ++q) rcm[q] = imu * ir[q] + jmu * jr[q];
+        for (int q = 0; q < 3; ++q) vcm[q] = imu * iv[q] + jmu * jv[q];
+        for (int q = 0; q < 3; ++q) rcm[q] += vcm[q] * c->dt;
+        orc_set_caps(ORC_PAIR_SPLIT_CAP, ORC_PAIR_ENERGY_CAP, ORC_PAIR_SOLVE_BUDGET);
+        orc_solves = 0;
+        orc_capped = 0;
+        orc_kepler(c->dt, m, e2, r0, v0, r1, v1);
+        if (c->capped) c->capped[k] = orc_capped;
+        for (int q = 0; q < 3; ++q) {
+            c->o[q][a] = rcm[q] + jmu * r1[q];
+            c->o[3 + q][a] = vcm[q] + jmu * v1[q];
+            c->o[q][b] = rcm[q] - imu * r1[q];
+            c->o[3 + q][b] = vcm[q] - imu * v1[q];
+        }
     }
 }
 
@@ -466,4 +587,47 @@ void orc_sakura(size_t ni, const real *im, const real *irx, const real *iry, con
     c.nj = nj; c.dt = dt; c.flag = flag;
     c.o[0] = idrx; c.o[1] = idry; c.o[2] = idrz; c.o[3] = idvx; c.o[4] = idvy; c.o[5] = idvz;
     run_sliced(sakura_range, &c, ni, nthreads);
+}
+
+void orc_nreg_x(size_t ni, const real *im, const real *irx, const real *iry, const real *irz, const real *ie2,
+                const real *ivx, const real *ivy, const real *ivz,
+                size_t nj, const real *jm, const real *jrx, const real *jry, const real *jrz, const real *je2,
+                const real *jvx, const real *jvy, const real *jvz,
+                real dt, real *imrx, real *imry, real *imrz, real *iax, real *iay, real *iaz, real *iu,
+                int nthreads)
+{
+    struct call c; memset(&c, 0, sizeof c);
+    SET5(c.I, im, irx, iry, irz, ie2); SETV(c.I, ivx, ivy, ivz);
+    SET5(c.J, jm, jrx, jry, jrz, je2); SETV(c.J, jvx, jvy, jvz);
+    c.nj = nj; c.dt = dt;
+    c.o[0] = imrx; c.o[1] = imry; c.o[2] = imrz; c.o[3] = iax; c.o[4] = iay; c.o[5] = iaz; c.o[6] = iu;
+    run_sliced(nreg_x_range, &c, ni, nthreads);
+}
+
+void orc_nreg_v(size_t ni, const real *im, const real *ivx, const real *ivy, const real *ivz,
+                const real *iax, const real *iay, const real *iaz,
+                size_t nj, const real *jm, const real *jvx, const real *jvy, const real *jvz,
+                const real *jax, const real *jay, const real *jaz,
+                real dt, real *imvx, real *imvy, real *imvz, real *ik, int nthreads)
+{
+    struct call c; memset(&c, 0, sizeof c);
+    c.I.m = im; SETV(c.I, ivx, ivy, ivz); c.I.ax = iax; c.I.ay = iay; c.I.az = iaz;
+    c.J.m = jm; SETV(c.J, jvx, jvy, jvz); c.J.ax = jax; c.J.ay = jay; c.J.az = jaz;
+    c.nj = nj; c.dt = dt;
+    c.o[0] = imvx; c.o[1] = imvy; c.o[2] = imvz; c.o[3] = ik;
+    run_sliced(nreg_v_range, &c, ni, nthreads);
+}
+
+/* npairs independent pairs (2 npairs particles); libtupan.h kepler_solver_kernel
+ * is the npairs = 1 case. */
+void orc_kepler_solver(size_t npairs, const real *m, const real *rx, const real *ry, const real *rz,
+                       const real *e2, const real *vx, const real *vy, const real *vz, real dt,
+                       real *r1x, real *r1y, real *r1z, real *v1x, real *v1y, real *v1z, int *capped,
+                       int nthreads)
+{
+    struct kcall c;
+    c.capped = capped;
+    c.m = m; c.rx = rx; c.ry = ry; c.rz = rz; c.e2 = e2; c.vx = vx; c.vy = vy; c.vz = vz; c.dt = dt;
+    c.o[0] = r1x; c.o[1] = r1y; c.o[2] = r1z; c.o[3] = v1x; c.o[4] = v1y; c.o[5] = v1z;
+    run_sliced(kepler_range, &c, npairs, nthreads);
 }

@@ -35,7 +35,14 @@ SPECS = {
     "tstep": (P8, (ctypes.c_double,), ("tstep", "tstepij")),
     "pnacc": (P8, (ctypes.c_ulong,) + (ctypes.c_double,) * 7, ("pnax", "pnay", "pnaz")),
     "sakura": (P8, (ctypes.c_double, ctypes.c_long), ("drx", "dry", "drz", "dvx", "dvy", "dvz")),
+    "nreg_x": (P8, (ctypes.c_double,), ("mrx", "mry", "mrz", "ax", "ay", "az", "u")),
+    "nreg_v": (("mass", "vx", "vy", "vz", "ax", "ay", "az"), (ctypes.c_double,), ("mvx", "mvy", "mvz", "mk")),
 }
+# drop-in host symbols that are not <name>_kernel (libtupan.h:152-201)
+HOST_SYMBOLS = {"nreg_x": "nreg_Xkernel", "nreg_v": "nreg_Vkernel"}
+# the Kepler pair solver's fields, in argument order (libtupan.h:231-246)
+KEPLER_FIELDS = P8
+KEPLER_OUT = ("rx", "ry", "rz", "vx", "vy", "vz")
 
 _DP = ctypes.c_void_p
 
@@ -52,7 +59,7 @@ def _load():
     lib = ctypes.CDLL(LIB_PATH)
     for name, (fields, scal, outs) in SPECS.items():
         for prefix in ("tg_", ""):
-            fn = getattr(lib, prefix + name + ("" if prefix else "_kernel"))
+            fn = getattr(lib, "tg_" + name if prefix else HOST_SYMBOLS.get(name, name + "_kernel"))
             args = [ctypes.c_size_t if prefix else ctypes.c_ulong] + [_DP] * len(fields)
             args += [ctypes.c_size_t if prefix else ctypes.c_ulong] + [_DP] * len(fields)
             args += list(scal) + [_DP] * len(outs)
@@ -84,6 +91,14 @@ def _load():
     lib.tg_acc_vjp.argtypes = [ctypes.c_size_t] + [_DP] * 12 + [ctypes.c_int, _DP]
     lib.tg_probe_fma_tflops.restype = ctypes.c_double
     lib.tg_probe_fma_tflops.argtypes = [ctypes.c_int, ctypes.c_int, _DP]
+    lib.tg_div3.restype = ctypes.c_int
+    lib.tg_div3.argtypes = [ctypes.c_size_t] + [_DP] * 6 + [ctypes.c_double, _DP]
+    lib.tg_sum.restype = ctypes.c_int
+    lib.tg_sum.argtypes = [ctypes.c_size_t, _DP, _DP, _DP]
+    lib.tg_kepler_solver.restype = ctypes.c_int
+    lib.tg_kepler_solver.argtypes = [ctypes.c_size_t] + [_DP] * 8 + [ctypes.c_double] + [_DP] * 6 + [_DP]
+    lib.kepler_solver_kernel.restype = None
+    lib.kepler_solver_kernel.argtypes = [_DP] * 8 + [ctypes.c_double] + [_DP] * 6
     return lib
 
 
@@ -112,6 +127,19 @@ def sync_status(stream=None):
     if rc < 0:
         raise TupanGB300Error("tg_sync_status failed: %s" % last_error())
     return rc
+
+
+def psum(t):
+    """float(sum of a float64 CUDA tensor) in numpy's pairwise order (tg_sum),
+    so the value equals numpy.sum of the same array bit for bit."""
+    import torch
+    t = t.contiguous()
+    if not (t.is_cuda and t.dtype == torch.float64):
+        raise TypeError("psum expects a float64 CUDA tensor")
+    out = torch.empty(1, dtype=torch.float64, device=t.device)
+    check(lib.tg_sum(t.numel(), t.data_ptr(), out.data_ptr(), torch.cuda.current_stream().cuda_stream),
+          "tg_sum")
+    return float(out.item())
 
 
 def ptr_array(tensors):

@@ -145,11 +145,12 @@ struct HostStage {
 HostStage g_stage[MAX_DEV];
 
 struct HostCall {
-    int kernel;
+    int nf;                 // input arrays per set, in the launch lambda's order
+    int no;                 // output arrays
     size_t ni, nj;
     const double *in_i[14];
     const double *in_j[14];
-    double *out[6];
+    double *out[tg::MAX_OUTPUTS];
 };
 
 // Copies the host arrays in, runs `launch` on device copies, copies out.
@@ -164,7 +165,7 @@ void host_call(const HostCall &h, F launch) {
     }
     HostStage &st = g_stage[dev];
     std::lock_guard<std::mutex> lk(st.mu);
-    const int nf = tg::kernel_fields(h.kernel), no = tg::kernel_outputs(h.kernel);
+    const int nf = h.nf, no = h.no;
     const size_t need = (size_t)nf * (h.ni + h.nj) + (size_t)no * h.ni + 8;
     cudaError_t e = cudaSuccess;
     if (!st.stream) e = cudaStreamCreateWithFlags(&st.stream, cudaStreamNonBlocking);
@@ -182,7 +183,7 @@ void host_call(const HostCall &h, F launch) {
     }
     double *p = st.buf;
     const double *di[14] = {}, *dj[14] = {};
-    double *dout[6] = {};
+    double *dout[tg::MAX_OUTPUTS] = {};
     for (int f = 0; f < nf && e == cudaSuccess; ++f) {
         if (h.ni) e = cudaMemcpyAsync(p, h.in_i[f], h.ni * sizeof(double), cudaMemcpyHostToDevice, st.stream);
         di[f] = p; p += h.ni;
@@ -356,13 +357,70 @@ int tg_acc_vjp(size_t n, const double *m, const double *rx, const double *ry, co
     return run(tg::K_ACC_VJP, a, prec, stream);
 }
 
+int tg_nreg_x(size_t ni, const double *im, const double *irx, const double *iry, const double *irz,
+              const double *ie2, const double *ivx, const double *ivy, const double *ivz, size_t nj,
+              const double *jm, const double *jrx, const double *jry, const double *jrz,
+              const double *je2, const double *jvx, const double *jvy, const double *jvz, double dt,
+              double *imrx, double *imry, double *imrz, double *iax, double *iay, double *iaz,
+              double *iu, int prec, void *stream) {
+    tg::PairArgs a = blank();
+    set5(a.I, im, irx, iry, irz, ie2); setv(a.I, ivx, ivy, ivz);
+    set5(a.J, jm, jrx, jry, jrz, je2); setv(a.J, jvx, jvy, jvz);
+    a.ni = ni; a.nj = nj; a.dt = dt;
+    a.out[0] = imrx; a.out[1] = imry; a.out[2] = imrz;
+    a.out[3] = iax; a.out[4] = iay; a.out[5] = iaz; a.out[6] = iu;
+    if (prec != TG_PREC_FP64 && prec != TG_PREC_DS32) return fail(TG_EINVAL, "unknown precision");
+    return run(tg::K_NREG_X, a, TG_PREC_FP64, stream);
+}
+
+int tg_nreg_v(size_t ni, const double *im, const double *ivx, const double *ivy, const double *ivz,
+              const double *iax, const double *iay, const double *iaz, size_t nj, const double *jm,
+              const double *jvx, const double *jvy, const double *jvz, const double *jax,
+              const double *jay, const double *jaz, double dt, double *imvx, double *imvy,
+              double *imvz, double *ik, int prec, void *stream) {
+    tg::PairArgs a = blank();
+    // slots F_RX..F_E2 carry the mass pointer (staged, never read)
+    set5(a.I, im, im, im, im, im); setv(a.I, ivx, ivy, ivz);
+    a.I.f[tg::F_AX] = iax; a.I.f[tg::F_AY] = iay; a.I.f[tg::F_AZ] = iaz;
+    set5(a.J, jm, jm, jm, jm, jm); setv(a.J, jvx, jvy, jvz);
+    a.J.f[tg::F_AX] = jax; a.J.f[tg::F_AY] = jay; a.J.f[tg::F_AZ] = jaz;
+    a.ni = ni; a.nj = nj; a.dt = dt;
+    a.out[0] = imvx; a.out[1] = imvy; a.out[2] = imvz; a.out[3] = ik;
+    if (prec != TG_PREC_FP64 && prec != TG_PREC_DS32) return fail(TG_EINVAL, "unknown precision");
+    return run(tg::K_NREG_V, a, TG_PREC_FP64, stream);
+}
+
+int tg_kepler_solver(size_t npairs, const double *m, const double *rx, const double *ry,
+                     const double *rz, const double *e2, const double *vx, const double *vy,
+                     const double *vz, double dt, double *r1x, double *r1y, double *r1z, double *v1x,
+                     double *v1y, double *v1z, void *stream) {
+    g_err.clear();
+    if (npairs > MAX_N / 2) return fail(TG_EINVAL, "npairs above 2^30");
+    if (npairs == 0) return TG_OK;
+    const double *in[8] = {m, rx, ry, rz, e2, vx, vy, vz};
+    double *out[6] = {r1x, r1y, r1z, v1x, v1y, v1z};
+    for (const double *p : in)
+        if (!p) return fail(TG_EINVAL, "null input pointer");
+    for (double *p : out)
+        if (!p) return fail(TG_EINVAL, "null output pointer");
+    DevCtx *c = nullptr;
+    int rc = current_ctx(&c);
+    if (rc != TG_OK) return rc;
+    tg::PSet ps;
+    std::memset(&ps, 0, sizeof ps);
+    for (int f = 0; f < 8; ++f) ps.f[f] = in[f];
+    cudaError_t e = tg::launch_kepler_pairs(npairs, ps, dt, out, c->status, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(TG_ECUDA, "kernel launch", e);
+    return TG_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Drop-in host entry points (libtupan.h signatures).
 // ---------------------------------------------------------------------------
 #define HC_BEGIN(K, NI, NJ)                        \
     HostCall h;                                    \
     std::memset(&h, 0, sizeof h);                  \
-    h.kernel = (K); h.ni = (NI); h.nj = (NJ);
+    h.nf = tg::kernel_fields(K); h.no = tg::kernel_outputs(K); h.ni = (NI); h.nj = (NJ);
 #define I5(m, x, y, z, e) h.in_i[0] = m; h.in_i[1] = x; h.in_i[2] = y; h.in_i[3] = z; h.in_i[4] = e;
 #define J5(m, x, y, z, e) h.in_j[0] = m; h.in_j[1] = x; h.in_j[2] = y; h.in_j[3] = z; h.in_j[4] = e;
 #define IV(u, v, w) h.in_i[5] = u; h.in_i[6] = v; h.in_i[7] = w;
@@ -489,6 +547,60 @@ void sakura_kernel(const unsigned long ni, const double *_im, const double *_irx
         return tg_sakura(ni, i[0], i[1], i[2], i[3], i[4], i[5], i[6], i[7], nj, j[0], j[1], j[2],
                          j[3], j[4], j[5], j[6], j[7], dt, flag, o[0], o[1], o[2], o[3], o[4], o[5],
                          TG_PREC_FP64, s);
+    });
+}
+
+void nreg_Xkernel(const unsigned long ni, const double *_im, const double *_irx, const double *_iry,
+                  const double *_irz, const double *_ie2, const double *_ivx, const double *_ivy,
+                  const double *_ivz, const unsigned long nj, const double *_jm, const double *_jrx,
+                  const double *_jry, const double *_jrz, const double *_je2, const double *_jvx,
+                  const double *_jvy, const double *_jvz, const double dt, double *_idrx,
+                  double *_idry, double *_idrz, double *_iax, double *_iay, double *_iaz,
+                  double *_iu) {
+    HC_BEGIN(tg::K_NREG_X, ni, nj)
+    I5(_im, _irx, _iry, _irz, _ie2) IV(_ivx, _ivy, _ivz)
+    J5(_jm, _jrx, _jry, _jrz, _je2) JV(_jvx, _jvy, _jvz)
+    h.out[0] = _idrx; h.out[1] = _idry; h.out[2] = _idrz;
+    h.out[3] = _iax; h.out[4] = _iay; h.out[5] = _iaz; h.out[6] = _iu;
+    host_call(h, [&](const double **i, const double **j, double **o, cudaStream_t s) {
+        return tg_nreg_x(ni, i[0], i[1], i[2], i[3], i[4], i[5], i[6], i[7], nj, j[0], j[1], j[2],
+                         j[3], j[4], j[5], j[6], j[7], dt, o[0], o[1], o[2], o[3], o[4], o[5], o[6],
+                         TG_PREC_FP64, s);
+    });
+}
+
+void nreg_Vkernel(const unsigned long ni, const double *_im, const double *_ivx, const double *_ivy,
+                  const double *_ivz, const double *_iax, const double *_iay, const double *_iaz,
+                  const unsigned long nj, const double *_jm, const double *_jvx, const double *_jvy,
+                  const double *_jvz, const double *_jax, const double *_jay, const double *_jaz,
+                  const double dt, double *_idvx, double *_idvy, double *_idvz, double *_ik) {
+    HC_BEGIN(tg::K_NREG_V, ni, nj)
+    h.nf = 7;   // m, vx, vy, vz, ax, ay, az
+    const double *ii[7] = {_im, _ivx, _ivy, _ivz, _iax, _iay, _iaz};
+    const double *jj[7] = {_jm, _jvx, _jvy, _jvz, _jax, _jay, _jaz};
+    for (int f = 0; f < 7; ++f) { h.in_i[f] = ii[f]; h.in_j[f] = jj[f]; }
+    h.out[0] = _idvx; h.out[1] = _idvy; h.out[2] = _idvz; h.out[3] = _ik;
+    host_call(h, [&](const double **i, const double **j, double **o, cudaStream_t s) {
+        return tg_nreg_v(ni, i[0], i[1], i[2], i[3], i[4], i[5], i[6], nj, j[0], j[1], j[2], j[3],
+                         j[4], j[5], j[6], dt, o[0], o[1], o[2], o[3], TG_PREC_FP64, s);
+    });
+}
+
+void kepler_solver_kernel(const double *_im, const double *_irx, const double *_iry,
+                          const double *_irz, const double *_ie2, const double *_ivx,
+                          const double *_ivy, const double *_ivz, const double dt, double *_ir1x,
+                          double *_ir1y, double *_ir1z, double *_iv1x, double *_iv1y,
+                          double *_iv1z) {
+    // one pair: two particles in, two out (the outputs may alias the inputs)
+    HostCall h;
+    std::memset(&h, 0, sizeof h);
+    h.nf = 8; h.no = 6; h.ni = 2; h.nj = 0;
+    const double *ii[8] = {_im, _irx, _iry, _irz, _ie2, _ivx, _ivy, _ivz};
+    for (int f = 0; f < 8; ++f) h.in_i[f] = ii[f];
+    h.out[0] = _ir1x; h.out[1] = _ir1y; h.out[2] = _ir1z; h.out[3] = _iv1x; h.out[4] = _iv1y; h.out[5] = _iv1z;
+    host_call(h, [&](const double **i, const double **, double **o, cudaStream_t s) {
+        return tg_kepler_solver(1, i[0], i[1], i[2], i[3], i[4], i[5], i[6], i[7], dt, o[0], o[1], o[2],
+                                o[3], o[4], o[5], s);
     });
 }
 

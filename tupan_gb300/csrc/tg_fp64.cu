@@ -286,6 +286,123 @@ struct AccVjp64 {
     }
 };
 
+// NREG_X (nreg_kernels_common.h:7-60): the pair separation is drifted by dt
+// with the relative velocity; sums m_j r_ij, the softened acceleration and
+// m_i sum m_j / r_ij.
+struct NregX64 {
+    static constexpr int NF = 8, NO = 7;
+    struct St { double m, x, y, z, e, u, v, w, mr[3], a[3], pot; };
+    __device__ static void init(St &s, const PairArgs &a, size_t i) {
+        s.m = a.I.f[F_M][i]; s.x = a.I.f[F_RX][i]; s.y = a.I.f[F_RY][i]; s.z = a.I.f[F_RZ][i];
+        s.e = a.I.f[F_E2][i]; s.u = a.I.f[F_VX][i]; s.v = a.I.f[F_VY][i]; s.w = a.I.f[F_VZ][i];
+        for (int k = 0; k < 3; ++k) { s.mr[k] = 0.0; s.a[k] = 0.0; }
+        s.pot = 0.0;
+    }
+    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a) {
+        double rx = dsub(s.x, sj[F_RX][jj]), ry = dsub(s.y, sj[F_RY][jj]), rz = dsub(s.z, sj[F_RZ][jj]);
+        const double e2 = dadd(s.e, sj[F_E2][jj]);
+        const double vx = dsub(s.u, sj[F_VX][jj]), vy = dsub(s.v, sj[F_VY][jj]), vz = dsub(s.w, sj[F_VZ][jj]);
+        rx = dadd(rx, dmul(vx, a.dt));
+        ry = dadd(ry, dmul(vy, a.dt));
+        rz = dadd(rz, dmul(vz, a.dt));
+        const double r2 = ddot3(rx, ry, rz, rx, ry, rz);
+        const double q2 = soft_q2(r2, e2);
+        const double q1 = dsqrt(q2);
+        const double mj = sj[F_M][jj];
+        const double q3 = dmul(dmul(q2, q1), mj);
+        s.mr[0] = dadd(s.mr[0], dmul(mj, rx));
+        s.mr[1] = dadd(s.mr[1], dmul(mj, ry));
+        s.mr[2] = dadd(s.mr[2], dmul(mj, rz));
+        s.a[0] = dsub(s.a[0], dmul(q3, rx));
+        s.a[1] = dsub(s.a[1], dmul(q3, ry));
+        s.a[2] = dsub(s.a[2], dmul(q3, rz));
+        s.pot = dadd(s.pot, dmul(mj, q1));
+    }
+    __device__ static void store(const St &s, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 3; ++k) { a.out[k][i] = s.mr[k]; a.out[3 + k][i] = s.a[k]; }
+        a.out[6][i] = dmul(s.m, s.pot);
+    }
+};
+
+// NREG_V (nreg_kernels_common.h:62-102): the relative velocity is kicked by
+// dt with the relative acceleration; sums m_j v_ij and m_i sum m_j |v_ij|^2.
+struct NregV64 {
+    static constexpr int NF = 11, NO = 4;
+    struct St { double m, u, v, w, ax, ay, az, mv[3], k; };
+    __device__ static void init(St &s, const PairArgs &a, size_t i) {
+        s.m = a.I.f[F_M][i]; s.u = a.I.f[F_VX][i]; s.v = a.I.f[F_VY][i]; s.w = a.I.f[F_VZ][i];
+        s.ax = a.I.f[F_AX][i]; s.ay = a.I.f[F_AY][i]; s.az = a.I.f[F_AZ][i];
+        for (int k = 0; k < 3; ++k) s.mv[k] = 0.0;
+        s.k = 0.0;
+    }
+    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a) {
+        double vx = dsub(s.u, sj[F_VX][jj]), vy = dsub(s.v, sj[F_VY][jj]), vz = dsub(s.w, sj[F_VZ][jj]);
+        const double ax = dsub(s.ax, sj[F_AX][jj]), ay = dsub(s.ay, sj[F_AY][jj]), az = dsub(s.az, sj[F_AZ][jj]);
+        vx = dadd(vx, dmul(ax, a.dt));
+        vy = dadd(vy, dmul(ay, a.dt));
+        vz = dadd(vz, dmul(az, a.dt));
+        const double v2 = ddot3(vx, vy, vz, vx, vy, vz);
+        const double mj = sj[F_M][jj];
+        s.mv[0] = dadd(s.mv[0], dmul(mj, vx));
+        s.mv[1] = dadd(s.mv[1], dmul(mj, vy));
+        s.mv[2] = dadd(s.mv[2], dmul(mj, vz));
+        s.k = dadd(s.k, dmul(mj, v2));
+    }
+    __device__ static void store(const St &s, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 3; ++k) a.out[k][i] = s.mv[k];
+        a.out[3][i] = dmul(s.m, s.k);
+    }
+};
+
+// Kepler pair solver (kepler_solver_kernel_common.h:8-81): one thread per
+// pair (2p, 2p+1).  The centre of mass drifts freely; the relative orbit
+// follows the bounded universal-variable solver with the pair bounds.  All
+// inputs of a pair are read before any output is written, so the outputs
+// may alias the inputs (the reference updates the particles in place).
+__global__ void __launch_bounds__(64) kepler_pairs(size_t npairs, PSet in, double dt, double *o0,
+                                                   double *o1, double *o2, double *o3, double *o4,
+                                                   double *o5, unsigned *status) {
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npairs) return;
+    const size_t ia = 2 * p, ib = 2 * p + 1;
+    const double im = in.f[F_M][ia], jm = in.f[F_M][ib];
+    double ir[3], jr[3], iv[3], jv[3];
+    for (int q = 0; q < 3; ++q) {
+        ir[q] = in.f[F_RX + q][ia]; jr[q] = in.f[F_RX + q][ib];
+        iv[q] = in.f[F_VX + q][ia]; jv[q] = in.f[F_VX + q][ib];
+    }
+    const double e2 = dadd(in.f[F_E2][ia], in.f[F_E2][ib]);
+    double r0[3], v0[3], rcm[3], vcm[3], r1[3], v1[3];
+    for (int q = 0; q < 3; ++q) { r0[q] = dsub(ir[q], jr[q]); v0[q] = dsub(iv[q], jv[q]); }
+    const double m = dadd(im, jm);
+    const double imu = ddiv(im, m), jmu = ddiv(jm, m);
+    for (int q = 0; q < 3; ++q) rcm[q] = dadd(dmul(imu, ir[q]), dmul(jmu, jr[q]));
+    for (int q = 0; q < 3; ++q) vcm[q] = dadd(dmul(imu, iv[q]), dmul(jmu, jv[q]));
+    for (int q = 0; q < 3; ++q) rcm[q] = dadd(rcm[q], dmul(vcm[q], dt));
+    KepBudget b;
+    b.split_cap = KEP_PAIR_SPLIT_CAP;
+    b.energy_cap = KEP_PAIR_ENERGY_CAP;
+    b.solve_budget = KEP_PAIR_SOLVE_BUDGET;
+    kep_solve(dt, m, e2, r0, v0, r1, v1, b);
+    double *o[6] = {o0, o1, o2, o3, o4, o5};
+    for (int q = 0; q < 3; ++q) {
+        o[q][ia] = dadd(rcm[q], dmul(jmu, r1[q]));
+        o[3 + q][ia] = dadd(vcm[q], dmul(jmu, v1[q]));
+        o[q][ib] = dsub(rcm[q], dmul(imu, r1[q]));
+        o[3 + q][ib] = dsub(vcm[q], dmul(imu, v1[q]));
+    }
+    if (b.flags) atomicOr(status, b.flags);
+}
+
+cudaError_t launch_kepler_pairs(size_t npairs, const PSet &in, double dt, double *const out[6],
+                                unsigned *status, cudaStream_t s) {
+    if (npairs == 0) return cudaSuccess;
+    const unsigned t = 64;
+    kepler_pairs<<<(unsigned)((npairs + t - 1) / t), t, 0, s>>>(npairs, in, dt, out[0], out[1], out[2],
+                                                                 out[3], out[4], out[5], status);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // Generic sequential-j engine.
 // ---------------------------------------------------------------------------
@@ -392,6 +509,8 @@ cudaError_t launch_fp64(int kernel, const PairArgs &a, int sms, cudaStream_t s) 
         case K_PNACC: return run<PNAcc64>(a, sms, s);
         case K_SAKURA: return run<Sakura64>(a, sms, s);
         case K_ACC_VJP: return run<AccVjp64>(a, sms, s);
+        case K_NREG_X: return run<NregX64>(a, sms, s);
+        case K_NREG_V: return run<NregV64>(a, sms, s);
         default: return cudaErrorInvalidValue;
     }
 }

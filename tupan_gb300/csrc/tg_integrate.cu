@@ -12,6 +12,11 @@
 //                            127-157, 200-235)
 //   tg_hermite_correct       Hermite corrector of order 2/4/6/8
 //                            (hermite.py:39-53, 93-119, 160-196, 238-283)
+//   tg_div3                  x = mx / d for three arrays (NREG's r = mr / M,
+//                            v = mv / M; nreg.py:27-29, 50-52)
+//   tg_sum                   float64 sum in numpy's pairwise order, for the
+//                            reductions that steer the reference integrators
+//                            (total mass, energies; nreg.py:22-63)
 //
 // Every expression is evaluated with uncontracted IEEE operations in the
 // order numpy evaluates the reference's Python expressions, so a GPU
@@ -125,6 +130,64 @@ __global__ void k_correct(CorrArgs p) {
     }
 }
 
+// numpy's float64 add-reduction of a contiguous array: blocks of at most 128
+// elements are summed with eight interleaved accumulators combined as
+// ((r0+r1)+(r2+r3))+((r4+r5)+(r6+r7)), then the tail in order; blocks of
+// fewer than 8 elements are summed in order from 0; longer ranges split at
+// n/2 rounded down to a multiple of 8 and add the halves; the reduction
+// starts from the identity 0.  One thread walks the recursion with an
+// explicit stack (depth <= 64): the reduction is O(n) adds with eight
+// independent chains per block, negligible next to the O(n^2) kernels whose
+// outputs it reduces.
+__device__ double pw_block(const double *a, size_t n) {
+    if (n < 8) {
+        double r = 0.0;
+        for (size_t i = 0; i < n; ++i) r = dadd(r, a[i]);
+        return r;
+    }
+    double r[8];
+    for (int j = 0; j < 8; ++j) r[j] = a[j];
+    size_t i = 8;
+    for (; i < n - (n % 8); i += 8)
+        for (int j = 0; j < 8; ++j) r[j] = dadd(r[j], a[i + j]);
+    double res = dadd(dadd(dadd(r[0], r[1]), dadd(r[2], r[3])), dadd(dadd(r[4], r[5]), dadd(r[6], r[7])));
+    for (; i < n; ++i) res = dadd(res, a[i]);
+    return res;
+}
+
+__global__ void k_sum_pairwise(size_t n, const double *a, double *out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    struct Frame { size_t off, n; double left; int stage; };
+    Frame st[64];
+    int sp = 0;
+    st[0] = Frame{0, n, 0.0, 0};
+    double ret = 0.0;
+    while (sp >= 0) {
+        Frame &f = st[sp];
+        if (f.n <= 128) { ret = pw_block(a + f.off, f.n); --sp; continue; }
+        size_t n2 = f.n / 2;
+        n2 -= n2 % 8;
+        if (f.stage == 0) {
+            f.stage = 1;
+            st[++sp] = Frame{f.off, n2, 0.0, 0};
+        } else if (f.stage == 1) {
+            f.left = ret;
+            f.stage = 2;
+            st[++sp] = Frame{f.off + n2, f.n - n2, 0.0, 0};
+        } else {
+            ret = dadd(f.left, ret);
+            --sp;
+        }
+    }
+    *out = dadd(0.0, ret);
+}
+
+__global__ void k_div3(size_t n, Ptr3 x, CPtr3 mx, double d) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int c = 0; c < 3; ++c) x.x[c][i] = ddiv(mx.x[c][i], d);
+}
+
 inline unsigned blocks_for(size_t n) { return (unsigned)((n + 255) / 256); }
 
 int check_ptrs(const void *const *p, int k) {
@@ -201,6 +264,21 @@ int tg_hermite_correct(int order, size_t n, double tau, const double *const *rv0
     for (int q = 0; q < m; ++q)
         for (int c = 0; c < 3; ++c) { a.d0[q][c] = deriv0[3 * q + c]; a.d1[q][c] = deriv1[3 * q + c]; }
     k_correct<<<blocks_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(a);
+    return launched();
+}
+
+int tg_div3(size_t n, double *x, double *y, double *z, const double *mx, const double *my,
+            const double *mz, double d, void *stream) {
+    if (n == 0) return TG_OK;
+    const void *p[6] = {x, y, z, mx, my, mz};
+    if (check_ptrs(p, 6)) return TG_EINVAL;
+    k_div3<<<blocks_for(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(n, Ptr3{{x, y, z}}, CPtr3{{mx, my, mz}}, d);
+    return launched();
+}
+
+int tg_sum(size_t n, const double *x, double *out, void *stream) {
+    if (!out || (n > 0 && !x)) return TG_EINVAL;
+    k_sum_pairwise<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>(n, x, out);
     return launched();
 }
 

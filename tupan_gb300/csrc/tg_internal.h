@@ -14,18 +14,25 @@ enum Field : int {
 };
 
 enum Kernel : int { K_PHI = 0, K_ACC, K_ACC_JERK, K_SNAP_CRACKLE, K_TSTEP, K_PNACC, K_SAKURA,
-                    K_ACC_VJP, K_COUNT };
+                    K_ACC_VJP, K_NREG_X, K_NREG_V, K_COUNT };
 // K_ACC_VJP reads the upstream gradient of the acceleration from the
 // F_AX..F_AZ slots of the particle set and writes r-bar (3) and m-bar (1).
+// K_NREG_V reads m, v and a (F_M, F_VX..F_AZ); its F_RX..F_E2 slots are
+// filled with the mass pointer so the contiguous field range stays valid.
 
-// Number of per-particle input fields each kernel reads (libtupan.h:2-246).
+// Number of leading per-particle field slots each kernel stages
+// (libtupan.h:2-246; the slots follow the Field order).
 constexpr int kernel_fields(int k) {
-    return k == K_PHI || k == K_ACC ? 5 : (k == K_SNAP_CRACKLE || k == K_ACC_VJP ? 14 : 8);
+    return k == K_PHI || k == K_ACC ? 5
+         : (k == K_SNAP_CRACKLE || k == K_ACC_VJP ? 14 : (k == K_NREG_V ? 11 : 8));
 }
 // Number of output arrays.
 constexpr int kernel_outputs(int k) {
-    return k == K_PHI ? 1 : (k == K_ACC || k == K_PNACC ? 3 : (k == K_TSTEP ? 2 : (k == K_ACC_VJP ? 4 : 6)));
+    return k == K_PHI ? 1
+         : (k == K_ACC || k == K_PNACC ? 3
+         : (k == K_TSTEP ? 2 : (k == K_ACC_VJP || k == K_NREG_V ? 4 : (k == K_NREG_X ? 7 : 6))));
 }
+constexpr int MAX_OUTPUTS = 7;
 
 struct PSet {
     const double *f[F_COUNT];
@@ -34,9 +41,9 @@ struct PSet {
 struct PairArgs {
     PSet I, J;
     size_t ni, nj;
-    double *out[6];
+    double *out[MAX_OUTPUTS];
     double eta;               // Tstep
-    double dt;                // Sakura
+    double dt;                // Sakura, NREG_X, NREG_V
     long long flag;           // Sakura
     unsigned long order;      // PNAcc
     double inv[8];            // PNAcc: inv[k] = 1/c^k
@@ -45,6 +52,11 @@ struct PairArgs {
 
 // Launchers (stream-ordered, asynchronous).  Return a cudaError_t.
 cudaError_t launch_fp64(int kernel, const PairArgs &a, int sms, cudaStream_t s);
+
+// Kepler pair solver: pair p = particles 2p and 2p+1 of `in` (F_M..F_VZ);
+// writes r, v after dt to out[0..5] (which may alias the inputs).
+cudaError_t launch_kepler_pairs(size_t npairs, const PSet &in, double dt, double *const out[6],
+                                unsigned *status, cudaStream_t s);
 
 // Split-FP32 path: packs j-records into `ws` and runs the stream-K kernel.
 struct Ds32Plan {

@@ -3,7 +3,8 @@
 // Restates, for the GPU, the pair evolution of tupan/lib/src/
 // sakura_kernel_common.h:8-191 (get_acc, leapfrog, twobody_solver,
 // evolve_twobody) and the universal-variable Kepler solver of
-// tupan/lib/src/universal_kepler_solver.h:17-614: Stumpff functions in their
+// tupan/lib/src/universal_kepler_solver.h:17-614 (also behind the Kepler
+// pair solver of kepler_solver_kernel_common.h:8-81): Stumpff functions in their
 // closed forms, order-5 Laguerre iteration (tolerance 2^-42, 64 iterations),
 // period folding for bound orbits, the hyperbolic first guess, the Lagrange
 // f/g update with r1 = sqrt(r1^2 + e2), step halving when the solver fails and
@@ -12,8 +13,9 @@
 //
 // The reference retries without bound and never returns for some inputs
 // (radial orbits with v = 0; softened close pairs whose energy test cannot
-// pass).  Here every retry loop is bounded: at most KEP_SPLIT_CAP halvings,
-// KEP_ENERGY_CAP doublings and KEP_SOLVE_BUDGET Kepler solves per pair.  When
+// pass).  Here every retry loop is bounded: at most split_cap halvings,
+// energy_cap doublings and solve_budget Kepler solves per pair (KepBudget;
+// KEP_* for Sakura, KEP_PAIR_* for the pair solver).  When
 // a bound is hit the last iterate is kept and a status bit is raised, which
 // the host turns into a nonzero return code.  Arithmetic operations use the
 // exact (uncontracted) helpers so that the leapfrog branch is bit-identical to
@@ -25,14 +27,23 @@ namespace tg {
 
 constexpr double KEP_TOL = 2.2737367544323205948e-13;  // 2^-42
 constexpr int KEP_MAXITER = 64;
+// Bounds for Sakura's pairwise kernel (N^2 pair evolutions per call) ...
 constexpr int KEP_SPLIT_CAP = 6;       // up to 64 sub-steps after solver failures
 constexpr int KEP_ENERGY_CAP = 4;      // up to 16 sub-steps for the energy test
 constexpr int KEP_SOLVE_BUDGET = 1024; // Kepler solves per pair evolution
+// ... and for the Kepler pair solver (a few pairs per call): up to 1024
+// sub-steps for either test and 65536 solves per pair.
+constexpr int KEP_PAIR_SPLIT_CAP = 10;
+constexpr int KEP_PAIR_ENERGY_CAP = 10;
+constexpr int KEP_PAIR_SOLVE_BUDGET = 65536;
 constexpr double KEP_PI = 3.141592653589793;
 
 struct KepBudget {
     int solves = 0;
     unsigned flags = 0;
+    int split_cap = KEP_SPLIT_CAP;
+    int energy_cap = KEP_ENERGY_CAP;
+    int solve_budget = KEP_SOLVE_BUDGET;
 };
 
 __device__ __forceinline__ int ksign(double x) { return (x > 0) - (x < 0); }
@@ -154,11 +165,11 @@ __device__ void kep_split(double dt, double m, double e2, const double r0[3], co
         for (int q = 0; q < 3; ++q) { r[q] = r0[q]; v[q] = v0[q]; }
         bool failed = false;
         for (long long i = 0; i < n; ++i) {
-            if (b.solves >= KEP_SOLVE_BUDGET) { b.flags |= ST_KEPLER_CAP; return; }
+            if (b.solves >= b.solve_budget) { b.flags |= ST_KEPLER_CAP; return; }
             if (kep_once(ddiv(dt, (double)n), m, e2, r, v, b) != 0) { failed = true; break; }
         }
         if (!failed) return;
-        if (tries >= KEP_SPLIT_CAP) { b.flags |= ST_KEPLER_CAP; return; }
+        if (tries >= b.split_cap) { b.flags |= ST_KEPLER_CAP; return; }
         n *= 2;
     }
 }
@@ -187,7 +198,7 @@ __device__ void kep_solve(double dt, double m, double e2, const double r0[3], co
     const double tol = dmul(64.0, KEP_TOL);
     if (dmul(2.0, fabs(dsub(en1, en0))) < dmul(tol, dadd(u1, u0))) return;
     long long n = 1;
-    for (int tries = 0; tries < KEP_ENERGY_CAP; ++tries) {
+    for (int tries = 0; tries < b.energy_cap; ++tries) {
         n *= 2;
         for (int q = 0; q < 3; ++q) { r[q] = r0[q]; v[q] = v0[q]; }
         bool bad = false;

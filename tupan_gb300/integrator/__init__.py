@@ -3,7 +3,8 @@
 Base and Integrator follow tupan/integrator/__init__.py:13-157 (base time
 step, power-of-two block step commensurate with the current time,
 evolve_step); Hermite (hermite2..8, ahermite2..8), SIA21 (sia21s/sia21a,
-kdk/dkd) and Sakura (sakura, asakura) are in the submodules.  All particle
+kdk/dkd), NREG (nreg, anreg) and Sakura (sakura, asakura) are in the
+submodules.  All particle
 state stays on the GPU; the element-wise updates are the fused FP64 kernels
 of libtupan_gb300 (tg_drift, tg_kick, tg_hermite_predict, ...), evaluated in
 the reference's operation order.
@@ -80,18 +81,20 @@ class Base(object):
             self.reporter.diagnostic_report(self.ps)
 
 
-from . import hermite, sakura, sia  # noqa: E402
+from . import hermite, nreg, sakura, sia  # noqa: E402
 
 
 class Integrator(object):
     """Method dispatcher (integrator/__init__.py:108-157)."""
-    PROVIDED_METHODS = (sia.SIA.PROVIDED_METHODS + sakura.Sakura.PROVIDED_METHODS
-                        + hermite.Hermite.PROVIDED_METHODS)
+    PROVIDED_METHODS = (sia.SIA.PROVIDED_METHODS + nreg.NREG.PROVIDED_METHODS
+                        + sakura.Sakura.PROVIDED_METHODS + hermite.Hermite.PROVIDED_METHODS)
 
     def __init__(self, eta, time, ps, **kwargs):
         method = kwargs.pop("method", None)
         if method in sia.SIA.PROVIDED_METHODS:
             self.integrator = sia.SIA(eta, time, ps, method, **kwargs)
+        elif method in nreg.NREG.PROVIDED_METHODS:
+            self.integrator = nreg.NREG(eta, time, ps, method, **kwargs)
         elif method in sakura.Sakura.PROVIDED_METHODS:
             self.integrator = sakura.Sakura(eta, time, ps, method, **kwargs)
         elif method in hermite.Hermite.PROVIDED_METHODS:

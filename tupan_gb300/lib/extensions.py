@@ -1,10 +1,10 @@
 """High-level kernel interface, mirroring tupan/lib/extensions.py.
 
-Same class names (Phi, Acc, AccJerk, SnapCrackle, Tstep, PNAcc, Sakura), the
-same `calc(ips, jps, *args)` call, the same output attribute names registered
-on `ips` through `ips.register_auxiliary_attribute(name, "real")`, the same
-module singletons and the same `clight` object (extensions.py:30-60,
-94-97, 100-507, 654-666).  The only backend is "CUDA": the GB300 library
+Same class names (Phi, Acc, AccJerk, SnapCrackle, Tstep, PNAcc, Sakura,
+NREG_X, NREG_V, Kepler), the same `calc(ips, jps, *args)` call, the same
+output attribute names registered on `ips` through
+`ips.register_auxiliary_attribute(name, "real")`, the same module singletons
+and the same `clight` object (extensions.py:30-60, 94-97, 100-651, 654-666).  The only backend is "CUDA": the GB300 library
 libtupan_gb300.so, reached through a Kernel object with the reference's
 protocol (cty, set_gsize, set_args, map_buffers, run; cffi_backend.py:90-126).
 
@@ -32,6 +32,9 @@ __all__ = ["Phi", "phi",
            "Tstep", "tstep",
            "PNAcc", "pnacc",
            "Sakura", "sakura",
+           "NREG_X", "nreg_x",
+           "NREG_V", "nreg_v",
+           "Kepler", "kepler",
            "Clight", "clight", "get_kernel"]
 
 PRECISIONS = {"float64": _native.PREC_FP64, "ds32": _native.PREC_DS32,
@@ -113,8 +116,9 @@ class CUDAKernel(object):
         if prec not in PRECISIONS:
             raise ValueError("Inappropriate 'prec': %r. Supported: %s" % (prec, sorted(PRECISIONS)))
         self.prec = prec
-        self.name = name[:-len("_kernel")] if name.endswith("_kernel") else name
-        if self.name not in _native.SPECS:
+        host = {v: k for k, v in _native.HOST_SYMBOLS.items()}
+        self.name = host.get(name, name[:-len("_kernel")] if name.endswith("_kernel") else name)
+        if self.name not in _native.SPECS and self.name != "kepler_solver":
             raise ValueError("unknown kernel %r" % name)
         types = namedtuple("Types", ["c_int", "c_int_p", "c_uint", "c_uint_p", "c_real", "c_real_p"])
         self.cty = types(c_int=int, c_int_p=None, c_uint=int, c_uint_p=None, c_real=float,
@@ -133,6 +137,8 @@ class CUDAKernel(object):
         self.args = list(args)
 
     def run(self):
+        if self.name == "kepler_solver":
+            return self._run_kepler()
         fields, scal, outs = _native.SPECS[self.name]
         nf, ns, no = len(fields), len(scal), len(outs)
         a = self.args
@@ -150,6 +156,21 @@ class CUDAKernel(object):
             if st:
                 warnings.warn("sakura: Kepler retry bound reached for some pairs (status %d); "
                               "the last iterate was kept" % st, RuntimeWarning)
+
+    def _run_kepler(self):
+        # args: m, rx, ry, rz, e2, vx, vy, vz, dt, then the six outputs
+        a = self.args
+        n = a[0].tensor.numel()
+        if n % 2:
+            raise ValueError("kepler_solver: the particle set must hold whole pairs (n = %d)" % n)
+        stream = torch.cuda.current_stream().cuda_stream
+        rc = _native.lib.tg_kepler_solver(n // 2, *[x.ptr for x in a[:8]], float(a[8]),
+                                          *[x.ptr for x in a[9:15]], stream)
+        _native.check(rc, "tg_kepler_solver")
+        st = _native.sync_status(stream)
+        if st:
+            warnings.warn("kepler_solver: retry bound reached for some pairs (status %d); "
+                          "the last iterate was kept" % st, RuntimeWarning)
 
     def map_buffers(self, arrays, buffers):
         for arr, buf in zip(arrays, buffers):
@@ -269,6 +290,59 @@ class Sakura(AbstractExtension):
         super(Sakura, self).set_args(ips, jps, float(dt), int(flag))
 
 
+class NREG_X(AbstractExtension):
+    """NREG position step (extensions.py:510-566): calc(ips, jps, dt) ->
+    (mrx, mry, mrz, ax, ay, az, u).  Always FP64."""
+    name = "nreg_Xkernel"
+    outputs = ("mrx", "mry", "mrz", "ax", "ay", "az", "u")
+
+    def set_args(self, ips, jps, dt):
+        super(NREG_X, self).set_args(ips, jps, float(dt))
+
+
+class NREG_V(AbstractExtension):
+    """NREG velocity step (extensions.py:569-617): calc(ips, jps, dt) ->
+    (mvx, mvy, mvz, mk).  Always FP64."""
+    name = "nreg_Vkernel"
+    outputs = ("mvx", "mvy", "mvz", "mk")
+
+    def set_args(self, ips, jps, dt):
+        super(NREG_V, self).set_args(ips, jps, float(dt))
+
+
+class Kepler(object):
+    """Kepler pair solver (extensions.py:620-651): calc(ips, jps, dt) moves
+    the particles of `ips` in place; every consecutive pair (2p, 2p+1) is
+    one two-body problem (the reference passes exactly one pair).  `jps` is
+    unused, as in the reference.  FP64."""
+    name = "kepler_solver_kernel"
+    fields = ("mass", "rx", "ry", "rz", "eps2", "vx", "vy", "vz")
+    outputs = ("rx", "ry", "rz", "vx", "vy", "vz")
+
+    def __init__(self, backend="CUDA", prec=None):
+        self.kernel = get_kernel(self.name, backend, prec)
+        self.argtypes = (self.kernel.cty.c_real_p,) * len(self.fields)
+        self.restypes = (self.kernel.c_real_out,) * len(self.outputs)
+
+    def set_args(self, ips, jps, dt):
+        self._inargs = tuple(getattr(ips, f) for f in self.fields)
+        self._outargs = tuple(getattr(ips, f) for f in self.outputs)
+        self.inargs = prepare_args(self._inargs, self.argtypes)
+        self.outargs = prepare_args(self._outargs, self.restypes)
+        self.kernel.set_args(self.inargs + [float(dt)] + self.outargs)
+
+    def run(self):
+        self.kernel.run()
+
+    def get_result(self):
+        return self.kernel.map_buffers(self._outargs, self.outargs)
+
+    def calc(self, ips, jps, dt):
+        self.set_args(ips, jps, dt)
+        self.run()
+        return self.get_result()
+
+
 backend = "CUDA"
 
 clight = Clight()
@@ -279,10 +353,14 @@ snap_crackle = SnapCrackle(backend)
 tstep = Tstep(backend)
 pnacc = PNAcc(backend)
 sakura = Sakura(backend)
+nreg_x = NREG_X(backend)
+nreg_v = NREG_V(backend)
+kepler = Kepler(backend)
 
 
 def set_precision(prec):
-    """Switch every module singleton to `prec` ("float64" or "ds32")."""
+    """Switch every module singleton to `prec` ("float64" or "ds32").  The
+    Sakura, NREG and Kepler kernels compute in FP64 either way."""
     global phi, acc, acc_jerk, snap_crackle, tstep, pnacc, sakura
     phi = Phi(backend, prec)
     acc = Acc(backend, prec)

@@ -10,6 +10,7 @@ stays resident in HBM between kernel calls.
 import numpy as np
 import torch
 
+from ._native import psum
 from .lib import extensions
 
 REAL_ATTRS = ("mass", "eps2", "rx", "ry", "rz", "vx", "vy", "vz", "time", "tstep")
@@ -105,19 +106,21 @@ class ParticleSystem(object):
         return float(self.tstep.abs().max())
 
     # ---- diagnostics (body.py:74-321), reduced on the GPU in FP64 ------------
+    # Sums go through tg_sum (numpy's pairwise order), so each value equals
+    # the reference's numpy reduction of the same arrays bit for bit.
     @property
     def total_mass(self):
-        return float(self.mass.sum())
+        return psum(self.mass)
 
     @property
     def com_r(self):
         m = self.mass
-        return torch.stack([(m * self.rx).sum(), (m * self.ry).sum(), (m * self.rz).sum()]).cpu().numpy() / self.total_mass
+        return np.array([psum(m * self.rx), psum(m * self.ry), psum(m * self.rz)]) / self.total_mass
 
     @property
     def com_v(self):
         m = self.mass
-        return torch.stack([(m * self.vx).sum(), (m * self.vy).sum(), (m * self.vz).sum()]).cpu().numpy() / self.total_mass
+        return np.array([psum(m * self.vx), psum(m * self.vy), psum(m * self.vz)]) / self.total_mass
 
     def com_move_to(self, com_r, com_v):
         self.rx += float(com_r[0]); self.ry += float(com_r[1]); self.rz += float(com_r[2])
@@ -145,7 +148,7 @@ class ParticleSystem(object):
 
     @property
     def kinetic_energy(self):
-        return float(self.ke.sum())
+        return psum(self.ke)
 
     @property
     def pe(self):
@@ -154,7 +157,7 @@ class ParticleSystem(object):
 
     @property
     def potential_energy(self):
-        return 0.5 * float(self.pe.sum())
+        return 0.5 * psum(self.pe)
 
     @property
     def virial_energy(self):
