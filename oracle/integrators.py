@@ -6,8 +6,10 @@ logic and update expressions in numpy's evaluation order:
 
   Base.get_base_tstep / get_min_block_tstep   tupan/integrator/__init__.py:49-78
   Hermite H2/H4/H6/H8 epredict/ecorrect/epec  tupan/integrator/hermite.py:20-283, 387-410
-  SIA21 kdk/dkd with the shared-step bridge   tupan/integrator/sia.py:64-86, 193-230, 300-352, 1032-1123
+  SIA21..SIA69 kdk/dkd, s./a./h. modes with   tupan/integrator/sia.py:24-86, 186-230, 300-961, 1032-1123
+  the slow/fast split and FewBody             tupan/integrator/fewbody.py:13-57
   sakura_step / asakura step                  tupan/integrator/sakura.py:22-50, 100-159
+  NREG nreg_x/nreg_v/anreg_step/nreg_step     tupan/integrator/nreg.py:22-165
 
 With the FP64 oracle kernels (bit-identical to the reference C backend) the
 trajectories are bit-identical to the reference integrators; pinned in
@@ -39,6 +41,7 @@ def make_ps(d):
     ps["time"] = np.zeros(ps.n)
     ps["tstep"] = np.zeros(ps.n)
     ps["nstep"] = np.zeros(ps.n, dtype=np.int64)
+    ps["id"] = np.arange(ps.n, dtype=np.int64)
     return ps
 
 
@@ -47,8 +50,14 @@ class Kernels(object):
         self.o = Oracle()
         self.nthreads = nthreads
 
-    def acc(self, ps):
-        ps["ax"], ps["ay"], ps["az"] = self.o.calc("acc", ps, ps, nthreads=self.nthreads)
+    def acc(self, ps, jps=None):
+        ps["ax"], ps["ay"], ps["az"] = self.o.calc("acc", ps, ps if jps is None else jps,
+                                                   nthreads=self.nthreads)
+
+    def kepler(self, ps, dt):
+        r = self.o.kepler(ps, dt)
+        for k, v in zip(("rx", "ry", "rz", "vx", "vy", "vz"), r):
+            ps[k] = v
 
     def acc_jerk(self, ps):
         r = self.o.calc("acc_jerk", ps, ps, nthreads=self.nthreads)
@@ -62,6 +71,19 @@ class Kernels(object):
 
     def tstep(self, ps, eta):
         ps["tstep"], ps["tstepij"] = self.o.calc("tstep", ps, ps, eta, nthreads=self.nthreads)
+
+    def phi(self, ps):
+        ps["phi"], = self.o.calc("phi", ps, ps, nthreads=self.nthreads)
+
+    def nreg_x(self, ps, dt):
+        r = self.o.calc("nreg_x", ps, ps, dt, nthreads=self.nthreads)
+        for k, v in zip(("mrx", "mry", "mrz", "ax", "ay", "az", "u"), r):
+            ps[k] = v
+
+    def nreg_v(self, ps, dt):
+        r = self.o.calc("nreg_v", ps, ps, dt, nthreads=self.nthreads)
+        for k, v in zip(("mvx", "mvy", "mvz", "mk"), r):
+            ps[k] = v
 
     def sakura(self, ps, dt, flag):
         r = self.o.calc("sakura", ps, ps, dt, flag, nthreads=self.nthreads)
@@ -188,39 +210,136 @@ class Hermite(Base):
         return ps1
 
 
-# --- SIA21 ---------------------------------------------------------------
-class SIA21(Base):
+# --- SIA ------------------------------------------------------------------
+SIA_COEFS = {
+    "sia21": ([1.0], [0.5]),
+    "sia22": ([0.5], [0.1931833275037836, 0.6136333449924328]),
+    "sia43": ([1.3512071919596575, -1.7024143839193150],
+              [0.6756035959798288, -0.17560359597982877]),
+    "sia44": ([0.7123418310626056, -0.21234183106260562],
+              [0.1786178958448091, -0.06626458266981843, 0.7752933736500186]),
+    "sia45": ([-0.0844296195070715, 0.354900057157426, 0.459059124699291],
+              [0.2750081212332419, -0.1347950099106792, 0.35978688867743724]),
+    "sia46": ([0.209515106613362, -0.143851773179818, 0.434336666566456],
+              [0.0792036964311957, 0.353172906049774, -0.0420650803577195, 0.21937695575349958]),
+    "sia67": ([0.7845136104775573, 0.23557321335935813, -1.177679984178871, 1.3151863206839112],
+              [0.39225680523877865, 0.5100434119184577, -0.47105338540975644, 0.06875316825252015]),
+    "sia69": ([0.39103020330868477, 0.334037289611136, -0.7062272811875614, 0.08187754964805945,
+               0.7985644772393624],
+              [0.19551510165434238, 0.3625337464599104, -0.1860949957882127, -0.31217486576975095,
+               0.44022101344371095]),
+}
+
+
+def sia_sequence(first, second):
+    """The symmetric operator sequence of one SIA propagator (sia.py:300-961):
+    operator 0 with the coefficients `second` opens and closes it and
+    alternates with operator 1 (coefficients `first`)."""
+    half = []
+    for i in range(len(first)):
+        half += [(0, second[i]), (1, first[i])]
+    if len(second) == len(first) + 1:
+        half.append((0, second[-1]))
+    return half + half[:-1][::-1]
+
+
+def ps_select(ps, mask):
+    return PS({k: v[mask] for k, v in ps.items()})
+
+
+def ps_join(slow, fast):
+    if not fast.n:
+        return slow
+    if not slow.n:
+        return fast
+    out = PS()
+    for k in set(slow) | set(fast):
+        a = slow.get(k, np.zeros(slow.n, dtype=fast[k].dtype if k in fast else np.float64))
+        b = fast.get(k, np.zeros(fast.n, dtype=a.dtype))
+        out[k] = np.concatenate((a, b))
+    return out
+
+
+class SIA(Base):
     def __init__(self, eta, time, ps, method, kernels):
-        super(SIA21, self).__init__(eta, time, ps, kernels)
+        super(SIA, self).__init__(eta, time, ps, kernels)
         self.method = method
+        self.ops = sia_sequence(*SIA_COEFS[method[:5]])
+        mode = method[5]
+        self.update_tstep = mode in "ah"
+        self.shared_tstep = mode in "sa"
+        self.kdk = method.endswith("kdk")
 
     def drift(self, ps, tau):
         for a in "xyz":
             ps["r" + a] += ps["v" + a] * tau
 
-    def kick(self, ps, tau):
-        self.k.acc(ps)
+    def kick_n(self, ps, tau):
         for a in "xyz":
             ps["v" + a] += ps["a" + a] * tau
 
+    def kick(self, ps, tau):
+        self.k.acc(ps)
+        self.kick_n(ps, tau)
+
+    def fewbody(self, ps, tau):
+        if ps.n == 1:
+            self.drift(ps, tau)
+        elif ps.n == 2:
+            self.k.kepler(ps, tau)
+        return ps
+
     def evolve(self, ps, tau):
-        if self.method.endswith("kdk"):
-            self.kick(ps, 0.5 * tau)
-            self.drift(ps, 1.0 * tau)
-            self.kick(ps, 0.5 * tau)
+        if ps.n <= 2:
+            return self.fewbody(ps, tau)
+        for op, c in self.ops:
+            if (op == 0) == self.kdk:
+                self.kick(ps, c * tau)
+            else:
+                self.drift(ps, c * tau)
+        return ps
+
+    def sf_kick(self, slow, fast, tau):
+        if slow.n and fast.n:
+            self.k.acc(slow, fast)
+            self.k.acc(fast, slow)
+            self.kick_n(slow, tau)
+            self.kick_n(fast, tau)
+
+    def bridge(self, slow, fast, tau):
+        for op, c in self.ops:
+            if op == 0:
+                slow = self.evolve(slow, c * tau)
+                fast = self.recurse(fast, c * tau)
+            else:
+                self.sf_kick(slow, fast, c * tau)
+        return slow, fast
+
+    def recurse(self, ps, tau):
+        if not ps.n:
+            return ps
+        flag = -1
+        if self.update_tstep:
+            flag = 1
+            self.k.tstep(ps, self.eta)
+            if self.shared_tstep:
+                tau = self.get_min_block_tstep(ps, tau)
+        if ps.n <= 2:
+            slow, fast = ps, PS({k: v[:0] for k, v in ps.items()})
         else:
-            self.drift(ps, 0.5 * tau)
-            self.kick(ps, 1.0 * tau)
-            self.drift(ps, 0.5 * tau)
+            cond = np.abs(ps["tstep"]) > flag * abs(tau)
+            slow, fast = ps_select(ps, cond), ps_select(ps, ~cond)
+        slow, fast = self.bridge(slow, fast, tau)
+        if fast.n == 0:
+            self.t_curr += tau
+        if slow.n:
+            slow["tstep"][...] = tau
+            slow["time"] += tau
+            slow["nstep"] += 1
+        return ps_join(slow, fast)
 
     def do_step(self, ps, tau):
-        if "a." in self.method:
-            self.k.tstep(ps, self.eta)
-            tau = self.get_min_block_tstep(ps, tau)
-        self.evolve(ps, 0.5 * tau)
-        self.evolve(ps, 0.5 * tau)
-        self.finish(ps, tau)
-        return ps
+        return self.recurse(ps, tau)
 
 
 # --- Sakura --------------------------------------------------------------
@@ -253,12 +372,78 @@ class Sakura(Base):
         return ps
 
 
+# --- NREG ----------------------------------------------------------------
+class NREG(Base):
+    """Algorithmic regularisation (nreg.py:22-165): positions move by h/W and
+    velocities by h/U in a fictitious time; the physical time is the sum of
+    the position steps.  E0, W, U, S are the reference's class attributes of
+    the particle type."""
+
+    def __init__(self, eta, time, ps, method, kernels):
+        super(NREG, self).__init__(eta, time, ps, kernels)
+        self.method = method
+        self.initialised = False
+
+    def energies(self, ps):
+        ke = float((0.5 * ps["mass"] * (ps["vx"] ** 2 + ps["vy"] ** 2 + ps["vz"] ** 2)).sum())
+        self.k.phi(ps)
+        pe = 0.5 * float((ps["mass"] * ps["phi"]).sum())
+        return ke, pe
+
+    def initialise(self, ps):
+        ke, pe = self.energies(ps)
+        self.E0 = ke + pe
+        self.W = self.U = self.S = -pe
+        self.initialised = True
+
+    def nreg_x(self, ps, dt):
+        mtot = float(ps["mass"].sum())
+        self.k.nreg_x(ps, dt)
+        for a in "xyz":
+            ps["r" + a][...] = ps["mr" + a] / mtot
+        self.U = 0.5 * ps["u"].sum()
+        self.t_curr += dt
+
+    def nreg_v(self, ps, dt):
+        mtot = float(ps["mass"].sum())
+        self.k.nreg_v(ps, dt)
+        for a in "xyz":
+            ps["v" + a][...] = ps["mv" + a] / mtot
+        K = 0.25 * ps["mk"].sum() / mtot
+        self.W = K - self.E0
+
+    def anreg_step(self, ps, h):
+        self.nreg_x(ps, 0.5 * (h / self.W))
+        self.nreg_v(ps, (h / self.U))
+        self.nreg_x(ps, 0.5 * (h / self.W))
+
+    def nreg_step(self, ps, h):
+        self.anreg_step(ps, 0.5 * (h * self.S))
+        self.S = 1 / (2 / self.W - 1 / self.S)
+        self.anreg_step(ps, 0.5 * (h * self.S))
+
+    def do_step(self, ps, tau):
+        if not self.initialised:
+            self.initialise(ps)
+        t0 = self.t_curr
+        if "anreg" in self.method:
+            self.anreg_step(ps, tau / 2)
+        else:
+            self.nreg_step(ps, tau)
+        ps["tstep"][...] = self.t_curr - t0
+        ps["time"] += tau
+        ps["nstep"] += 1
+        return ps
+
+
 def integrator(method, eta, ps, kernels=None, time=0.0):
     kernels = kernels or Kernels()
+    if method in ("nreg", "anreg"):
+        return NREG(eta, time, ps, method, kernels)
     if "hermite" in method:
         return Hermite(eta, time, ps, method, kernels)
-    if method.startswith("sia21"):
-        return SIA21(eta, time, ps, method, kernels)
+    if method.startswith("sia"):
+        return SIA(eta, time, ps, method, kernels)
     if "sakura" in method:
         return Sakura(eta, time, ps, method, kernels)
     raise ValueError(method)

@@ -141,7 +141,7 @@ def main():
         print("wrote", path, os.path.getsize(path), "bytes,", len(calls), "calls")
 
 
-if __name__ == "__main__" and "--integrators" not in sys.argv:
+if __name__ == "__main__" and "--integrators" not in sys.argv and "--nreg-kepler" not in sys.argv:
     main()
 
 
@@ -159,6 +159,22 @@ INTEGRATOR_RUNS = (
     ("sia21a.kdk", 0.01, 1.0 / 32, 1e-3),
     ("sakura", 1.0 / 128, 1.0 / 64, 0.0),
     ("asakura", 0.01, 1.0 / 64, 0.0),
+    ("nreg", 1.0 / 256, 1.0 / 32, 1e-3),
+    ("anreg", 1.0 / 256, 1.0 / 32, 1e-3),
+    ("sia22s.dkd", 1.0 / 256, 1.0 / 32, 1e-3),
+    ("sia43s.kdk", 1.0 / 256, 1.0 / 32, 1e-3),
+    ("sia44a.dkd", 0.01, 1.0 / 32, 1e-3),
+    ("sia45s.kdk", 1.0 / 256, 1.0 / 64, 1e-3),
+    ("sia46a.kdk", 0.01, 1.0 / 64, 1e-3),
+    ("sia67s.dkd", 1.0 / 128, 1.0 / 64, 1e-3),
+    ("sia69s.kdk", 1.0 / 128, 1.0 / 64, 1e-3),
+    # hierarchical split; eps2 = 0 so that two-body subsystems take the
+    # Kepler solver's unsoftened branch, whose retries always terminate
+    ("sia21h.dkd", 1.0 / 128, 1.0 / 32, 0.0),
+    ("sia21h.kdk", 1.0 / 128, 1.0 / 32, 0.0),
+    ("sia22h.dkd", 1.0 / 128, 1.0 / 32, 1e-3),
+    ("sia44h.kdk", 1.0 / 128, 1.0 / 64, 0.0),
+    ("sia69h.kdk", 1.0 / 128, 1.0 / 64, 0.0),
 )
 
 
@@ -197,6 +213,7 @@ def reference_trajectories(ref_root="/root/reference"):
         store["cfg_" + key] = np.array([eta, t_end, eps2, steps, integ.time])
         for f in ("rx", "ry", "rz", "vx", "vy", "vz"):
             store["end_%s_%s" % (key, f)] = np.array(getattr(out, f))
+        store["end_%s_id" % key] = np.array(out.id, dtype=np.int64)
         print(method, steps, "steps to", integ.time)
     path = os.path.join(HERE, "golden_integrators.npz")
     np.savez_compressed(path, **store)
@@ -205,3 +222,99 @@ def reference_trajectories(ref_root="/root/reference"):
 
 if __name__ == "__main__" and "--integrators" in sys.argv:
     reference_trajectories()
+
+
+# ---------------------------------------------------------------------------
+# NREG_X / NREG_V and the Kepler pair solver (libtupan.h:152-201, 231-246).
+#
+#   python tests/golden/make_golden.py --nreg-kepler
+#
+# golden_nreg.npz: nreg_x and nreg_v of the reference on the inputs of the
+# four kernel cases above (read back from their fixtures) at dt = 0, 1/64 and
+# -0.3, plus the i=all vs j=prefix / i=prefix vs j=all sweeps on "sweep" at
+# dt = 1/64.
+# golden_kepler.npz: kepler_solver_kernel of the reference, one call per
+# pair, on seeded pairs: bound orbits (e up to 0.95, apocentre start),
+# hyperbolic encounters, pairs with eps2 = (1e-6 a)^2 / 2, a pair at r = 0
+# and a massless companion; dt = 1/64, 0.37 and -0.5.  Softened pairs that
+# need more sub-steps than the GPU solver's bounds are not in the fixture
+# (the reference's retry loops are unbounded; see tests/test_gpu_nreg_kepler.py).
+# ---------------------------------------------------------------------------
+NREG_DTS = (0.0, 1.0 / 64, -0.3)
+KEPLER_DTS = (1.0 / 64, 0.37, -0.5)
+
+
+def kepler_pairs(rng, npairs, kind, soft=0.0):
+    p8 = ("mass", "rx", "ry", "rz", "eps2", "vx", "vy", "vz")
+    ps = {f: np.zeros(2 * npairs) for f in p8}
+    for p in range(npairs):
+        m1, m2 = rng.random() * 0.5 + 0.01, rng.random() * 0.5 + 0.01
+        a = np.exp(rng.uniform(np.log(1e-3), np.log(1.0)))
+        e = 0.95 * np.sqrt(rng.random())
+        M = m1 + m2
+        if kind == "hyper":
+            r = a
+            v = np.sqrt(2 * M / r) * (1.2 + rng.random())
+        else:
+            r = a * (1 + e)
+            v = np.sqrt(M * (1 - e) / (a * (1 + e)))
+        q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        rr, vv = q @ np.array([r, 0.0, 0.0]), q @ np.array([0.0, v, 0.0])
+        cm, cv = rng.normal(size=3), rng.normal(size=3) * 0.3
+        ri, rj = cm + m2 / M * rr, cm - m1 / M * rr
+        vi, vj = cv + m2 / M * vv, cv - m1 / M * vv
+        for k, c in enumerate("xyz"):
+            ps["r" + c][2 * p], ps["r" + c][2 * p + 1] = ri[k], rj[k]
+            ps["v" + c][2 * p], ps["v" + c][2 * p + 1] = vi[k], vj[k]
+        ps["mass"][2 * p], ps["mass"][2 * p + 1] = m1, m2
+        ps["eps2"][2 * p] = ps["eps2"][2 * p + 1] = (a * soft) ** 2 / 2
+    return ps
+
+
+def kepler_edge_pairs():
+    # a pair at r = 0 (centre of mass drifts only) and a massless companion
+    p8 = ("mass", "rx", "ry", "rz", "eps2", "vx", "vy", "vz")
+    ps = {f: np.zeros(4) for f in p8}
+    ps["mass"][:] = [0.3, 0.2, 0.5, 0.0]
+    ps["rx"][:] = [1.0, 1.0, -0.5, -0.4]
+    ps["ry"][:] = [0.5, 0.5, 0.2, 0.2]
+    ps["vx"][:] = [0.1, -0.2, 0.0, 0.0]
+    ps["vy"][:] = [0.0, 0.3, 0.0, 1.5]
+    return ps
+
+
+def nreg_kepler():
+    ref = ReferenceLib()
+    store = {}
+    for case in ("sweep", "plummer", "binary", "edge"):
+        z = np.load(os.path.join(HERE, "golden_%s.npz" % case))
+        ps = {f: z["in_" + f] for f in FIELDS}
+        for dt in NREG_DTS:
+            for name in ("nreg_x", "nreg_v"):
+                key = "%s_%s_%r" % (case, name, dt)
+                store[key] = np.stack(ref.calc(name, ps, ps, dt))
+                if case == "sweep" and dt == 1.0 / 64:
+                    for p in PREFIXES:
+                        sub = {f: ps[f][:p] for f in FIELDS}
+                        store["J%d_" % p + key] = np.stack(ref.calc(name, ps, sub, dt))
+                        store["I%d_" % p + key] = np.stack(ref.calc(name, sub, ps, dt))
+    path = os.path.join(HERE, "golden_nreg.npz")
+    np.savez_compressed(path, **store)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+    rng = np.random.default_rng(5)
+    sets = {"bound": kepler_pairs(rng, 16, "bound"), "hyper": kepler_pairs(rng, 16, "hyper"),
+            "soft": kepler_pairs(rng, 16, "bound", soft=1e-6), "edge": kepler_edge_pairs()}
+    store = {}
+    for kind, ps in sets.items():
+        for f, v in ps.items():
+            store["in_%s_%s" % (kind, f)] = v
+        for dt in KEPLER_DTS:
+            store["out_%s_%r" % (kind, dt)] = np.stack(ref.kepler(ps, dt))
+    path = os.path.join(HERE, "golden_kepler.npz")
+    np.savez_compressed(path, **store)
+    print("wrote", path, os.path.getsize(path), "bytes")
+
+
+if __name__ == "__main__" and "--nreg-kepler" in sys.argv:
+    nreg_kepler()

@@ -84,3 +84,91 @@ def test_oracle_matches_reference_build(orc, seed):
     for flag in (-2, -1, 1, 2):
         _check("sakura", orc.calc("sakura", ps, ps, 0.01, flag),
                np.stack(ref.calc("sakura", ps, ps, 0.01, flag)))
+
+
+# ---------------------------------------------------------------------------
+# NREG_X / NREG_V and the Kepler pair solver (golden_nreg.npz,
+# golden_kepler.npz from tests/golden/make_golden.py --nreg-kepler).
+# ---------------------------------------------------------------------------
+NREG_DTS = (0.0, 1.0 / 64, -0.3)
+KEPLER_DTS = (1.0 / 64, 0.37, -0.5)
+KEPLER_KINDS = ("bound", "hyper", "soft", "edge")
+P8 = ("mass", "rx", "ry", "rz", "eps2", "vx", "vy", "vz")
+
+
+def load_nreg():
+    import os
+    from golden_io import GOLDEN
+    return np.load(os.path.join(GOLDEN, "golden_nreg.npz"))
+
+
+def load_kepler():
+    import os
+    from golden_io import GOLDEN
+    z = np.load(os.path.join(GOLDEN, "golden_kepler.npz"))
+    sets = {k: {f: z["in_%s_%s" % (k, f)] for f in P8} for k in KEPLER_KINDS}
+    return z, sets
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_nreg_matches_golden(orc, case):
+    g = load_nreg()
+    _, ps, _ = load(case)
+    for dt in NREG_DTS:
+        for name in ("nreg_x", "nreg_v"):
+            key = "%s_%s_%r" % (case, name, dt)
+            assert np.array_equal(np.stack(orc.calc(name, ps, ps, dt, nthreads=3)), g[key]), key
+
+
+def test_oracle_nreg_prefix_sweeps(orc):
+    g = load_nreg()
+    _, ps, _ = load("sweep")
+    for name in ("nreg_x", "nreg_v"):
+        key = "sweep_%s_%r" % (name, 1.0 / 64)
+        for p in PREFIXES:
+            sub = {f: ps[f][:p] for f in FIELDS}
+            assert np.array_equal(np.stack(orc.calc(name, ps, sub, 1.0 / 64)), g["J%d_" % p + key])
+            assert np.array_equal(np.stack(orc.calc(name, sub, ps, 1.0 / 64)), g["I%d_" % p + key])
+
+
+@pytest.mark.parametrize("kind", KEPLER_KINDS)
+def test_oracle_kepler_matches_golden(orc, kind):
+    z, sets = load_kepler()
+    for dt in KEPLER_DTS:
+        capped = []
+        got = np.stack(orc.kepler(sets[kind], dt, nthreads=2, capped=capped))
+        assert not any(capped), (kind, dt)
+        assert np.array_equal(got, z["out_%s_%r" % (kind, dt)]), (kind, dt)
+
+
+def test_oracle_kepler_reports_bounds(orc):
+    """A softened close pair whose energy test cannot pass within the bounds
+    (the reference keeps halving its sub-steps for millions of solves)."""
+    ps = {f: np.zeros(2) for f in P8}
+    ps["mass"][:] = [0.5, 0.5]
+    ps["rx"][:] = [1e-3, -1e-3]
+    ps["vy"][:] = [10.0, -10.0]
+    ps["eps2"][:] = [1e-7, 1e-7]
+    capped = []
+    out = np.stack(orc.kepler(ps, 0.37, capped=capped))
+    assert capped == [True]
+    assert np.all(np.isfinite(out))
+
+
+@pytest.mark.skipif(not reference_available(), reason="reference not built here")
+def test_oracle_nreg_kepler_match_reference_build(orc):
+    ref = ReferenceLib()
+    rng = np.random.default_rng(3)
+    n = 120
+    ps = {f: rng.normal(size=n) for f in FIELDS}
+    ps["mass"] = rng.random(n)
+    ps["eps2"] = rng.random(n) * 1e-3
+    for name in ("nreg_x", "nreg_v"):
+        for dt in (0.01, -0.07):
+            assert np.array_equal(np.stack(orc.calc(name, ps, ps, dt)), np.stack(ref.calc(name, ps, ps, dt)))
+    from golden.make_golden import kepler_pairs
+    pairs = kepler_pairs(np.random.default_rng(11), 6, "bound")
+    capped = []
+    got = np.stack(orc.kepler(pairs, 0.2, capped=capped))
+    assert not any(capped)
+    assert np.array_equal(got, np.stack(ref.kepler(pairs, 0.2)))

@@ -66,6 +66,21 @@ class ParticleSystem(object):
             setattr(new, k, v.clone())
         return new
 
+    def append(self, other):
+        """Concatenate `other`'s particles after these (body.py:641-645); an
+        attribute present on one side only is zero-filled on the other."""
+        if not other.n:
+            return
+        mine, theirs = self._arrays(), other._arrays()
+        for k in set(mine) | set(theirs):
+            a, b = mine.get(k), theirs.get(k)
+            if a is None:
+                a = torch.zeros(self.n, dtype=b.dtype, device=b.device)
+            if b is None:
+                b = torch.zeros(other.n, dtype=a.dtype, device=a.device)
+            setattr(self, k, torch.cat((a, b)))
+        self.n += other.n
+
     def __getitem__(self, slc):
         new = ParticleSystem.__new__(ParticleSystem)
         new.__dict__["_device"] = self._device
