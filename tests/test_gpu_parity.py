@@ -186,6 +186,24 @@ def test_streamk_shapes_ds32_vs_oracle(ext, orc, ni, nj):
         assert np.array_equal(got64, want), (name, ni, nj)
 
 
+@pytest.mark.parametrize("n", [500, 3000])
+def test_uniform_softening_path_is_bit_identical(ext, n):
+    """Tiles whose pairs all share one softening value take the form with the
+    softening add hoisted; it must give the per-pair form's bits.  Changing
+    one i-particle's eps2 sends its whole i-tile (the first 512 i) down the
+    per-pair form while every other pair keeps the same softening value, so
+    all other particles' results must be unchanged bit for bit."""
+    d = plummer(n, seed=11)
+    J = PS(d)
+    I2 = dict(d)
+    I2["eps2"] = d["eps2"].copy()
+    I2["eps2"][0] *= 2.0
+    for name in ("acc", "acc_jerk", "phi"):
+        uniform = run_kernel(ext, name, "ds32", PS(d), J, ())
+        general = run_kernel(ext, name, "ds32", PS(I2), J, ())
+        assert np.array_equal(uniform[:, 1:], general[:, 1:]), name
+
+
 def test_ds32_is_deterministic(ext):
     d = plummer(6000, seed=3)
     P = PS(d)

@@ -63,6 +63,7 @@ struct DsArgs {
     const float4 *rec;   // packed j-records
     double *part;        // [gridDim.x][2][IPT][NP][DS_THREADS]
     int *ticket;         // [NIT]
+    const float *tile_e2;  // [NJT] common j softening per tile or NaN; may be null
     long long nit, njt;  // i-tiles, j-tiles
 };
 
@@ -172,21 +173,24 @@ __device__ __forceinline__ float2 hi2(float4 q) { return make_float2(q.z, q.w); 
 template <int IPT_, bool REFINE>
 struct AccDS {
     static constexpr int IPT = IPT_, JF = 8, NQ = 4, NP = 3;
+    static constexpr bool UE2 = true;
     struct IS { IPos q; float2 e; float2 a[3]; Comp c[3]; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {
         load_pos(a, i, s.q);
         s.e = f2(__double2float_rn(a.I.f[F_E2][i]));
         for (int k = 0; k < 3; ++k) { s.a[k] = f2(0.f); s.c[k] = Comp{0.f, 0.f}; }
     }
-    // record: {xh,yh} {zh,xl} {yl,zl} {m,e2}
-    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R) {
+    // record: {xh,yh} {zh,xl} {yl,zl} {m,e2}.  UE: every pair of the tile
+    // has the softening E (= ie2 + je2 for all pairs), so the add is hoisted.
+    template <bool UE>
+    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R, float2 E) {
         const float4 q0 = R[0], q1 = R[1], q2 = R[2], q3 = R[3];
 #pragma unroll
         for (int u = 0; u < IPT; ++u) {
             IS &s = S[u];
             float2 dx, dy, dz;
             pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), dx, dy, dz);
-            const float2 e2 = add2(s.e, hi2(q3));
+            const float2 e2 = UE ? E : add2(s.e, hi2(q3));
             const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
             // 1/r^2 from y*y here: with one more MUFU per pair Acc would be
             // XU-bound (18 packed FP32 ops vs 4 MUFU per two pairs)
@@ -212,20 +216,22 @@ struct AccDS {
 template <int IPT_, bool REFINE>
 struct PhiDS {
     static constexpr int IPT = IPT_, JF = 8, NQ = 4, NP = 1;
+    static constexpr bool UE2 = true;
     struct IS { IPos q; float2 e; float2 p; Comp c; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {
         load_pos(a, i, s.q);
         s.e = f2(__double2float_rn(a.I.f[F_E2][i]));
         s.p = f2(0.f); s.c = Comp{0.f, 0.f};
     }
-    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R) {
+    template <bool UE>
+    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R, float2 E) {
         const float4 q0 = R[0], q1 = R[1], q2 = R[2], q3 = R[3];
 #pragma unroll
         for (int u = 0; u < IPT; ++u) {
             IS &s = S[u];
             float2 dx, dy, dz;
             pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), dx, dy, dz);
-            const float2 e2 = add2(s.e, hi2(q3));
+            const float2 e2 = UE ? E : add2(s.e, hi2(q3));
             const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
             const float2 y = inv_r<REFINE>(ss, dx, dy, dz);
             s.p = fnma2(lo2(q3), y, s.p);
@@ -241,6 +247,7 @@ struct PhiDS {
 template <int IPT_, bool REFINE>
 struct AccJerkDS {
     static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 6;
+    static constexpr bool UE2 = true;
     struct IS { IPos q; float2 u, v, w, e; float2 a[6]; Comp c[6]; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {
         load_pos(a, i, s.q);
@@ -251,15 +258,17 @@ struct AccJerkDS {
         for (int k = 0; k < 6; ++k) { s.a[k] = f2(0.f); s.c[k] = Comp{0.f, 0.f}; }
     }
     // record: {xh,yh} {zh,xl} {yl,zl} {vx,vy} {vz,m} {e2,pad}
-    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R) {
-        const float4 q0 = R[0], q1 = R[1], q2 = R[2], q3 = R[3], q4 = R[4], q5 = R[5];
+    template <bool UE>
+    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R, float2 E) {
+        const float4 q0 = R[0], q1 = R[1], q2 = R[2], q3 = R[3], q4 = R[4];
+        const float4 q5 = UE ? q4 : R[5];
 #pragma unroll
         for (int u = 0; u < IPT; ++u) {
             IS &s = S[u];
             float2 dx, dy, dz;
             pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), dx, dy, dz);
             const float2 du = sub2(s.u, lo2(q3)), dv = sub2(s.v, hi2(q3)), dw = sub2(s.w, lo2(q4));
-            const float2 e2 = add2(s.e, lo2(q5));
+            const float2 e2 = UE ? E : add2(s.e, lo2(q5));
             const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
             float2 y, y2;
             if (REFINE) { y = inv_r<true>(ss, dx, dy, dz); y2 = mul2(y, y); }
@@ -290,6 +299,7 @@ struct AccJerkDS {
 template <int IPT_, bool REFINE>
 struct TstepDS {
     static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 2;
+    static constexpr bool UE2 = false;
     struct IS { IPos q; float2 u, v, w, e, m; float eta; float2 ws; float wmax; Comp c; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {
         load_pos(a, i, s.q);
@@ -344,6 +354,7 @@ struct TstepDS {
 template <int IPT_, bool REFINE>
 struct SnapCrackleDS {
     static constexpr int IPT = IPT_, JF = 18, NQ = 9, NP = 6;
+    static constexpr bool UE2 = false;
     struct IS { IPos q; float2 v[3], A[3], J[3], e; float2 o[6]; Comp c[6]; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {
         load_pos(a, i, s.q);
@@ -411,6 +422,7 @@ struct SnapCrackleDS {
 template <int IPT_, bool REFINE>
 struct PNAccDS {
     static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 3;
+    static constexpr bool UE2 = false;
     struct IS {
         IPos q; float iu, iv, iw; float2 u, v, w, e; float im, iv2; unsigned long order;
         float inv2, inv4, inv5, inv6, inv7; float2 a[3]; Comp c[3];
@@ -481,6 +493,7 @@ struct PNAccDS {
 template <int IPT_, bool REFINE>
 struct AccVjpDS {
     static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 4;
+    static constexpr bool UE2 = false;
     struct IS { IPos q; float2 e, m, g[3]; float2 o[4]; Comp c[4]; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {
         load_pos(a, i, s.q);
@@ -523,6 +536,33 @@ struct AccVjpDS {
     }
     static PackSpec pack() { return PackSpec{12, 6, {F_M, F_E2, F_AX, F_AY, F_AZ, -2}}; }
 };
+
+// One packed step of kernel K over a j-record; UE selects the uniform-
+// softening form for kernels that have it (E = the tile's common ie2 + je2).
+template <class K, bool UE>
+__device__ __forceinline__ void kstep(typename K::IS (&st)[K::IPT], const float4 *R, float2 E) {
+    if constexpr (K::UE2) K::template step<UE>(st, R, E);
+    else K::step(st, R);
+}
+
+// Per j-tile softening: tile_e2[t] = float(e2_j) if every valid j of tile t
+// has the same float value (bit pattern), else NaN.  One CTA per tile.
+__global__ void ds32_tile_e2(const double *e2, size_t nj, float *tile_e2) {
+    __shared__ unsigned first;
+    const size_t j0 = (size_t)blockIdx.x * DS_TILE;
+    if (threadIdx.x == 0) first = __float_as_uint(__double2float_rn(e2[j0]));
+    __syncthreads();
+    bool same = true;
+    for (int q = threadIdx.x; q < DS_TILE; q += blockDim.x) {
+        const size_t j = j0 + q;
+        if (j < nj) same &= __float_as_uint(__double2float_rn(e2[j])) == first;
+    }
+    same = __syncthreads_and(same);
+    if (threadIdx.x == 0) {
+        const float v = __uint_as_float(first);
+        tile_e2[blockIdx.x] = (same && v == v) ? v : __uint_as_float(0x7fc00000u);
+    }
+}
 
 // ---------------------------------------------------------------------------
 // Stream-K geometry helpers.
@@ -580,6 +620,23 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
         const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
         K::load(st[q], a.p, i < a.p.ni ? i : last);
     }
+    // i-tile softening: the common float(ie2) of the tile, or NaN
+    __shared__ unsigned s_ie2;
+    auto tile_ie2 = [&]() -> float {
+        if constexpr (K::UE2) {
+            if (a.tile_e2 == nullptr) return __uint_as_float(0x7fc00000u);
+            if (tid == 0) s_ie2 = __float_as_uint(st[0].e.x);
+            __syncthreads();
+            bool same = true;
+#pragma unroll
+            for (int q = 0; q < IPT; ++q) same &= __float_as_uint(st[q].e.x) == s_ie2;
+            same = __syncthreads_and(same);
+            return same ? __uint_as_float(s_ie2) : __uint_as_float(0x7fc00000u);
+        } else {
+            return __uint_as_float(0x7fc00000u);
+        }
+    };
+    float ie2 = tile_ie2();
     bool aborted = false;
     long long abort_u = u1;                  // first unit whose tile never arrived
     long long issued_to = (u0 + DS_STAGES < u1) ? u0 + DS_STAGES : u1;   // tid 0 only
@@ -594,12 +651,26 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
             break;
         }
         const float4 *R = ring + s * TILE_Q;
+        // uniform softening for this unit: E = ie2 + je2, the value every
+        // pair's own add would give (NaN, i.e. not uniform, propagates)
+        const float ue = __fadd_rn(ie2, a.tile_e2 ? __ldg(a.tile_e2 + u % a.njt) : __uint_as_float(0x7fc00000u));
+        if (K::UE2 && ue == ue) {
+            const float2 E = f2(ue);
 #pragma unroll 1
-        for (int fb = 0; fb < DS_PAIRS; fb += DS_FOLD_PAIRS) {
+            for (int fb = 0; fb < DS_PAIRS; fb += DS_FOLD_PAIRS) {
 #pragma unroll DS_UNROLL
-            for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) K::step(st, R + (fb + pp) * K::NQ);
+                for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, true>(st, R + (fb + pp) * K::NQ, E);
 #pragma unroll
-            for (int q = 0; q < IPT; ++q) K::fold(st[q]);
+                for (int q = 0; q < IPT; ++q) K::fold(st[q]);
+            }
+        } else {
+#pragma unroll 1
+            for (int fb = 0; fb < DS_PAIRS; fb += DS_FOLD_PAIRS) {
+#pragma unroll DS_UNROLL
+                for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, false>(st, R + (fb + pp) * K::NQ, f2(0.f));
+#pragma unroll
+                for (int q = 0; q < IPT; ++q) K::fold(st[q]);
+            }
         }
         __syncthreads();   // stage s fully consumed
         if (tid == 0 && u + DS_STAGES < u1) {
@@ -663,6 +734,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
                 const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
                 K::load(st[q], a.p, i < a.p.ni ? i : last);
             }
+            ie2 = tile_ie2();
         }
     }
 
@@ -803,7 +875,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
 #pragma unroll 1
         for (int fb = 0; fb < DS_PAIRS; fb += DS_FOLD_PAIRS) {
 #pragma unroll DS_UNROLL
-            for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) K::step(st, R + (fb + pp) * K::NQ);
+            for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, false>(st, R + (fb + pp) * K::NQ, f2(0.f));
 #pragma unroll
             for (int q = 0; q < IPT; ++q) K::fold(st[q]);
         }
@@ -891,7 +963,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
 // ---------------------------------------------------------------------------
 struct Geometry {
     long long nit, njt, units, grid;
-    size_t rec_bytes, part_bytes, ticket_bytes;
+    size_t rec_bytes, part_bytes, ticket_bytes, tile_bytes;
 };
 
 template <class K>
@@ -922,31 +994,35 @@ static Geometry geometry(size_t ni, size_t nj, int sms) {
     g.rec_bytes = align_up((size_t)g.njt * DS_PAIRS * K::NQ * sizeof(float4), 256);
     g.part_bytes = align_up((size_t)g.grid * 2 * K::IPT * K::NP * DS_THREADS * sizeof(double), 256);
     g.ticket_bytes = align_up((size_t)g.nit * sizeof(int), 256);
+    g.tile_bytes = K::UE2 ? align_up((size_t)g.njt * sizeof(float), 256) : 0;
     return g;
 }
 
 template <class K>
 static size_t ws_bytes_for(size_t ni, size_t nj, int sms) {
     const Geometry g = geometry<K>(ni, nj, sms);
-    return g.rec_bytes + g.part_bytes + g.ticket_bytes;
+    return g.rec_bytes + g.part_bytes + g.ticket_bytes + g.tile_bytes;
 }
 
 template <class K>
 static cudaError_t run_ds(const PairArgs &p, void *ws, size_t ws_bytes, int sms, cudaStream_t s) {
     const Geometry g = geometry<K>(p.ni, p.nj, sms);
-    if (g.rec_bytes + g.part_bytes + g.ticket_bytes > ws_bytes) return cudaErrorInvalidValue;
+    if (g.rec_bytes + g.part_bytes + g.ticket_bytes + g.tile_bytes > ws_bytes) return cudaErrorInvalidValue;
     char *base = static_cast<char *>(ws);
     DsArgs a;
     a.p = p;
     a.rec = reinterpret_cast<const float4 *>(base);
     a.part = reinterpret_cast<double *>(base + g.rec_bytes);
     a.ticket = reinterpret_cast<int *>(base + g.rec_bytes + g.part_bytes);
+    float *tile_e2 = reinterpret_cast<float *>(base + g.rec_bytes + g.part_bytes + g.ticket_bytes);
+    a.tile_e2 = K::UE2 ? tile_e2 : nullptr;
     a.nit = g.nit;
     a.njt = g.njt;
     const size_t npairs = (size_t)g.njt * DS_PAIRS;
     const PackSpec spec = K::pack();
     const unsigned pack_blocks = (unsigned)((npairs * 2 + 255) / 256);
     ds32_pack<<<pack_blocks, 256, 0, s>>>(p.J, p.nj, npairs, spec, reinterpret_cast<float *>(base));
+    if (K::UE2) ds32_tile_e2<<<(unsigned)g.njt, 256, 0, s>>>(p.J.f[F_E2], p.nj, tile_e2);
     cudaError_t e = cudaMemsetAsync(a.ticket, 0, g.ticket_bytes, s);
     if (e != cudaSuccess) return e;
     const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
@@ -976,6 +1052,7 @@ static cudaError_t run_ds_capped(const PairArgs &p, void *ws, size_t ws_bytes, i
     a.rec = reinterpret_cast<const float4 *>(base);
     a.part = reinterpret_cast<double *>(base + g.rec_bytes);
     a.ticket = reinterpret_cast<int *>(base + g.rec_bytes + g.part_bytes);
+    a.tile_e2 = nullptr;   // general path only: the scratch layout stays fixed
     a.nit = g.nit;
     a.njt = g.njt;
     const size_t npairs = (size_t)g.njt * DS_PAIRS;
