@@ -247,7 +247,9 @@ struct PhiDS {
 template <int IPT_, bool REFINE>
 struct AccJerkDS {
     static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 6;
-    static constexpr bool UE2 = true;
+    // the hoisted-softening form is not used here: at 128 registers the
+    // extra live state spills and cancels the saved add (measured)
+    static constexpr bool UE2 = false;
     struct IS { IPos q; float2 u, v, w, e; float2 a[6]; Comp c[6]; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {
         load_pos(a, i, s.q);
@@ -256,6 +258,9 @@ struct AccJerkDS {
         s.w = f2(__double2float_rn(a.I.f[F_VZ][i]));
         s.e = f2(__double2float_rn(a.I.f[F_E2][i]));
         for (int k = 0; k < 6; ++k) { s.a[k] = f2(0.f); s.c[k] = Comp{0.f, 0.f}; }
+    }
+    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R) {
+        step<false>(S, R, f2(0.f));
     }
     // record: {xh,yh} {zh,xl} {yl,zl} {vx,vy} {vz,m} {e2,pad}
     template <bool UE>
