@@ -65,6 +65,12 @@ struct DsArgs {
     int *ticket;         // [NIT]
     const float *tile_e2;  // [NJT] common j softening per tile or NaN; may be null
     long long nit, njt;  // i-tiles, j-tiles
+    // A unit is (i-tile, part of a j-tile): small problems split each j-tile
+    // into jsub parts (1, 2, 4 or 8) so that the units outnumber the CTAs.
+    int jsub;
+    long long nju;       // units per i-tile = njt * jsub
+    int part_pairs;      // j-records per part (a whole number of fold blocks)
+    int part_q;          // float4 per part
 };
 
 __device__ __forceinline__ float fzero_norm(float x) { return x + 0.0f; }  // -0 -> +0
@@ -593,10 +599,10 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
     __shared__ int s_last;
     constexpr int IPT = K::IPT;
     constexpr int TILE_Q = DS_PAIRS * K::NQ;
-    constexpr unsigned TILE_BYTES = TILE_Q * sizeof(float4);
     constexpr int BI = DS_THREADS * IPT;   // i-particles per i-tile
+    const long long nju = a.nju;
 
-    const long long U = a.nit * a.njt;
+    const long long U = a.nit * nju;
     const long long G = gridDim.x;
     const long long k = blockIdx.x;
     const long long u0 = unit_start(k, U, G), u1 = unit_start(k + 1, U, G);
@@ -609,16 +615,17 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
     }
     __syncthreads();
     auto issue = [&](long long u, int s) {
-        const long long jt = u % a.njt;
-        mbar_expect_tx(&full[s], TILE_BYTES);
-        bulk_g2s(ring + s * TILE_Q, a.rec + jt * TILE_Q, TILE_BYTES, &full[s]);
+        const long long jp = u % a.nju;     // part jp % jsub of j-tile jp / jsub
+        const unsigned bytes = (unsigned)(a.part_q * sizeof(float4));
+        mbar_expect_tx(&full[s], bytes);
+        bulk_g2s(ring + s * TILE_Q, a.rec + jp * a.part_q, bytes, &full[s]);
     };
     if (tid == 0) {
         for (int s = 0; s < DS_STAGES && u0 + s < u1; ++s) issue(u0 + s, s);
     }
 
     const size_t last = a.p.ni - 1;
-    long long t = u0 / a.njt;
+    long long t = u0 / nju;
     typename K::IS st[IPT];
 #pragma unroll
     for (int q = 0; q < IPT; ++q) {
@@ -658,11 +665,14 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
         const float4 *R = ring + s * TILE_Q;
         // uniform softening for this unit: E = ie2 + je2, the value every
         // pair's own add would give (NaN, i.e. not uniform, propagates)
-        const float ue = __fadd_rn(ie2, a.tile_e2 ? __ldg(a.tile_e2 + u % a.njt) : __uint_as_float(0x7fc00000u));
+        float ue = __uint_as_float(0x7fc00000u);
+        if constexpr (K::UE2)
+            if (a.tile_e2) ue = __fadd_rn(ie2, __ldg(a.tile_e2 + (u % nju) / a.jsub));
         if (K::UE2 && ue == ue) {
             const float2 E = f2(ue);
 #pragma unroll 1
             for (int fb = 0; fb < DS_PAIRS; fb += DS_FOLD_PAIRS) {
+                if (fb >= a.part_pairs) break;
 #pragma unroll DS_UNROLL
                 for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, true>(st, R + (fb + pp) * K::NQ, E);
 #pragma unroll
@@ -671,6 +681,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
         } else {
 #pragma unroll 1
             for (int fb = 0; fb < DS_PAIRS; fb += DS_FOLD_PAIRS) {
+                if (fb >= a.part_pairs) break;
 #pragma unroll DS_UNROLL
                 for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, false>(st, R + (fb + pp) * K::NQ, f2(0.f));
 #pragma unroll
@@ -682,11 +693,11 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
             issue(u + DS_STAGES, s);
             issued_to = u + DS_STAGES + 1;
         }
-        const long long tn = (u + 1 < u1) ? (u + 1) / a.njt : -1;
+        const long long tn = (u + 1 < u1) ? (u + 1) / nju : -1;
         if (tn == t) continue;
 
         // ---- i-tile t is done for this CTA: store or hand over partials ----
-        const long long ta = t * a.njt, tb = ta + a.njt;
+        const long long ta = t * nju, tb = ta + nju;
         if (ta >= u0 && tb <= u1) {
 #pragma unroll
             for (int q = 0; q < IPT; ++q) {
@@ -696,7 +707,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
                 if (i < a.p.ni) K::store(p, a.p, i);
             }
         } else {
-            const int slot = (t == u0 / a.njt) ? 0 : 1;
+            const int slot = (t == u0 / nju) ? 0 : 1;
             double *mine = a.part + ((k * 2 + slot) * IPT * K::NP) * DS_THREADS;
 #pragma unroll
             for (int q = 0; q < IPT; ++q) {
@@ -717,7 +728,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
                 for (int q = 0; q < IPT; ++q) {
                     double acc[K::NP];
                     for (long long kk = klo; kk <= khi; ++kk) {
-                        const int sl = (t == unit_start(kk, U, G) / a.njt) ? 0 : 1;
+                        const int sl = (t == unit_start(kk, U, G) / nju) ? 0 : 1;
                         const double *src = a.part + ((kk * 2 + sl) * IPT * K::NP) * DS_THREADS;
                         double v[K::NP];
                         for (int w = 0; w < K::NP; ++w) v[w] = __ldcg(src + (q * K::NP + w) * DS_THREADS + tid);
@@ -968,6 +979,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
 // ---------------------------------------------------------------------------
 struct Geometry {
     long long nit, njt, units, grid;
+    int jsub;
     size_t rec_bytes, part_bytes, ticket_bytes, tile_bytes;
 };
 
@@ -993,8 +1005,11 @@ static Geometry geometry(size_t ni, size_t nj, int sms) {
     const size_t bi = (size_t)DS_THREADS * K::IPT;
     g.nit = (long long)((ni + bi - 1) / bi);
     g.njt = (long long)((nj + DS_TILE - 1) / DS_TILE);
-    g.units = g.nit * g.njt;
     const long long slots = (long long)sms * ctas_per_sm<K>();
+    // split j-tiles until there are at least two units per CTA slot
+    g.jsub = 1;
+    while (g.jsub < DS_PAIRS / DS_FOLD_PAIRS && g.jsub < 8 && g.nit * g.njt * g.jsub < 2 * slots) g.jsub *= 2;
+    g.units = g.nit * g.njt * g.jsub;
     g.grid = g.units < slots ? g.units : slots;
     g.rec_bytes = align_up((size_t)g.njt * DS_PAIRS * K::NQ * sizeof(float4), 256);
     g.part_bytes = align_up((size_t)g.grid * 2 * K::IPT * K::NP * DS_THREADS * sizeof(double), 256);
@@ -1023,6 +1038,10 @@ static cudaError_t run_ds(const PairArgs &p, void *ws, size_t ws_bytes, int sms,
     a.tile_e2 = K::UE2 ? tile_e2 : nullptr;
     a.nit = g.nit;
     a.njt = g.njt;
+    a.jsub = g.jsub;
+    a.nju = g.njt * g.jsub;
+    a.part_pairs = DS_PAIRS / g.jsub;
+    a.part_q = a.part_pairs * K::NQ;
     const size_t npairs = (size_t)g.njt * DS_PAIRS;
     const PackSpec spec = K::pack();
     const unsigned pack_blocks = (unsigned)((npairs * 2 + 255) / 256);
@@ -1060,6 +1079,10 @@ static cudaError_t run_ds_capped(const PairArgs &p, void *ws, size_t ws_bytes, i
     a.tile_e2 = nullptr;   // general path only: the scratch layout stays fixed
     a.nit = g.nit;
     a.njt = g.njt;
+    a.jsub = g.jsub;
+    a.nju = g.njt * g.jsub;
+    a.part_pairs = DS_PAIRS / g.jsub;
+    a.part_q = a.part_pairs * K::NQ;
     const size_t npairs = (size_t)g.njt * DS_PAIRS;
     const PackSpec spec = K::pack();
     const unsigned pack_blocks = (unsigned)((npairs * 2 + 255) / 256);
