@@ -724,22 +724,41 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
             }
             __syncthreads();
             if (s_last) {
+                // Sum the contributors' partials in CTA order (deterministic);
+                // two contributors' loads are in flight per step.
                 __threadfence();
-                for (int q = 0; q < IPT; ++q) {
-                    double acc[K::NP];
-                    for (long long kk = klo; kk <= khi; ++kk) {
-                        const int sl = (t == unit_start(kk, U, G) / nju) ? 0 : 1;
-                        const double *src = a.part + ((kk * 2 + sl) * IPT * K::NP) * DS_THREADS;
-                        double v[K::NP];
-                        for (int w = 0; w < K::NP; ++w) v[w] = __ldcg(src + (q * K::NP + w) * DS_THREADS + tid);
-                        if (kk == klo) {
-                            for (int w = 0; w < K::NP; ++w) acc[w] = v[w];
-                        } else {
-                            K::combine(acc, v);
+                auto slot_ptr = [&](long long kk) {
+                    const int sl = (t == unit_start(kk, U, G) / nju) ? 0 : 1;
+                    return a.part + ((kk * 2 + sl) * IPT * K::NP) * DS_THREADS + tid;
+                };
+                double acc[IPT][K::NP];
+                {
+                    const double *s0 = slot_ptr(klo);
+#pragma unroll
+                    for (int q = 0; q < IPT; ++q)
+#pragma unroll
+                        for (int w = 0; w < K::NP; ++w) acc[q][w] = __ldcg(s0 + (q * K::NP + w) * DS_THREADS);
+                }
+                for (long long kk = klo + 1; kk <= khi; kk += 2) {
+                    const bool two = kk + 1 <= khi;
+                    const double *s0 = slot_ptr(kk);
+                    const double *s1 = two ? slot_ptr(kk + 1) : s0;
+#pragma unroll
+                    for (int q = 0; q < IPT; ++q) {
+                        double v0[K::NP], v1[K::NP];
+#pragma unroll
+                        for (int w = 0; w < K::NP; ++w) {
+                            v0[w] = __ldcg(s0 + (q * K::NP + w) * DS_THREADS);
+                            v1[w] = __ldcg(s1 + (q * K::NP + w) * DS_THREADS);
                         }
+                        K::combine(acc[q], v0);
+                        if (two) K::combine(acc[q], v1);
                     }
+                }
+#pragma unroll
+                for (int q = 0; q < IPT; ++q) {
                     const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
-                    if (i < a.p.ni) K::store(acc, a.p, i);
+                    if (i < a.p.ni) K::store(acc[q], a.p, i);
                 }
             }
         }
@@ -977,6 +996,9 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
 // ---------------------------------------------------------------------------
 // Host side.
 // ---------------------------------------------------------------------------
+#ifndef TG_DS32_MAX_JSUB
+#define TG_DS32_MAX_JSUB 8   // most parts a j-tile is split into
+#endif
 struct Geometry {
     long long nit, njt, units, grid;
     int jsub;
@@ -1008,7 +1030,8 @@ static Geometry geometry(size_t ni, size_t nj, int sms) {
     const long long slots = (long long)sms * ctas_per_sm<K>();
     // split j-tiles until there are at least two units per CTA slot
     g.jsub = 1;
-    while (g.jsub < DS_PAIRS / DS_FOLD_PAIRS && g.jsub < 8 && g.nit * g.njt * g.jsub < 2 * slots) g.jsub *= 2;
+    while (g.jsub < DS_PAIRS / DS_FOLD_PAIRS && g.jsub < TG_DS32_MAX_JSUB && g.nit * g.njt * g.jsub < 2 * slots)
+        g.jsub *= 2;
     g.units = g.nit * g.njt * g.jsub;
     g.grid = g.units < slots ? g.units : slots;
     g.rec_bytes = align_up((size_t)g.njt * DS_PAIRS * K::NQ * sizeof(float4), 256);

@@ -12,6 +12,8 @@
 // Roofline: FP64 issue.  GB300 executes FP64 at a small fraction of the FP32
 // rate and each pair needs one IEEE divide and one square root, so these
 // kernels are the accuracy reference on the GPU, not the fast path.
+#include <type_traits>
+
 #include "tg_device.cuh"
 #include "tg_internal.h"
 #include "tg_kepler.cuh"
@@ -32,51 +34,53 @@ __device__ __forceinline__ double soft_q2(double r2, double e2) {
 // Per-kernel pair functors.  `sj[f][jj]` is the staged j-tile.
 // ---------------------------------------------------------------------------
 struct Phi64 {
-    static constexpr int NF = 5, NO = 1;
-    struct St { double x, y, z, e, phi; };
+    static constexpr int NF = 5, NO = 1, NT = 1;
+    struct St { double x, y, z, e, acc[NT]; };
     __device__ static void init(St &s, const PairArgs &a, size_t i) {
-        s = {a.I.f[F_RX][i], a.I.f[F_RY][i], a.I.f[F_RZ][i], a.I.f[F_E2][i], 0.0};
+        s = {a.I.f[F_RX][i], a.I.f[F_RY][i], a.I.f[F_RZ][i], a.I.f[F_E2][i], {0.0}};
     }
-    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &) {
+    __device__ static void terms(const St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &, double *t) {
         double dx = dsub(s.x, sj[F_RX][jj]), dy = dsub(s.y, sj[F_RY][jj]), dz = dsub(s.z, sj[F_RZ][jj]);
         double e2 = dadd(s.e, sj[F_E2][jj]);
         double r2 = ddot3(dx, dy, dz, dx, dy, dz);
         double q1 = dsqrt(soft_q2(r2, e2));
-        s.phi = dsub(s.phi, dmul(sj[F_M][jj], q1));
+        t[0] = dmul(sj[F_M][jj], q1);
     }
-    __device__ static void store(const St &s, const PairArgs &a, size_t i) { a.out[0][i] = s.phi; }
+    __device__ static double accum(int, double acc, double t) { return dsub(acc, t); }
+    __device__ static void store_acc(const double *acc, const St &, const PairArgs &a, size_t i) { a.out[0][i] = acc[0]; }
 };
 
 struct Acc64 {
-    static constexpr int NF = 5, NO = 3;
-    struct St { double x, y, z, e, ax, ay, az; };
+    static constexpr int NF = 5, NO = 3, NT = 3;
+    struct St { double x, y, z, e, acc[NT]; };
     __device__ static void init(St &s, const PairArgs &a, size_t i) {
-        s = {a.I.f[F_RX][i], a.I.f[F_RY][i], a.I.f[F_RZ][i], a.I.f[F_E2][i], 0.0, 0.0, 0.0};
+        s = {a.I.f[F_RX][i], a.I.f[F_RY][i], a.I.f[F_RZ][i], a.I.f[F_E2][i], {0.0, 0.0, 0.0}};
     }
-    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &) {
+    __device__ static void terms(const St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &, double *t) {
         double dx = dsub(s.x, sj[F_RX][jj]), dy = dsub(s.y, sj[F_RY][jj]), dz = dsub(s.z, sj[F_RZ][jj]);
         double e2 = dadd(s.e, sj[F_E2][jj]);
         double r2 = ddot3(dx, dy, dz, dx, dy, dz);
         double q2 = soft_q2(r2, e2);
         double q3 = dmul(dmul(q2, dsqrt(q2)), sj[F_M][jj]);
-        s.ax = dsub(s.ax, dmul(q3, dx));
-        s.ay = dsub(s.ay, dmul(q3, dy));
-        s.az = dsub(s.az, dmul(q3, dz));
+        t[0] = dmul(q3, dx);
+        t[1] = dmul(q3, dy);
+        t[2] = dmul(q3, dz);
     }
-    __device__ static void store(const St &s, const PairArgs &a, size_t i) {
-        a.out[0][i] = s.ax; a.out[1][i] = s.ay; a.out[2][i] = s.az;
+    __device__ static double accum(int, double acc, double t) { return dsub(acc, t); }
+    __device__ static void store_acc(const double *acc, const St &, const PairArgs &a, size_t i) {
+        a.out[0][i] = acc[0]; a.out[1][i] = acc[1]; a.out[2][i] = acc[2];
     }
 };
 
 struct AccJerk64 {
-    static constexpr int NF = 8, NO = 6;
-    struct St { double x, y, z, e, u, v, w, a[3], j[3]; };
+    static constexpr int NF = 8, NO = 6, NT = 6;
+    struct St { double x, y, z, e, u, v, w, acc[NT]; };
     __device__ static void init(St &s, const PairArgs &a, size_t i) {
         s.x = a.I.f[F_RX][i]; s.y = a.I.f[F_RY][i]; s.z = a.I.f[F_RZ][i]; s.e = a.I.f[F_E2][i];
         s.u = a.I.f[F_VX][i]; s.v = a.I.f[F_VY][i]; s.w = a.I.f[F_VZ][i];
-        for (int k = 0; k < 3; ++k) { s.a[k] = 0.0; s.j[k] = 0.0; }
+        for (int k = 0; k < NT; ++k) s.acc[k] = 0.0;
     }
-    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &) {
+    __device__ static void terms(const St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &, double *t) {
         double dx = dsub(s.x, sj[F_RX][jj]), dy = dsub(s.y, sj[F_RY][jj]), dz = dsub(s.z, sj[F_RZ][jj]);
         double e2 = dadd(s.e, sj[F_E2][jj]);
         double du = dsub(s.u, sj[F_VX][jj]), dv = dsub(s.v, sj[F_VY][jj]), dw = dsub(s.w, sj[F_VZ][jj]);
@@ -89,22 +93,23 @@ struct AccJerk64 {
         dv = dsub(dv, dmul(al, dy));
         dw = dsub(dw, dmul(al, dz));
         q3 = dmul(q3, sj[F_M][jj]);
-        s.a[0] = dsub(s.a[0], dmul(q3, dx)); s.a[1] = dsub(s.a[1], dmul(q3, dy)); s.a[2] = dsub(s.a[2], dmul(q3, dz));
-        s.j[0] = dsub(s.j[0], dmul(q3, du)); s.j[1] = dsub(s.j[1], dmul(q3, dv)); s.j[2] = dsub(s.j[2], dmul(q3, dw));
+        t[0] = dmul(q3, dx); t[1] = dmul(q3, dy); t[2] = dmul(q3, dz);
+        t[3] = dmul(q3, du); t[4] = dmul(q3, dv); t[5] = dmul(q3, dw);
     }
-    __device__ static void store(const St &s, const PairArgs &a, size_t i) {
-        for (int k = 0; k < 3; ++k) { a.out[k][i] = s.a[k]; a.out[3 + k][i] = s.j[k]; }
+    __device__ static double accum(int, double acc, double t) { return dsub(acc, t); }
+    __device__ static void store_acc(const double *acc, const St &, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 6; ++k) a.out[k][i] = acc[k];
     }
 };
 
 struct SnapCrackle64 {
-    static constexpr int NF = 14, NO = 6;
-    struct St { double f[14]; double s[3], c[3]; };
+    static constexpr int NF = 14, NO = 6, NT = 6;
+    struct St { double f[14]; double acc[NT]; };
     __device__ static void init(St &s, const PairArgs &a, size_t i) {
         for (int k = 0; k < 14; ++k) s.f[k] = a.I.f[k][i];
-        for (int k = 0; k < 3; ++k) { s.s[k] = 0.0; s.c[k] = 0.0; }
+        for (int k = 0; k < NT; ++k) s.acc[k] = 0.0;
     }
-    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &) {
+    __device__ static void terms(const St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &, double *t) {
         double r[3], v[3], A[3], J[3];
         for (int k = 0; k < 3; ++k) {
             r[k] = dsub(s.f[F_RX + k], sj[F_RX + k][jj]);
@@ -136,24 +141,25 @@ struct SnapCrackle64 {
             J[k] = dsub(J[k], dadd(dadd(dmul(al, A[k]), dmul(be, v[k])), dmul(ga, r[k])));
         q3 = dmul(q3, sj[F_M][jj]);
         for (int k = 0; k < 3; ++k) {
-            s.s[k] = dsub(s.s[k], dmul(q3, A[k]));
-            s.c[k] = dsub(s.c[k], dmul(q3, J[k]));
+            t[k] = dmul(q3, A[k]);
+            t[3 + k] = dmul(q3, J[k]);
         }
     }
-    __device__ static void store(const St &s, const PairArgs &a, size_t i) {
-        for (int k = 0; k < 3; ++k) { a.out[k][i] = s.s[k]; a.out[3 + k][i] = s.c[k]; }
+    __device__ static double accum(int, double acc, double t) { return dsub(acc, t); }
+    __device__ static void store_acc(const double *acc, const St &, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 6; ++k) a.out[k][i] = acc[k];
     }
 };
 
 struct Tstep64 {
-    static constexpr int NF = 8, NO = 2;
-    struct St { double m, x, y, z, e, u, v, w, wsum, wmax; };
+    static constexpr int NF = 8, NO = 2, NT = 2;
+    struct St { double m, x, y, z, e, u, v, w, acc[NT]; };   // acc: sum w2, max w2
     __device__ static void init(St &s, const PairArgs &a, size_t i) {
         s.m = a.I.f[F_M][i]; s.x = a.I.f[F_RX][i]; s.y = a.I.f[F_RY][i]; s.z = a.I.f[F_RZ][i];
         s.e = a.I.f[F_E2][i]; s.u = a.I.f[F_VX][i]; s.v = a.I.f[F_VY][i]; s.w = a.I.f[F_VZ][i];
-        s.wsum = 0.0; s.wmax = 0.0;
+        s.acc[0] = 0.0; s.acc[1] = 0.0;
     }
-    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a) {
+    __device__ static void terms(const St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a, double *t) {
         double dx = dsub(s.x, sj[F_RX][jj]), dy = dsub(s.y, sj[F_RY][jj]), dz = dsub(s.z, sj[F_RZ][jj]);
         double e2 = dadd(s.e, sj[F_E2][jj]);
         double du = dsub(s.u, sj[F_VX][jj]), dv = dsub(s.v, sj[F_VY][jj]), dw = dsub(s.w, sj[F_VZ][jj]);
@@ -170,12 +176,13 @@ struct Tstep64 {
         gam = dmul(gam, ddiv(a.eta, dsqrt(w2)));
         w2 = dsub(w2, dmul(gam, rv));
         if (!(r2 > 0)) w2 = 0.0;
-        s.wsum = dadd(s.wsum, w2);
-        s.wmax = fmax(w2, s.wmax);
+        t[0] = w2;
+        t[1] = w2;
     }
-    __device__ static void store(const St &s, const PairArgs &a, size_t i) {
-        a.out[0][i] = ddiv(a.eta, dsqrt(dadd(1.0, s.wsum)));
-        a.out[1][i] = ddiv(a.eta, dsqrt(dadd(1.0, s.wmax)));
+    __device__ static double accum(int c, double acc, double t) { return c == 0 ? dadd(acc, t) : fmax(t, acc); }
+    __device__ static void store_acc(const double *acc, const St &, const PairArgs &a, size_t i) {
+        a.out[0][i] = ddiv(a.eta, dsqrt(dadd(1.0, acc[0])));
+        a.out[1][i] = ddiv(a.eta, dsqrt(dadd(1.0, acc[1])));
     }
 };
 
@@ -403,6 +410,32 @@ cudaError_t launch_kepler_pairs(size_t npairs, const PSet &in, double dt, double
     return cudaGetLastError();
 }
 
+// Functors written as per-pair terms plus an ordered accumulation (Phi, Acc,
+// AccJerk, SnapCrackle, Tstep): pair() and store() for the sequential
+// engines are the terms folded into the accumulators one pair at a time,
+// the same operations in the same order as the reference loop.
+template <class K, class = void>
+struct has_terms : std::false_type {};
+template <class K>
+struct has_terms<K, decltype(void(K::NT))> : std::true_type {};
+
+template <class K>
+struct Seq : K {
+    __device__ static void pair(typename K::St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a) {
+        double t[K::NT];
+        K::terms(s, sj, jj, a, t);
+#pragma unroll
+        for (int c = 0; c < K::NT; ++c) s.acc[c] = K::accum(c, s.acc[c], t[c]);
+    }
+    __device__ static void store(const typename K::St &s, const PairArgs &a, size_t i) {
+        K::store_acc(s.acc, s, a, i);
+    }
+};
+template <class K, bool T = has_terms<K>::value>
+struct SeqOf { using type = K; };
+template <class K>
+struct SeqOf<K, true> { using type = Seq<K>; };
+
 // ---------------------------------------------------------------------------
 // Generic sequential-j engine.
 // ---------------------------------------------------------------------------
@@ -470,10 +503,11 @@ __global__ void __launch_bounds__(F64_THREADS) fp64_pairwise_seg(PairArgs a, con
     if (live) K::store(st, a, (size_t)(s0 + li));
 }
 
-template <class K>
+template <class K0>
 static cudaError_t run_seg(const PairArgs &a, long long C, long long nblocks, int threads,
                            const long long *block_off, const long long *seg_start, const long long *seg_n,
                            cudaStream_t s) {
+    using K = typename SeqOf<K0>::type;
     if (nblocks == 0) return cudaSuccess;
     fp64_pairwise_seg<K><<<(unsigned)nblocks, threads, 0, s>>>(a, block_off, seg_start, seg_n, C);
     return cudaGetLastError();
@@ -491,8 +525,85 @@ cudaError_t launch_fp64_seg(int kernel, const PairArgs &a, long long C, long lon
     }
 }
 
+// ---------------------------------------------------------------------------
+// Warp engine for small i-sets: IPW i-particles per warp, 32/IPW lanes per
+// i.  In each round the lanes of an i-group compute the terms of 32/IPW
+// consecutive j in parallel (the divide and square root dominate), write
+// them to shared memory, and lane c of the group folds component c of the
+// round's terms into its accumulator in j order -- the reference's
+// sequence of operations, so results stay bit-identical, while the grid
+// has 32/IPW times more threads than the thread-per-i engine.
+// ---------------------------------------------------------------------------
+constexpr int F64W_THREADS = 256;
+
+template <class K, int IPW>
+__global__ void __launch_bounds__(F64W_THREADS) fp64_warp(PairArgs a) {
+    constexpr int LPI = 32 / IPW;
+    constexpr int WARPS = F64W_THREADS / 32;
+    static_assert(K::NT <= LPI, "one lane per accumulated component");
+    __shared__ double sj[K::NF][F64_TILE];
+    __shared__ double tt[WARPS][IPW][K::NT][LPI + 1];
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int g = lane / LPI, l = lane % LPI;
+    const size_t i = ((size_t)blockIdx.x * WARPS + warp) * IPW + g;
+    const bool live = i < a.ni;
+    typename K::St st;
+    K::init(st, a, live ? i : 0);
+    double acc = 0.0;   // every accumulator of these kernels starts at 0
+    for (size_t j0 = 0; j0 < a.nj; j0 += F64_TILE) {
+        const int nt = (int)((a.nj - j0) < (size_t)F64_TILE ? (a.nj - j0) : F64_TILE);
+        for (int q = threadIdx.x; q < K::NF * F64_TILE; q += blockDim.x) {
+            const int f = q / F64_TILE, jj = q % F64_TILE;
+            if (jj < nt) sj[f][jj] = a.J.f[f][j0 + jj];
+        }
+        __syncthreads();
+        for (int r = 0; r < nt; r += LPI) {
+            if (r + l < nt) {
+                double t[K::NT];
+                K::terms(st, sj, r + l, a, t);
+#pragma unroll
+                for (int c = 0; c < K::NT; ++c) tt[warp][g][c][l] = t[c];
+            }
+            __syncwarp();
+            const int m = (nt - r) < LPI ? (nt - r) : LPI;
+            if (l < K::NT)
+                for (int q = 0; q < m; ++q) acc = K::accum(l, acc, tt[warp][g][l][q]);
+            __syncwarp();
+        }
+        __syncthreads();
+    }
+    double res[K::NT];
+#pragma unroll
+    for (int c = 0; c < K::NT; ++c) res[c] = __shfl_sync(0xffffffffu, acc, g * LPI + c);
+    if (l == 0 && live) K::store_acc(res, st, a, i);
+}
+
+// i-sets below this size use the warp engine (the thread-per-i engine has
+// fewer than ~14 warps per SM there, too few to keep the FP64 pipe busy).
+constexpr size_t F64W_MAX_NI = 32768;
+
 template <class K>
+static cudaError_t run_warp(const PairArgs &a, int sms, cudaStream_t s) {
+    constexpr int WARPS = F64W_THREADS / 32;
+    // fewest i per warp that still gives ~16 warps per SM
+    const size_t want = (size_t)16 * (sms > 0 ? sms : 1);
+    int ipw = 1;
+    if (K::NT <= 16 && a.ni / 2 >= want) ipw = 2;
+    if (K::NT <= 8 && a.ni / 4 >= want) ipw = 4;
+    const size_t warps = (a.ni + ipw - 1) / ipw;
+    const unsigned blocks = (unsigned)((warps + WARPS - 1) / WARPS);
+    if (ipw == 4) fp64_warp<K, 4><<<blocks, F64W_THREADS, 0, s>>>(a);
+    else if (ipw == 2) fp64_warp<K, 2><<<blocks, F64W_THREADS, 0, s>>>(a);
+    else fp64_warp<K, 1><<<blocks, F64W_THREADS, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <class K0>
 static cudaError_t run(const PairArgs &a, int sms, cudaStream_t s) {
+    if constexpr (has_terms<K0>::value) {
+        if (a.ni <= F64W_MAX_NI) return run_warp<K0>(a, sms, s);
+    }
+    using K = typename SeqOf<K0>::type;
     const unsigned t = fp64_threads(a.ni, sms);
     const size_t blocks = (a.ni + t - 1) / t;
     fp64_pairwise<K><<<(unsigned)blocks, t, 0, s>>>(a);
