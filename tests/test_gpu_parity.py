@@ -204,6 +204,21 @@ def test_uniform_softening_path_is_bit_identical(ext, n):
         assert np.array_equal(uniform[:, 1:], general[:, 1:]), name
 
 
+def test_fp64_engines_bit_identical_to_oracle(ext, orc):
+    """i-sets up to 32768 particles run on the warp engine (lane-parallel
+    pair terms folded in j order), larger ones on the thread-per-i engine;
+    both must reproduce the reference loop bit for bit."""
+    d = plummer(40000, seed=21)
+    for ni in (40000, 20000):
+        I = {f: d[f][:ni] for f in FIELDS}
+        J = {f: d[f][-257:] for f in FIELDS}
+        for name, sc in [("acc", ()), ("acc_jerk", ()), ("phi", ()), ("tstep", (0.01,)),
+                         ("snap_crackle", ())]:
+            want = np.stack(orc.calc(name, I, J, *sc, nthreads=8))
+            got = run_kernel(ext, name, "float64", PS(I), PS(J), sc)
+            assert np.array_equal(got, want), (name, ni)
+
+
 def test_ds32_is_deterministic(ext):
     d = plummer(6000, seed=3)
     P = PS(d)

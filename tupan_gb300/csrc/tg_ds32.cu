@@ -956,24 +956,42 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
             }
             __syncthreads();
             if (s_last) {
+                // contributors summed in CTA order; two in flight per step
                 __threadfence();
-                for (int q = 0; q < IPT; ++q) {
-                    double acc[K::NP];
-                    for (long long kk = klo; kk <= khi; ++kk) {
-                        const long long us = unit_start(kk, U, G);
-                        const long long ck = seg_find(a.unit_off, a.C, us);
-                        const int sl = (git == a.itile_off[ck] + tile_of(ck, us)) ? 0 : 1;
-                        const double *src = a.part + ((kk * 2 + sl) * IPT * K::NP) * DS_THREADS;
-                        double v[K::NP];
-                        for (int w = 0; w < K::NP; ++w) v[w] = __ldcg(src + (q * K::NP + w) * DS_THREADS + tid);
-                        if (kk == klo) {
-                            for (int w = 0; w < K::NP; ++w) acc[w] = v[w];
-                        } else {
-                            K::combine(acc, v);
+                auto slot_ptr = [&](long long kk) {
+                    const long long us = unit_start(kk, U, G);
+                    const long long ck = seg_find(a.unit_off, a.C, us);
+                    const int sl = (git == a.itile_off[ck] + tile_of(ck, us)) ? 0 : 1;
+                    return a.part + ((kk * 2 + sl) * IPT * K::NP) * DS_THREADS + tid;
+                };
+                double acc[IPT][K::NP];
+                {
+                    const double *s0 = slot_ptr(klo);
+#pragma unroll
+                    for (int q = 0; q < IPT; ++q)
+#pragma unroll
+                        for (int w = 0; w < K::NP; ++w) acc[q][w] = __ldcg(s0 + (q * K::NP + w) * DS_THREADS);
+                }
+                for (long long kk = klo + 1; kk <= khi; kk += 2) {
+                    const bool two = kk + 1 <= khi;
+                    const double *s0 = slot_ptr(kk);
+                    const double *s1 = two ? slot_ptr(kk + 1) : s0;
+#pragma unroll
+                    for (int q = 0; q < IPT; ++q) {
+                        double v0[K::NP], v1[K::NP];
+#pragma unroll
+                        for (int w = 0; w < K::NP; ++w) {
+                            v0[w] = __ldcg(s0 + (q * K::NP + w) * DS_THREADS);
+                            v1[w] = __ldcg(s1 + (q * K::NP + w) * DS_THREADS);
                         }
+                        K::combine(acc[q], v0);
+                        if (two) K::combine(acc[q], v1);
                     }
+                }
+#pragma unroll
+                for (int q = 0; q < IPT; ++q) {
                     const long long li = t * BI + q * DS_THREADS + tid;
-                    if (li < a.seg_n[c]) K::store(acc, a.p, (size_t)(a.seg_start[c] + li));
+                    if (li < a.seg_n[c]) K::store(acc[q], a.p, (size_t)(a.seg_start[c] + li));
                 }
             }
         }
