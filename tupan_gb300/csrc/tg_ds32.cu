@@ -26,6 +26,8 @@
 // instruction (FADD2/FMUL2/FFMA2); 1/sqrt is MUFU.RSQ plus one Newton step;
 // per-thread sums run in FP32 over 64 j and are then folded into Kahan-
 // compensated accumulators.  The roofline is the FP32 pipe (FFMA2 issue).
+#include <type_traits>
+
 #include "tg_device.cuh"
 #include "tg_internal.h"
 #include "tg_pn_terms.cuh"
@@ -253,17 +255,19 @@ struct PhiDS {
 template <int IPT_, bool REFINE>
 struct AccJerkDS {
     static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 6;
-    // the hoisted-softening form is not used here: at 128 registers the
-    // extra live state spills and cancels the saved add (measured)
-    static constexpr bool UE2 = false;
-    struct IS { IPos q; float2 u, v, w, e; float2 a[6]; Comp c[6]; };
+    static constexpr bool UE2 = true;
+    // The compensated sums live in shared memory (touched once per fold
+    // block), which keeps the registers below the limit with the
+    // hoisted-softening form.
+    static constexpr bool SMEM_COMP = true;
+    struct IS { IPos q; float2 u, v, w, e; float2 a[6]; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {
         load_pos(a, i, s.q);
         s.u = f2(__double2float_rn(a.I.f[F_VX][i]));
         s.v = f2(__double2float_rn(a.I.f[F_VY][i]));
         s.w = f2(__double2float_rn(a.I.f[F_VZ][i]));
         s.e = f2(__double2float_rn(a.I.f[F_E2][i]));
-        for (int k = 0; k < 6; ++k) { s.a[k] = f2(0.f); s.c[k] = Comp{0.f, 0.f}; }
+        for (int k = 0; k < 6; ++k) s.a[k] = f2(0.f);
     }
     __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R) {
         step<false>(S, R, f2(0.f));
@@ -296,10 +300,19 @@ struct AccJerkDS {
             s.a[5] = fnma2(mr3, tw, s.a[5]);
         }
     }
-    __device__ static void fold(IS &s) {
-        for (int k = 0; k < 6; ++k) { comp_add(s.c[k], __fadd_rn(s.a[k].x, s.a[k].y)); s.a[k] = f2(0.f); }
+    // c[k * DS_THREADS]: this thread's compensated sum k in shared memory
+    __device__ static void fold(IS &s, Comp *c) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            Comp v = c[k * DS_THREADS];
+            comp_add(v, __fadd_rn(s.a[k].x, s.a[k].y));
+            c[k * DS_THREADS] = v;
+            s.a[k] = f2(0.f);
+        }
     }
-    __device__ static void partials(const IS &s, double *p) { for (int k = 0; k < 6; ++k) p[k] = comp_value(s.c[k]); }
+    __device__ static void partials(const IS &, const Comp *c, double *p) {
+        for (int k = 0; k < 6; ++k) p[k] = comp_value(c[k * DS_THREADS]);
+    }
     __device__ static void combine(double *acc, const double *p) { for (int k = 0; k < 6; ++k) acc[k] += p[k]; }
     __device__ static void store(const double *p, const PairArgs &a, size_t i) {
         for (int k = 0; k < 6; ++k) a.out[k][i] = p[k];
@@ -556,6 +569,29 @@ __device__ __forceinline__ void kstep(typename K::IS (&st)[K::IPT], const float4
     else K::step(st, R);
 }
 
+// Compensated sums in registers (IS member) or, for kernels that set
+// SMEM_COMP, in shared memory at comp[(q * NP + k) * DS_THREADS + tid].
+template <class K, class = void>
+struct smem_comp : std::false_type {};
+template <class K>
+struct smem_comp<K, decltype(void(K::SMEM_COMP))> : std::integral_constant<bool, K::SMEM_COMP> {};
+
+template <class K>
+__device__ __forceinline__ void kfold(typename K::IS &st, Comp *c) {
+    if constexpr (smem_comp<K>::value) K::fold(st, c);
+    else K::fold(st);
+}
+template <class K>
+__device__ __forceinline__ void kpartials(const typename K::IS &st, const Comp *c, double *p) {
+    if constexpr (smem_comp<K>::value) K::partials(st, c, p);
+    else K::partials(st, p);
+}
+template <class K>
+__device__ __forceinline__ void kzero(Comp *c) {
+    if constexpr (smem_comp<K>::value)
+        for (int k = 0; k < K::NP; ++k) c[k * DS_THREADS] = Comp{0.f, 0.f};
+}
+
 // Per j-tile softening: tile_e2[t] = float(e2_j) if every valid j of tile t
 // has the same float value (bit pattern), else NaN.  One CTA per tile.
 __global__ void ds32_tile_e2(const double *e2, size_t nj, float *tile_e2) {
@@ -600,6 +636,8 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
     constexpr int IPT = K::IPT;
     constexpr int TILE_Q = DS_PAIRS * K::NQ;
     constexpr int BI = DS_THREADS * IPT;   // i-particles per i-tile
+    __shared__ Comp s_comp[smem_comp<K>::value ? IPT * K::NP * DS_THREADS : 1];
+    auto comp = [&](int q) { return s_comp + q * K::NP * DS_THREADS + threadIdx.x; };
     const long long nju = a.nju;
 
     const long long U = a.nit * nju;
@@ -631,6 +669,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
     for (int q = 0; q < IPT; ++q) {
         const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
         K::load(st[q], a.p, i < a.p.ni ? i : last);
+        kzero<K>(comp(q));
     }
     // i-tile softening: the common float(ie2) of the tile, or NaN
     __shared__ unsigned s_ie2;
@@ -676,7 +715,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
 #pragma unroll DS_UNROLL
                 for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, true>(st, R + (fb + pp) * K::NQ, E);
 #pragma unroll
-                for (int q = 0; q < IPT; ++q) K::fold(st[q]);
+                for (int q = 0; q < IPT; ++q) kfold<K>(st[q], comp(q));
             }
         } else {
 #pragma unroll 1
@@ -685,7 +724,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
 #pragma unroll DS_UNROLL
                 for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, false>(st, R + (fb + pp) * K::NQ, f2(0.f));
 #pragma unroll
-                for (int q = 0; q < IPT; ++q) K::fold(st[q]);
+                for (int q = 0; q < IPT; ++q) kfold<K>(st[q], comp(q));
             }
         }
         __syncthreads();   // stage s fully consumed
@@ -703,7 +742,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
             for (int q = 0; q < IPT; ++q) {
                 const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
                 double p[K::NP];
-                K::partials(st[q], p);
+                kpartials<K>(st[q], comp(q), p);
                 if (i < a.p.ni) K::store(p, a.p, i);
             }
         } else {
@@ -712,7 +751,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
 #pragma unroll
             for (int q = 0; q < IPT; ++q) {
                 double p[K::NP];
-                K::partials(st[q], p);
+                kpartials<K>(st[q], comp(q), p);
                 for (int v = 0; v < K::NP; ++v) mine[(q * K::NP + v) * DS_THREADS + tid] = p[v];
             }
             __threadfence();
@@ -768,6 +807,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
             for (int q = 0; q < IPT; ++q) {
                 const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
                 K::load(st[q], a.p, i < a.p.ni ? i : last);
+                kzero<K>(comp(q));
             }
             ie2 = tile_ie2();
         }
@@ -884,12 +924,15 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
     long long t = tile_of(c, u0);
     const long long git_first = a.itile_off[c] + t;
     typename K::IS st[IPT];
+    __shared__ Comp s_comp[smem_comp<K>::value ? IPT * K::NP * DS_THREADS : 1];
+    auto comp = [&](int q) { return s_comp + q * K::NP * DS_THREADS + threadIdx.x; };
     auto load_tile = [&](long long cl, long long tt) {
 #pragma unroll
         for (int q = 0; q < IPT; ++q) {
             const long long li = tt * BI + q * DS_THREADS + tid;
             const size_t i = (size_t)(a.seg_start[cl] + (li < a.seg_n[cl] ? li : 0));
             K::load(st[q], a.p, i);
+            kzero<K>(comp(q));
         }
     };
     load_tile(c, t);
@@ -912,7 +955,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
 #pragma unroll DS_UNROLL
             for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, false>(st, R + (fb + pp) * K::NQ, f2(0.f));
 #pragma unroll
-            for (int q = 0; q < IPT; ++q) K::fold(st[q]);
+            for (int q = 0; q < IPT; ++q) kfold<K>(st[q], comp(q));
         }
         __syncthreads();
         if (tid == 0 && u + DS_STAGES < u1) {
@@ -935,7 +978,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
             for (int q = 0; q < IPT; ++q) {
                 const long long li = t * BI + q * DS_THREADS + tid;
                 double p[K::NP];
-                K::partials(st[q], p);
+                kpartials<K>(st[q], comp(q), p);
                 if (li < a.seg_n[c]) K::store(p, a.p, (size_t)(a.seg_start[c] + li));
             }
         } else {
@@ -944,7 +987,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
 #pragma unroll
             for (int q = 0; q < IPT; ++q) {
                 double p[K::NP];
-                K::partials(st[q], p);
+                kpartials<K>(st[q], comp(q), p);
                 for (int v = 0; v < K::NP; ++v) mine[(q * K::NP + v) * DS_THREADS + tid] = p[v];
             }
             __threadfence();
@@ -1015,7 +1058,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
 // Host side.
 // ---------------------------------------------------------------------------
 #ifndef TG_DS32_MAX_JSUB
-#define TG_DS32_MAX_JSUB 8   // most parts a j-tile is split into
+#define TG_DS32_MAX_JSUB 2   // most parts a j-tile is split into (measured best at N = 4096)
 #endif
 struct Geometry {
     long long nit, njt, units, grid;

@@ -227,14 +227,14 @@ struct PNAcc64 {
 };
 
 struct Sakura64 {
-    static constexpr int NF = 8, NO = 6;
-    struct St { double f[8]; double d[6]; unsigned flags; };
+    static constexpr int NF = 8, NO = 6, NT = 6;
+    struct St { double f[8]; double acc[NT]; };
     __device__ static void init(St &s, const PairArgs &a, size_t i) {
         for (int k = 0; k < 8; ++k) s.f[k] = a.I.f[k][i];
-        for (int k = 0; k < 6; ++k) s.d[k] = 0.0;
-        s.flags = 0;
+        for (int k = 0; k < NT; ++k) s.acc[k] = 0.0;
     }
-    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a) {
+    // A pair that reaches a retry bound raises its status bit here (rare).
+    __device__ static void terms(const St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a, double *t) {
         double r0[3], v0[3], r1[3], v1[3];
         for (int k = 0; k < 3; ++k) {
             r0[k] = dsub(s.f[F_RX + k], sj[F_RX + k][jj]);
@@ -244,16 +244,16 @@ struct Sakura64 {
         double m = dadd(s.f[F_M], sj[F_M][jj]);
         KepBudget b;
         pair_evolve(a.dt, a.flag, m, e2, r0, v0, r1, v1, b);
-        s.flags |= b.flags;
+        if (b.flags) atomicOr(a.status, b.flags);
         double w = ddiv(sj[F_M][jj], m);
         for (int k = 0; k < 3; ++k) {
-            s.d[k] = dadd(s.d[k], dmul(w, dsub(r1[k], r0[k])));
-            s.d[3 + k] = dadd(s.d[3 + k], dmul(w, dsub(v1[k], v0[k])));
+            t[k] = dmul(w, dsub(r1[k], r0[k]));
+            t[3 + k] = dmul(w, dsub(v1[k], v0[k]));
         }
     }
-    __device__ static void store(const St &s, const PairArgs &a, size_t i) {
-        for (int k = 0; k < 6; ++k) a.out[k][i] = s.d[k];
-        if (s.flags) atomicOr(a.status, s.flags);
+    __device__ static double accum(int, double acc, double t) { return dadd(acc, t); }
+    __device__ static void store_acc(const double *acc, const St &, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 6; ++k) a.out[k][i] = acc[k];
     }
 };
 
