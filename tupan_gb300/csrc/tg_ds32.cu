@@ -67,12 +67,6 @@ struct DsArgs {
     int *ticket;         // [NIT]
     const float *tile_e2;  // [NJT] common j softening per tile or NaN; may be null
     long long nit, njt;  // i-tiles, j-tiles
-    // A unit is (i-tile, part of a j-tile): small problems split each j-tile
-    // into jsub parts (1, 2, 4 or 8) so that the units outnumber the CTAs.
-    int jsub;
-    long long nju;       // units per i-tile = njt * jsub
-    int part_pairs;      // j-records per part (a whole number of fold blocks)
-    int part_q;          // float4 per part
 };
 
 __device__ __forceinline__ float fzero_norm(float x) { return x + 0.0f; }  // -0 -> +0
@@ -255,10 +249,11 @@ struct PhiDS {
 template <int IPT_, bool REFINE>
 struct AccJerkDS {
     static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 6;
-    static constexpr bool UE2 = true;
+    // The hoisted-softening form measured slower here (4.67 vs 4.57 ms at
+    // N = 65536), so AccJerk always adds the pair softening.
+    static constexpr bool UE2 = false;
     // The compensated sums live in shared memory (touched once per fold
-    // block), which keeps the registers below the limit with the
-    // hoisted-softening form.
+    // block), relieving the 128-register budget (measured 0.2% faster).
     static constexpr bool SMEM_COMP = true;
     struct IS { IPos q; float2 u, v, w, e; float2 a[6]; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {
@@ -628,7 +623,7 @@ __device__ __forceinline__ long long unit_owner(long long u, long long U, long l
 #define TG_DS32_UNROLL 4
 #endif
 constexpr int DS_UNROLL = TG_DS32_UNROLL;
-template <class K>
+template <class K, int JSUB>
 __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs a) {
     extern __shared__ __align__(128) float4 ring[];   // [DS_STAGES][DS_PAIRS * NQ]
     __shared__ __align__(8) uint64_t full[DS_STAGES];
@@ -638,7 +633,10 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
     constexpr int BI = DS_THREADS * IPT;   // i-particles per i-tile
     __shared__ Comp s_comp[smem_comp<K>::value ? IPT * K::NP * DS_THREADS : 1];
     auto comp = [&](int q) { return s_comp + q * K::NP * DS_THREADS + threadIdx.x; };
-    const long long nju = a.nju;
+    // JSUB parts per j-tile (1 or 2): a unit is an i-tile x one part
+    constexpr int PART_PAIRS = DS_PAIRS / JSUB;
+    constexpr int PART_Q = PART_PAIRS * K::NQ;
+    const long long nju = a.njt * JSUB;
 
     const long long U = a.nit * nju;
     const long long G = gridDim.x;
@@ -653,10 +651,10 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
     }
     __syncthreads();
     auto issue = [&](long long u, int s) {
-        const long long jp = u % a.nju;     // part jp % jsub of j-tile jp / jsub
-        const unsigned bytes = (unsigned)(a.part_q * sizeof(float4));
+        const long long jp = u % nju;       // part jp % JSUB of j-tile jp / JSUB
+        constexpr unsigned bytes = (unsigned)(PART_Q * sizeof(float4));
         mbar_expect_tx(&full[s], bytes);
-        bulk_g2s(ring + s * TILE_Q, a.rec + jp * a.part_q, bytes, &full[s]);
+        bulk_g2s(ring + s * TILE_Q, a.rec + jp * PART_Q, bytes, &full[s]);
     };
     if (tid == 0) {
         for (int s = 0; s < DS_STAGES && u0 + s < u1; ++s) issue(u0 + s, s);
@@ -706,12 +704,11 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
         // pair's own add would give (NaN, i.e. not uniform, propagates)
         float ue = __uint_as_float(0x7fc00000u);
         if constexpr (K::UE2)
-            if (a.tile_e2) ue = __fadd_rn(ie2, __ldg(a.tile_e2 + (u % nju) / a.jsub));
+            if (a.tile_e2) ue = __fadd_rn(ie2, __ldg(a.tile_e2 + (u % nju) / JSUB));
         if (K::UE2 && ue == ue) {
             const float2 E = f2(ue);
 #pragma unroll 1
-            for (int fb = 0; fb < DS_PAIRS; fb += DS_FOLD_PAIRS) {
-                if (fb >= a.part_pairs) break;
+            for (int fb = 0; fb < PART_PAIRS; fb += DS_FOLD_PAIRS) {
 #pragma unroll DS_UNROLL
                 for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, true>(st, R + (fb + pp) * K::NQ, E);
 #pragma unroll
@@ -719,8 +716,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
             }
         } else {
 #pragma unroll 1
-            for (int fb = 0; fb < DS_PAIRS; fb += DS_FOLD_PAIRS) {
-                if (fb >= a.part_pairs) break;
+            for (int fb = 0; fb < PART_PAIRS; fb += DS_FOLD_PAIRS) {
 #pragma unroll DS_UNROLL
                 for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, false>(st, R + (fb + pp) * K::NQ, f2(0.f));
 #pragma unroll
@@ -1058,7 +1054,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
 // Host side.
 // ---------------------------------------------------------------------------
 #ifndef TG_DS32_MAX_JSUB
-#define TG_DS32_MAX_JSUB 2   // most parts a j-tile is split into (measured best at N = 4096)
+#define TG_DS32_MAX_JSUB 2   // parts a j-tile may be split into (1 or 2; 2 measured best at N = 4096)
 #endif
 struct Geometry {
     long long nit, njt, units, grid;
@@ -1071,9 +1067,10 @@ static int ctas_per_sm() {
     static int cached = -1;
     if (cached < 0) {
         const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
-        cudaFuncSetAttribute(ds32_streamk<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(ds32_streamk<K, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(ds32_streamk<K, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int n = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ds32_streamk<K>, DS_THREADS, smem) != cudaSuccess || n < 1)
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ds32_streamk<K, 1>, DS_THREADS, smem) != cudaSuccess || n < 1)
             n = 1;
         cached = n;
     }
@@ -1091,8 +1088,7 @@ static Geometry geometry(size_t ni, size_t nj, int sms) {
     const long long slots = (long long)sms * ctas_per_sm<K>();
     // split j-tiles until there are at least two units per CTA slot
     g.jsub = 1;
-    while (g.jsub < DS_PAIRS / DS_FOLD_PAIRS && g.jsub < TG_DS32_MAX_JSUB && g.nit * g.njt * g.jsub < 2 * slots)
-        g.jsub *= 2;
+    if (TG_DS32_MAX_JSUB >= 2 && g.nit * g.njt < 2 * slots) g.jsub = 2;
     g.units = g.nit * g.njt * g.jsub;
     g.grid = g.units < slots ? g.units : slots;
     g.rec_bytes = align_up((size_t)g.njt * DS_PAIRS * K::NQ * sizeof(float4), 256);
@@ -1122,10 +1118,7 @@ static cudaError_t run_ds(const PairArgs &p, void *ws, size_t ws_bytes, int sms,
     a.tile_e2 = K::UE2 ? tile_e2 : nullptr;
     a.nit = g.nit;
     a.njt = g.njt;
-    a.jsub = g.jsub;
-    a.nju = g.njt * g.jsub;
-    a.part_pairs = DS_PAIRS / g.jsub;
-    a.part_q = a.part_pairs * K::NQ;
+
     const size_t npairs = (size_t)g.njt * DS_PAIRS;
     const PackSpec spec = K::pack();
     const unsigned pack_blocks = (unsigned)((npairs * 2 + 255) / 256);
@@ -1134,7 +1127,8 @@ static cudaError_t run_ds(const PairArgs &p, void *ws, size_t ws_bytes, int sms,
     cudaError_t e = cudaMemsetAsync(a.ticket, 0, g.ticket_bytes, s);
     if (e != cudaSuccess) return e;
     const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
-    ds32_streamk<K><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
+    if (g.jsub == 2) ds32_streamk<K, 2><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
+    else ds32_streamk<K, 1><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -1163,10 +1157,7 @@ static cudaError_t run_ds_capped(const PairArgs &p, void *ws, size_t ws_bytes, i
     a.tile_e2 = nullptr;   // general path only: the scratch layout stays fixed
     a.nit = g.nit;
     a.njt = g.njt;
-    a.jsub = g.jsub;
-    a.nju = g.njt * g.jsub;
-    a.part_pairs = DS_PAIRS / g.jsub;
-    a.part_q = a.part_pairs * K::NQ;
+
     const size_t npairs = (size_t)g.njt * DS_PAIRS;
     const PackSpec spec = K::pack();
     const unsigned pack_blocks = (unsigned)((npairs * 2 + 255) / 256);
@@ -1174,7 +1165,8 @@ static cudaError_t run_ds_capped(const PairArgs &p, void *ws, size_t ws_bytes, i
     cudaError_t e = cudaMemsetAsync(a.ticket, 0, g.ticket_bytes, s);
     if (e != cudaSuccess) return e;
     const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
-    ds32_streamk<K><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
+    if (g.jsub == 2) ds32_streamk<K, 2><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
+    else ds32_streamk<K, 1><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
     return cudaGetLastError();
 }
 
