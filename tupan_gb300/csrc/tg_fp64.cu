@@ -187,15 +187,15 @@ struct Tstep64 {
 };
 
 struct PNAcc64 {
-    static constexpr int NF = 8, NO = 3;
-    struct St { double m, x, y, z, e, u, v, w, iv2, a[3]; };
+    static constexpr int NF = 8, NO = 3, NT = 3;
+    struct St { double m, x, y, z, e, u, v, w, iv2, acc[NT]; };
     __device__ static void init(St &s, const PairArgs &a, size_t i) {
         s.m = a.I.f[F_M][i]; s.x = a.I.f[F_RX][i]; s.y = a.I.f[F_RY][i]; s.z = a.I.f[F_RZ][i];
         s.e = a.I.f[F_E2][i]; s.u = a.I.f[F_VX][i]; s.v = a.I.f[F_VY][i]; s.w = a.I.f[F_VZ][i];
         s.iv2 = s.u * s.u + s.v * s.v + s.w * s.w;
-        s.a[0] = s.a[1] = s.a[2] = 0.0;
+        s.acc[0] = s.acc[1] = s.acc[2] = 0.0;
     }
-    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a) {
+    __device__ static void terms(const St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a, double *t) {
         double jm = sj[F_M][jj];
         double ju = sj[F_VX][jj], jv = sj[F_VY][jj], jw = sj[F_VZ][jj];
         double rx = s.x - sj[F_RX][jj], ry = s.y - sj[F_RY][jj], rz = s.z - sj[F_RZ][jj];
@@ -217,12 +217,13 @@ struct PNAcc64 {
                            a.inv[2], a.inv[4], a.inv[5], a.inv[6], a.inv[7], A, B);
         A *= jm * q3;
         B *= jm * q2;
-        s.a[0] += A * rx + B * vx;
-        s.a[1] += A * ry + B * vy;
-        s.a[2] += A * rz + B * vz;
+        t[0] = A * rx + B * vx;
+        t[1] = A * ry + B * vy;
+        t[2] = A * rz + B * vz;
     }
-    __device__ static void store(const St &s, const PairArgs &a, size_t i) {
-        for (int k = 0; k < 3; ++k) a.out[k][i] = s.a[k];
+    __device__ static double accum(int, double acc, double t) { return acc + t; }
+    __device__ static void store_acc(const double *acc, const St &, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 3; ++k) a.out[k][i] = acc[k];
     }
 };
 
@@ -297,15 +298,14 @@ struct AccVjp64 {
 // with the relative velocity; sums m_j r_ij, the softened acceleration and
 // m_i sum m_j / r_ij.
 struct NregX64 {
-    static constexpr int NF = 8, NO = 7;
-    struct St { double m, x, y, z, e, u, v, w, mr[3], a[3], pot; };
+    static constexpr int NF = 8, NO = 7, NT = 7;   // terms: m_j r (3), q3 r (3), m_j q1
+    struct St { double m, x, y, z, e, u, v, w, acc[NT]; };
     __device__ static void init(St &s, const PairArgs &a, size_t i) {
         s.m = a.I.f[F_M][i]; s.x = a.I.f[F_RX][i]; s.y = a.I.f[F_RY][i]; s.z = a.I.f[F_RZ][i];
         s.e = a.I.f[F_E2][i]; s.u = a.I.f[F_VX][i]; s.v = a.I.f[F_VY][i]; s.w = a.I.f[F_VZ][i];
-        for (int k = 0; k < 3; ++k) { s.mr[k] = 0.0; s.a[k] = 0.0; }
-        s.pot = 0.0;
+        for (int k = 0; k < NT; ++k) s.acc[k] = 0.0;
     }
-    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a) {
+    __device__ static void terms(const St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a, double *t) {
         double rx = dsub(s.x, sj[F_RX][jj]), ry = dsub(s.y, sj[F_RY][jj]), rz = dsub(s.z, sj[F_RZ][jj]);
         const double e2 = dadd(s.e, sj[F_E2][jj]);
         const double vx = dsub(s.u, sj[F_VX][jj]), vy = dsub(s.v, sj[F_VY][jj]), vz = dsub(s.w, sj[F_VZ][jj]);
@@ -317,32 +317,30 @@ struct NregX64 {
         const double q1 = dsqrt(q2);
         const double mj = sj[F_M][jj];
         const double q3 = dmul(dmul(q2, q1), mj);
-        s.mr[0] = dadd(s.mr[0], dmul(mj, rx));
-        s.mr[1] = dadd(s.mr[1], dmul(mj, ry));
-        s.mr[2] = dadd(s.mr[2], dmul(mj, rz));
-        s.a[0] = dsub(s.a[0], dmul(q3, rx));
-        s.a[1] = dsub(s.a[1], dmul(q3, ry));
-        s.a[2] = dsub(s.a[2], dmul(q3, rz));
-        s.pot = dadd(s.pot, dmul(mj, q1));
+        t[0] = dmul(mj, rx); t[1] = dmul(mj, ry); t[2] = dmul(mj, rz);
+        t[3] = dmul(q3, rx); t[4] = dmul(q3, ry); t[5] = dmul(q3, rz);
+        t[6] = dmul(mj, q1);
     }
-    __device__ static void store(const St &s, const PairArgs &a, size_t i) {
-        for (int k = 0; k < 3; ++k) { a.out[k][i] = s.mr[k]; a.out[3 + k][i] = s.a[k]; }
-        a.out[6][i] = dmul(s.m, s.pot);
+    __device__ static double accum(int c, double acc, double t) {
+        return (c >= 3 && c < 6) ? dsub(acc, t) : dadd(acc, t);
+    }
+    __device__ static void store_acc(const double *acc, const St &s, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 6; ++k) a.out[k][i] = acc[k];
+        a.out[6][i] = dmul(s.m, acc[6]);
     }
 };
 
 // NREG_V (nreg_kernels_common.h:62-102): the relative velocity is kicked by
 // dt with the relative acceleration; sums m_j v_ij and m_i sum m_j |v_ij|^2.
 struct NregV64 {
-    static constexpr int NF = 11, NO = 4;
-    struct St { double m, u, v, w, ax, ay, az, mv[3], k; };
+    static constexpr int NF = 11, NO = 4, NT = 4;   // terms: m_j v (3), m_j |v|^2
+    struct St { double m, u, v, w, ax, ay, az, acc[NT]; };
     __device__ static void init(St &s, const PairArgs &a, size_t i) {
         s.m = a.I.f[F_M][i]; s.u = a.I.f[F_VX][i]; s.v = a.I.f[F_VY][i]; s.w = a.I.f[F_VZ][i];
         s.ax = a.I.f[F_AX][i]; s.ay = a.I.f[F_AY][i]; s.az = a.I.f[F_AZ][i];
-        for (int k = 0; k < 3; ++k) s.mv[k] = 0.0;
-        s.k = 0.0;
+        for (int k = 0; k < NT; ++k) s.acc[k] = 0.0;
     }
-    __device__ static void pair(St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a) {
+    __device__ static void terms(const St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a, double *t) {
         double vx = dsub(s.u, sj[F_VX][jj]), vy = dsub(s.v, sj[F_VY][jj]), vz = dsub(s.w, sj[F_VZ][jj]);
         const double ax = dsub(s.ax, sj[F_AX][jj]), ay = dsub(s.ay, sj[F_AY][jj]), az = dsub(s.az, sj[F_AZ][jj]);
         vx = dadd(vx, dmul(ax, a.dt));
@@ -350,14 +348,13 @@ struct NregV64 {
         vz = dadd(vz, dmul(az, a.dt));
         const double v2 = ddot3(vx, vy, vz, vx, vy, vz);
         const double mj = sj[F_M][jj];
-        s.mv[0] = dadd(s.mv[0], dmul(mj, vx));
-        s.mv[1] = dadd(s.mv[1], dmul(mj, vy));
-        s.mv[2] = dadd(s.mv[2], dmul(mj, vz));
-        s.k = dadd(s.k, dmul(mj, v2));
+        t[0] = dmul(mj, vx); t[1] = dmul(mj, vy); t[2] = dmul(mj, vz);
+        t[3] = dmul(mj, v2);
     }
-    __device__ static void store(const St &s, const PairArgs &a, size_t i) {
-        for (int k = 0; k < 3; ++k) a.out[k][i] = s.mv[k];
-        a.out[3][i] = dmul(s.m, s.k);
+    __device__ static double accum(int, double acc, double t) { return dadd(acc, t); }
+    __device__ static void store_acc(const double *acc, const St &s, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 3; ++k) a.out[k][i] = acc[k];
+        a.out[3][i] = dmul(s.m, acc[3]);
     }
 };
 
