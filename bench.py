@@ -50,6 +50,10 @@ FLOP_ACC_JERK = 42  # tupan/lib/src/acc_jerk_kernel_common.h:56
 # from an ncu capture (profiles/ds32_acc_jerk_n65536.txt)
 TRAFFIC_ACC_JERK_N65536 = 6.86e6
 METRIC = "Gint/s Acc+AccJerk split-FP32 (N=65536 Plummer-Salpeter, eps2=1e-6)"
+# library kernels per step: Acc = pack + softening flags + stream-K,
+# AccJerk = pack + stream-K
+LAUNCHES_PER_STEP = 5
+SMALL_SIZES = (4096, 16384)
 P5 = ("mass", "rx", "ry", "rz", "eps2")
 P8 = P5 + ("vx", "vy", "vz")
 
@@ -198,6 +202,43 @@ def rel_errors(got, want):
             "median": float(np.median(r)), "rms": float(np.sqrt((r * r).mean()))}
 
 
+def small_sizes(dev, sp):
+    """Acc and AccJerk at N = 4096 and 16384 (same workload family): median
+    CUDA-event time of split FP32 and FP64 calls and the split-FP32 force
+    error against FP64."""
+    import torch
+    from tupan_gb300 import _native
+    out = {}
+    for n in SMALL_SIZES:
+        d = workload(n, 0)
+        T = {k: torch.tensor(d[k], dtype=torch.float64, device=dev) for k in P8}
+        rec = {}
+        res = {}
+        for name, fields, no in (("acc", P5, 3), ("acc_jerk", P8, 6)):
+            for prec, pname, reps in ((_native.PREC_DS32, "ds32", 7), (_native.PREC_FP64, "fp64", 3)):
+                o = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(no)]
+
+                def call():
+                    _native.call_device(name, n, [T[k].data_ptr() for k in fields], n,
+                                        [T[k].data_ptr() for k in fields], (), [x.data_ptr() for x in o], prec, sp)
+                call()
+                ms = []
+                for _ in range(reps):
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    call()
+                    e1.record()
+                    e1.synchronize()
+                    ms.append(e0.elapsed_time(e1))
+                med = float(np.median(ms))
+                rec["%s_%s" % (name, pname)] = {"ms": med, "gint_s": n * n / (med * 1e-3) / 1e9}
+                res[(name, pname)] = np.stack([x.cpu().numpy() for x in o])
+        rec["force_error_acc_max"] = rel_errors(res[("acc", "ds32")], res[("acc", "fp64")])["max"]
+        rec["force_error_jerk_max"] = rel_errors(res[("acc_jerk", "ds32")][3:], res[("acc_jerk", "fp64")][3:])["max"]
+        out[str(n)] = rec
+    return out
+
+
 def ours(args, rank, world, dist):
     import torch
     from tupan_gb300 import _native
@@ -274,7 +315,7 @@ def ours(args, rank, world, dist):
     line = {"metric": METRIC, "value": value, "unit": "Gint/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "ds32", "data": "synthetic",
-            "config": config(n), "gpu_launches": 4 * args.steps,
+            "config": config(n), "gpu_launches": LAUNCHES_PER_STEP * args.steps,
             "kernels": {"acc_ds32": {"ms": acc_ms, "gint_s": n * n / (acc_ms * 1e-3) / 1e9},
                         "acc_jerk_ds32": {"ms": aj_ms, "gint_s": n * n / (aj_ms * 1e-3) / 1e9}},
             "roofline": {"bound": "fp32", "kernel": "ds32_streamk<AccJerkDS>",
@@ -309,6 +350,10 @@ def ours(args, rank, world, dist):
         line["force_error"] = {"acc": rel_errors(ds_acc, f_acc), "acc_in_acc_jerk": rel_errors(ds_aj[:3], f_aj[:3]),
                                "jerk": rel_errors(ds_aj[3:], f_aj[3:]),
                                "against": "FP64 GPU kernels (bit-identical to the reference C backend)"}
+
+    # ---- the smaller sizes of the same workload (parity/measurement only) --
+    if rank == 0 and not args.no_fp64:
+        line["sizes"] = small_sizes(dev, sp)
 
     # ---- end to end through the drop-in host entry points ---------------
     pin = {k: torch.tensor(d[k], dtype=torch.float64).pin_memory() for k in P8}

@@ -47,6 +47,9 @@ constexpr int DS_THREADS = TG_DS32_THREADS;   // threads per CTA
 #ifndef TG_DS32_FOLD
 #define TG_DS32_FOLD 64
 #endif
+#ifndef TG_DS32_UNROLL
+#define TG_DS32_UNROLL 4   // j-records per unrolled block (kernels may override)
+#endif
 constexpr int DS_TILE = TG_DS32_TILE;     // j-particles per tile
 constexpr int DS_PAIRS = DS_TILE / 2;
 constexpr int DS_STAGES = TG_DS32_STAGES;
@@ -250,19 +253,19 @@ template <int IPT_, bool REFINE>
 struct AccJerkDS {
     static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 6;
     // The hoisted-softening form measured slower here (4.67 vs 4.57 ms at
-    // N = 65536), so AccJerk always adds the pair softening.
+    // N = 65536), so AccJerk always adds the pair softening; its
+    // compensated sums stay in registers (shared-memory sums measured 0.3%
+    // slower); eight records per unrolled block (0.8% faster than four).
     static constexpr bool UE2 = false;
-    // The compensated sums live in shared memory (touched once per fold
-    // block), relieving the 128-register budget (measured 0.2% faster).
-    static constexpr bool SMEM_COMP = true;
-    struct IS { IPos q; float2 u, v, w, e; float2 a[6]; };
+    static constexpr int UNROLL = 8;
+    struct IS { IPos q; float2 u, v, w, e; float2 a[6]; Comp c[6]; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {
         load_pos(a, i, s.q);
         s.u = f2(__double2float_rn(a.I.f[F_VX][i]));
         s.v = f2(__double2float_rn(a.I.f[F_VY][i]));
         s.w = f2(__double2float_rn(a.I.f[F_VZ][i]));
         s.e = f2(__double2float_rn(a.I.f[F_E2][i]));
-        for (int k = 0; k < 6; ++k) s.a[k] = f2(0.f);
+        for (int k = 0; k < 6; ++k) { s.a[k] = f2(0.f); s.c[k] = Comp{0.f, 0.f}; }
     }
     __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R) {
         step<false>(S, R, f2(0.f));
@@ -295,19 +298,10 @@ struct AccJerkDS {
             s.a[5] = fnma2(mr3, tw, s.a[5]);
         }
     }
-    // c[k * DS_THREADS]: this thread's compensated sum k in shared memory
-    __device__ static void fold(IS &s, Comp *c) {
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-            Comp v = c[k * DS_THREADS];
-            comp_add(v, __fadd_rn(s.a[k].x, s.a[k].y));
-            c[k * DS_THREADS] = v;
-            s.a[k] = f2(0.f);
-        }
+    __device__ static void fold(IS &s) {
+        for (int k = 0; k < 6; ++k) { comp_add(s.c[k], __fadd_rn(s.a[k].x, s.a[k].y)); s.a[k] = f2(0.f); }
     }
-    __device__ static void partials(const IS &, const Comp *c, double *p) {
-        for (int k = 0; k < 6; ++k) p[k] = comp_value(c[k * DS_THREADS]);
-    }
+    __device__ static void partials(const IS &s, double *p) { for (int k = 0; k < 6; ++k) p[k] = comp_value(s.c[k]); }
     __device__ static void combine(double *acc, const double *p) { for (int k = 0; k < 6; ++k) acc[k] += p[k]; }
     __device__ static void store(const double *p, const PairArgs &a, size_t i) {
         for (int k = 0; k < 6; ++k) a.out[k][i] = p[k];
@@ -571,6 +565,11 @@ struct smem_comp : std::false_type {};
 template <class K>
 struct smem_comp<K, decltype(void(K::SMEM_COMP))> : std::integral_constant<bool, K::SMEM_COMP> {};
 
+template <class K, class = void>
+struct kunroll : std::integral_constant<int, TG_DS32_UNROLL> {};
+template <class K>
+struct kunroll<K, decltype(void(K::UNROLL))> : std::integral_constant<int, K::UNROLL> {};
+
 template <class K>
 __device__ __forceinline__ void kfold(typename K::IS &st, Comp *c) {
     if constexpr (smem_comp<K>::value) K::fold(st, c);
@@ -619,10 +618,6 @@ __device__ __forceinline__ long long unit_owner(long long u, long long U, long l
 #ifndef TG_DS32_MINB
 #define TG_DS32_MINB 2
 #endif
-#ifndef TG_DS32_UNROLL
-#define TG_DS32_UNROLL 4
-#endif
-constexpr int DS_UNROLL = TG_DS32_UNROLL;
 template <class K, int JSUB>
 __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs a) {
     extern __shared__ __align__(128) float4 ring[];   // [DS_STAGES][DS_PAIRS * NQ]
@@ -631,6 +626,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
     constexpr int IPT = K::IPT;
     constexpr int TILE_Q = DS_PAIRS * K::NQ;
     constexpr int BI = DS_THREADS * IPT;   // i-particles per i-tile
+    constexpr int UNR = kunroll<K>::value;
     __shared__ Comp s_comp[smem_comp<K>::value ? IPT * K::NP * DS_THREADS : 1];
     auto comp = [&](int q) { return s_comp + q * K::NP * DS_THREADS + threadIdx.x; };
     // JSUB parts per j-tile (1 or 2): a unit is an i-tile x one part
@@ -709,7 +705,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
             const float2 E = f2(ue);
 #pragma unroll 1
             for (int fb = 0; fb < PART_PAIRS; fb += DS_FOLD_PAIRS) {
-#pragma unroll DS_UNROLL
+#pragma unroll UNR
                 for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, true>(st, R + (fb + pp) * K::NQ, E);
 #pragma unroll
                 for (int q = 0; q < IPT; ++q) kfold<K>(st[q], comp(q));
@@ -717,7 +713,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
         } else {
 #pragma unroll 1
             for (int fb = 0; fb < PART_PAIRS; fb += DS_FOLD_PAIRS) {
-#pragma unroll DS_UNROLL
+#pragma unroll UNR
                 for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, false>(st, R + (fb + pp) * K::NQ, f2(0.f));
 #pragma unroll
                 for (int q = 0; q < IPT; ++q) kfold<K>(st[q], comp(q));
@@ -886,6 +882,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
     constexpr int TILE_Q = DS_PAIRS * K::NQ;
     constexpr unsigned TILE_BYTES = TILE_Q * sizeof(float4);
     constexpr int BI = DS_THREADS * IPT;
+    constexpr int UNR = kunroll<K>::value;
 
     const long long U = a.U;
     const long long G = gridDim.x;
@@ -948,7 +945,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
         const float4 *R = ring + s * TILE_Q;
 #pragma unroll 1
         for (int fb = 0; fb < DS_PAIRS; fb += DS_FOLD_PAIRS) {
-#pragma unroll DS_UNROLL
+#pragma unroll UNR
             for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, false>(st, R + (fb + pp) * K::NQ, f2(0.f));
 #pragma unroll
             for (int q = 0; q < IPT; ++q) kfold<K>(st[q], comp(q));
