@@ -618,29 +618,20 @@ __device__ __forceinline__ long long unit_owner(long long u, long long U, long l
 #ifndef TG_DS32_MINB
 #define TG_DS32_MINB 2
 #endif
-template <class K, int JSUB, int WG>
+template <class K, int JSUB>
 __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs a) {
     extern __shared__ __align__(128) float4 ring[];   // [DS_STAGES][DS_PAIRS * NQ]
     __shared__ __align__(8) uint64_t full[DS_STAGES];
     __shared__ int s_last;
     constexpr int IPT = K::IPT;
     constexpr int TILE_Q = DS_PAIRS * K::NQ;
-    // WG warp groups (1 or 4): each group holds the same i-particles and
-    // folds its own share of every j-part; the groups' sums are combined in
-    // group order in shared memory when an i-tile is finished.  Small
-    // problems use WG = 4 so that the (smaller) i-tiles give enough units.
-    constexpr int TPG = DS_THREADS / WG;   // threads per group
-    constexpr int BI = TPG * IPT;          // i-particles per i-tile
+    constexpr int BI = DS_THREADS * IPT;   // i-particles per i-tile
     constexpr int UNR = kunroll<K>::value;
-    const int grp = threadIdx.x / TPG, gt = threadIdx.x % TPG;
-    __shared__ double s_red[WG > 1 ? (WG - 1) * K::NP * TPG : 1];
     __shared__ Comp s_comp[smem_comp<K>::value ? IPT * K::NP * DS_THREADS : 1];
     auto comp = [&](int q) { return s_comp + q * K::NP * DS_THREADS + threadIdx.x; };
     // JSUB parts per j-tile (1 or 2): a unit is an i-tile x one part
     constexpr int PART_PAIRS = DS_PAIRS / JSUB;
     constexpr int PART_Q = PART_PAIRS * K::NQ;
-    constexpr int GROUP_PAIRS = PART_PAIRS / WG;   // records each group folds per unit
-    static_assert(GROUP_PAIRS % DS_FOLD_PAIRS == 0, "whole fold blocks per group");
     const long long nju = a.njt * JSUB;
 
     const long long U = a.nit * nju;
@@ -670,7 +661,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
     typename K::IS st[IPT];
 #pragma unroll
     for (int q = 0; q < IPT; ++q) {
-        const size_t i = (size_t)t * BI + q * TPG + gt;
+        const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
         K::load(st[q], a.p, i < a.p.ni ? i : last);
         kzero<K>(comp(q));
     }
@@ -704,7 +695,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
             abort_u = u;
             break;
         }
-        const float4 *R = ring + s * TILE_Q + grp * GROUP_PAIRS * K::NQ;
+        const float4 *R = ring + s * TILE_Q;
         // uniform softening for this unit: E = ie2 + je2, the value every
         // pair's own add would give (NaN, i.e. not uniform, propagates)
         float ue = __uint_as_float(0x7fc00000u);
@@ -713,7 +704,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
         if (K::UE2 && ue == ue) {
             const float2 E = f2(ue);
 #pragma unroll 1
-            for (int fb = 0; fb < GROUP_PAIRS; fb += DS_FOLD_PAIRS) {
+            for (int fb = 0; fb < PART_PAIRS; fb += DS_FOLD_PAIRS) {
 #pragma unroll UNR
                 for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, true>(st, R + (fb + pp) * K::NQ, E);
 #pragma unroll
@@ -721,7 +712,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
             }
         } else {
 #pragma unroll 1
-            for (int fb = 0; fb < GROUP_PAIRS; fb += DS_FOLD_PAIRS) {
+            for (int fb = 0; fb < PART_PAIRS; fb += DS_FOLD_PAIRS) {
 #pragma unroll UNR
                 for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, false>(st, R + (fb + pp) * K::NQ, f2(0.f));
 #pragma unroll
@@ -737,43 +728,23 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
         if (tn == t) continue;
 
         // ---- i-tile t is done for this CTA: store or hand over partials ----
-        // This CTA's sums for the tile: per group, then (WG > 1) combined in
-        // group order into group 0 through shared memory.
-        double p[IPT][K::NP];
-#pragma unroll
-        for (int q = 0; q < IPT; ++q) kpartials<K>(st[q], comp(q), p[q]);
-        if constexpr (WG > 1) {
-#pragma unroll
-            for (int q = 0; q < IPT; ++q) {
-                if (grp > 0)
-                    for (int w = 0; w < K::NP; ++w) s_red[((grp - 1) * K::NP + w) * TPG + gt] = p[q][w];
-                __syncthreads();
-                if (grp == 0) {
-                    for (int g = 1; g < WG; ++g) {
-                        double v[K::NP];
-                        for (int w = 0; w < K::NP; ++w) v[w] = s_red[((g - 1) * K::NP + w) * TPG + gt];
-                        K::combine(p[q], v);
-                    }
-                }
-                __syncthreads();
-            }
-        }
         const long long ta = t * nju, tb = ta + nju;
         if (ta >= u0 && tb <= u1) {
-            if (grp == 0) {
 #pragma unroll
-                for (int q = 0; q < IPT; ++q) {
-                    const size_t i = (size_t)t * BI + q * TPG + gt;
-                    if (i < a.p.ni) K::store(p[q], a.p, i);
-                }
+            for (int q = 0; q < IPT; ++q) {
+                const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
+                double p[K::NP];
+                kpartials<K>(st[q], comp(q), p);
+                if (i < a.p.ni) K::store(p, a.p, i);
             }
         } else {
             const int slot = (t == u0 / nju) ? 0 : 1;
             double *mine = a.part + ((k * 2 + slot) * IPT * K::NP) * DS_THREADS;
-            if (grp == 0) {
 #pragma unroll
-                for (int q = 0; q < IPT; ++q)
-                    for (int v = 0; v < K::NP; ++v) mine[(q * K::NP + v) * DS_THREADS + gt] = p[q][v];
+            for (int q = 0; q < IPT; ++q) {
+                double p[K::NP];
+                kpartials<K>(st[q], comp(q), p);
+                for (int v = 0; v < K::NP; ++v) mine[(q * K::NP + v) * DS_THREADS + tid] = p[v];
             }
             __threadfence();
             __syncthreads();
@@ -783,13 +754,13 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
                 s_last = (prev == (int)(khi - klo));
             }
             __syncthreads();
-            if (s_last && grp == 0) {
+            if (s_last) {
                 // Sum the contributors' partials in CTA order (deterministic);
                 // two contributors' loads are in flight per step.
                 __threadfence();
                 auto slot_ptr = [&](long long kk) {
                     const int sl = (t == unit_start(kk, U, G) / nju) ? 0 : 1;
-                    return a.part + ((kk * 2 + sl) * IPT * K::NP) * DS_THREADS + gt;
+                    return a.part + ((kk * 2 + sl) * IPT * K::NP) * DS_THREADS + tid;
                 };
                 double acc[IPT][K::NP];
                 {
@@ -817,7 +788,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
                 }
 #pragma unroll
                 for (int q = 0; q < IPT; ++q) {
-                    const size_t i = (size_t)t * BI + q * TPG + gt;
+                    const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
                     if (i < a.p.ni) K::store(acc[q], a.p, i);
                 }
             }
@@ -826,7 +797,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
             t = tn;
 #pragma unroll
             for (int q = 0; q < IPT; ++q) {
-                const size_t i = (size_t)t * BI + q * TPG + gt;
+                const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
                 K::load(st[q], a.p, i < a.p.ni ? i : last);
                 kzero<K>(comp(q));
             }
@@ -1084,62 +1055,35 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
 #endif
 struct Geometry {
     long long nit, njt, units, grid;
-    int jsub, wg;
+    int jsub;
     size_t rec_bytes, part_bytes, ticket_bytes, tile_bytes;
 };
 
-// Resident CTAs per SM of one instantiation (after raising its dynamic
-// shared-memory limit); cached per instantiation.
-template <class K, int JSUB, int WG>
-static int occupancy() {
+template <class K>
+static int ctas_per_sm() {
     static int cached = -1;
     if (cached < 0) {
         const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
-        cudaFuncSetAttribute(ds32_streamk<K, JSUB, WG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(ds32_streamk<K, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(ds32_streamk<K, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int n = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ds32_streamk<K, JSUB, WG>, DS_THREADS, smem) != cudaSuccess ||
-            n < 1)
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ds32_streamk<K, 1>, DS_THREADS, smem) != cudaSuccess || n < 1)
             n = 1;
         cached = n;
     }
     return cached;
 }
 
-template <class K>
-static int ctas_per_sm() {
-    occupancy<K, 2, 1>();
-    occupancy<K, 2, 4>();
-    occupancy<K, 1, 4>();
-    return occupancy<K, 1, 1>();
-}
-
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
-
-template <class K>
-static void launch_streamk(const struct Geometry &g, const DsArgs &a, size_t smem, cudaStream_t s) {
-    const unsigned grid = (unsigned)g.grid;
-    if (g.wg == 4) {
-        if (g.jsub == 2) ds32_streamk<K, 2, 4><<<grid, DS_THREADS, smem, s>>>(a);
-        else ds32_streamk<K, 1, 4><<<grid, DS_THREADS, smem, s>>>(a);
-    } else {
-        if (g.jsub == 2) ds32_streamk<K, 2, 1><<<grid, DS_THREADS, smem, s>>>(a);
-        else ds32_streamk<K, 1, 1><<<grid, DS_THREADS, smem, s>>>(a);
-    }
-}
 
 template <class K>
 static Geometry geometry(size_t ni, size_t nj, int sms) {
     Geometry g;
+    const size_t bi = (size_t)DS_THREADS * K::IPT;
+    g.nit = (long long)((ni + bi - 1) / bi);
     g.njt = (long long)((nj + DS_TILE - 1) / DS_TILE);
     const long long slots = (long long)sms * ctas_per_sm<K>();
-    // Small problems: first four warp groups per CTA (quarter-size i-tiles,
-    // if that keeps the CTAs per SM), then two parts per j-tile, until
-    // there are at least two units per CTA slot.
-    const size_t bi1 = (size_t)DS_THREADS * K::IPT;
-    const long long nit1 = (long long)((ni + bi1 - 1) / bi1);
-    g.wg = (nit1 * g.njt < 2 * slots && occupancy<K, 1, 4>() >= occupancy<K, 1, 1>()) ? 4 : 1;
-    const size_t bi = bi1 / g.wg;
-    g.nit = (long long)((ni + bi - 1) / bi);
+    // split j-tiles until there are at least two units per CTA slot
     g.jsub = 1;
     if (TG_DS32_MAX_JSUB >= 2 && g.nit * g.njt < 2 * slots) g.jsub = 2;
     g.units = g.nit * g.njt * g.jsub;
@@ -1180,7 +1124,8 @@ static cudaError_t run_ds(const PairArgs &p, void *ws, size_t ws_bytes, int sms,
     cudaError_t e = cudaMemsetAsync(a.ticket, 0, g.ticket_bytes, s);
     if (e != cudaSuccess) return e;
     const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
-    launch_streamk<K>(g, a, smem, s);
+    if (g.jsub == 2) ds32_streamk<K, 2><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
+    else ds32_streamk<K, 1><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -1217,7 +1162,8 @@ static cudaError_t run_ds_capped(const PairArgs &p, void *ws, size_t ws_bytes, i
     cudaError_t e = cudaMemsetAsync(a.ticket, 0, g.ticket_bytes, s);
     if (e != cudaSuccess) return e;
     const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
-    launch_streamk<K>(g, a, smem, s);
+    if (g.jsub == 2) ds32_streamk<K, 2><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
+    else ds32_streamk<K, 1><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
     return cudaGetLastError();
 }
 
