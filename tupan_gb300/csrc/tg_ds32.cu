@@ -198,8 +198,11 @@ struct AccDS {
             const float2 e2 = UE ? E : add2(s.e, hi2(q3));
             const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
             // 1/r^2 from y*y here: with one more MUFU per pair Acc would be
-            // XU-bound (18 packed FP32 ops vs 4 MUFU per two pairs)
-            const float2 y = inv_r<REFINE>(ss, dx, dy, dz);
+            // XU-bound (18 packed FP32 ops vs 4 MUFU per two pairs).  With a
+            // uniform softening E > 1e-20 no mask is needed: a pair at r = 0
+            // has dr = +0, so its finite m y^3 adds exactly nothing, as the
+            // masked form does.
+            const float2 y = UE ? make_float2(rsqrt_hw(ss.x), rsqrt_hw(ss.y)) : inv_r<REFINE>(ss, dx, dy, dz);
             const float2 y2 = mul2(y, y);
             const float2 mr3 = mul2(mul2(lo2(q3), y), y2);
             s.a[0] = fnma2(mr3, dx, s.a[0]);
@@ -701,7 +704,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
         float ue = __uint_as_float(0x7fc00000u);
         if constexpr (K::UE2)
             if (a.tile_e2) ue = __fadd_rn(ie2, __ldg(a.tile_e2 + (u % nju) / JSUB));
-        if (K::UE2 && ue == ue) {
+        if (K::UE2 && ue > 1e-20f) {   // NaN (not uniform) and tiny softening take the per-pair form
             const float2 E = f2(ue);
 #pragma unroll 1
             for (int fb = 0; fb < PART_PAIRS; fb += DS_FOLD_PAIRS) {
