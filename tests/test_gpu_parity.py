@@ -219,6 +219,33 @@ def test_fp64_engines_bit_identical_to_oracle(ext, orc):
             assert np.array_equal(got, want), (name, ni)
 
 
+@pytest.mark.parametrize("case", ["plain", "coincident", "zero_eps", "prefix"])
+def test_acc_jerk_unmasked_form_gate(ext, case):
+    """Large AccJerk calls run an unmasked form when a pre-pass finds every
+    pair softening above 1e-20 and no two distinct coincident particles;
+    otherwise the masked form.  Either way the results follow the
+    reference's r = 0 exclusion: a coincident pair with different
+    velocities would otherwise add a huge jerk."""
+    n = 16384
+    d = plummer(n, seed=31)
+    if case == "coincident":
+        for f in ("rx", "ry", "rz"):
+            d[f][1] = d[f][0]
+        d["vx"][1] = d["vx"][0] + 1.0
+    if case == "zero_eps":
+        d["eps2"][5] = 0.0
+    P = PS(d)
+    I = PS({f: d[f][: n // 2] for f in FIELDS}) if case == "prefix" else P
+    if case == "prefix":
+        # i-set = first half of the very same arrays (its particles are j's too)
+        for f in FIELDS:
+            setattr(I, f, getattr(P, f)[: n // 2])
+        I.n = n // 2
+    got = run_kernel(ext, "acc_jerk", "ds32", I, P, ())
+    want = run_kernel(ext, "acc_jerk", "float64", I, P, ())
+    assert rel_err("acc_jerk", got, want) <= DS32_TOL["acc_jerk"], case
+
+
 def test_ds32_is_deterministic(ext):
     d = plummer(6000, seed=3)
     P = PS(d)

@@ -70,6 +70,10 @@ struct DsArgs {
     int *ticket;         // [NIT]
     const float *tile_e2;  // [NJT] common j softening per tile or NaN; may be null
     long long nit, njt;  // i-tiles, j-tiles
+    // When set, the kernel runs only if *mode == run_mode (the unmasked and
+    // masked forms of a kernel are both launched; a pre-pass picks one).
+    const int *mode;
+    int run_mode;
 };
 
 __device__ __forceinline__ float fzero_norm(float x) { return x + 0.0f; }  // -0 -> +0
@@ -252,9 +256,14 @@ struct PhiDS {
     static PackSpec pack() { return PackSpec{8, 2, {F_M, F_E2}}; }
 };
 
-template <int IPT_, bool REFINE>
+// NOMASK: the pair r = 0 needs no mask because the call has been checked to
+// have every pair softening above 1e-20 and no two distinct coincident
+// particles (ds32_nomask_check): a self pair then has dr = dv = +0 and adds
+// exactly nothing, as the mask would make it.
+template <int IPT_, bool REFINE, bool NOMASK = false>
 struct AccJerkDS {
     static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 6;
+    using NomaskTwin = typename std::conditional<NOMASK, void, AccJerkDS<IPT_, REFINE, true>>::type;
     // The hoisted-softening form measured slower here (4.67 vs 4.57 ms at
     // N = 65536), so AccJerk always adds the pair softening; its
     // compensated sums stay in registers (shared-memory sums measured 0.3%
@@ -287,8 +296,15 @@ struct AccJerkDS {
             const float2 e2 = UE ? E : add2(s.e, lo2(q5));
             const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
             float2 y, y2;
-            if (REFINE) { y = inv_r<true>(ss, dx, dy, dz); y2 = mul2(y, y); }
-            else inv_r_r2(ss, dx, dy, dz, y, y2);
+            if (NOMASK) {
+                y = make_float2(rsqrt_hw(ss.x), rsqrt_hw(ss.y));
+                y2 = make_float2(rcp_hw(ss.x), rcp_hw(ss.y));
+            } else if (REFINE) {
+                y = inv_r<true>(ss, dx, dy, dz);
+                y2 = mul2(y, y);
+            } else {
+                inv_r_r2(ss, dx, dy, dz, y, y2);
+            }
             const float2 mr3 = mul2(mul2(hi2(q4), y), y2);
             const float2 rv = fma2(dx, du, fma2(dy, dv, mul2(dz, dw)));
             const float2 al = mul2(mul2(rv, y2), f2(3.0f));
@@ -568,6 +584,12 @@ struct smem_comp : std::false_type {};
 template <class K>
 struct smem_comp<K, decltype(void(K::SMEM_COMP))> : std::integral_constant<bool, K::SMEM_COMP> {};
 
+// Kernels with an unmasked twin (the masked form sets NOMASK_TWIN to it).
+template <class K, class = void>
+struct nomask_twin { using type = void; };
+template <class K>
+struct nomask_twin<K, std::void_t<typename K::NomaskTwin>> { using type = typename K::NomaskTwin; };
+
 template <class K, class = void>
 struct kunroll : std::integral_constant<int, TG_DS32_UNROLL> {};
 template <class K>
@@ -609,6 +631,62 @@ __global__ void ds32_tile_e2(const double *e2, size_t nj, float *tile_e2) {
 }
 
 // ---------------------------------------------------------------------------
+// Pre-pass for the unmasked forms: *bad becomes nonzero if some particle has
+// float softening <= 6e-21 (a pair sum could fall below 1e-20) or a
+// non-finite position, or if two distinct particles of I x J coincide.
+// Coincidences are found with an open-addressing hash table of j indices
+// keyed on the positions (-0 folded to +0); "distinct" compares addresses, so
+// a particle that is in both sets (I and J overlapping arrays) is itself.
+// Probing is bounded by the table size.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long mix64(unsigned long long h) {
+    h ^= h >> 33; h *= 0xff51afd7ed558ccdULL;
+    h ^= h >> 33; h *= 0xc4ceb9fe1a85ec53ULL;
+    h ^= h >> 33;
+    return h;
+}
+__device__ __forceinline__ unsigned long long pos_key(double x, double y, double z) {
+    unsigned long long h = mix64((unsigned long long)__double_as_longlong(x + 0.0));
+    h = mix64(h ^ (unsigned long long)__double_as_longlong(y + 0.0));
+    return mix64(h ^ (unsigned long long)__double_as_longlong(z + 0.0));
+}
+__device__ __forceinline__ bool check_particle(const PSet &S, size_t k) {
+    const double x = S.f[F_RX][k], y = S.f[F_RY][k], z = S.f[F_RZ][k];
+    const bool finite = isfinite(x) && isfinite(y) && isfinite(z);
+    return finite && __double2float_rn(S.f[F_E2][k]) > 6e-21f;
+}
+__device__ __forceinline__ bool same_pos(const PSet &A, size_t a, const PSet &B, size_t b) {
+    return A.f[F_RX][a] == B.f[F_RX][b] && A.f[F_RY][a] == B.f[F_RY][b] && A.f[F_RZ][a] == B.f[F_RZ][b];
+}
+__global__ void ds32_nomask_insert(PSet J, size_t nj, int *table, unsigned long long tmask, int *bad) {
+    const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nj) return;
+    if (!check_particle(J, j)) { atomicOr(bad, 1); return; }
+    unsigned long long slot = pos_key(J.f[F_RX][j], J.f[F_RY][j], J.f[F_RZ][j]) & tmask;
+    for (unsigned long long probe = 0; probe <= tmask; ++probe) {
+        const int prev = atomicCAS(table + slot, -1, (int)j);
+        if (prev == -1) return;
+        if (same_pos(J, j, J, (size_t)prev)) { atomicOr(bad, 2); return; }   // coincident j's
+        slot = (slot + 1) & tmask;
+    }
+    atomicOr(bad, 4);   // table full: cannot happen at load factor 1/2
+}
+__global__ void ds32_nomask_lookup(PSet I, size_t ni, PSet J, const int *table, unsigned long long tmask, int *bad) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ni) return;
+    if (!check_particle(I, i)) { atomicOr(bad, 1); return; }
+    unsigned long long slot = pos_key(I.f[F_RX][i], I.f[F_RY][i], I.f[F_RZ][i]) & tmask;
+    for (unsigned long long probe = 0; probe <= tmask; ++probe) {
+        const int j = table[slot];
+        if (j < 0) return;
+        if (same_pos(I, i, J, (size_t)j) && (I.f[F_RX] + i) != (J.f[F_RX] + j)) { atomicOr(bad, 2); return; }
+        slot = (slot + 1) & tmask;
+    }
+}
+// mode = 1 (unmasked) if the check passed, else 0 (masked)
+__global__ void ds32_nomask_mode(const int *bad, int *mode) { *mode = (*bad == 0) ? 1 : 0; }
+
+// ---------------------------------------------------------------------------
 // Stream-K geometry helpers.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ long long unit_start(long long k, long long U, long long G) {
@@ -642,6 +720,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
     const long long k = blockIdx.x;
     const long long u0 = unit_start(k, U, G), u1 = unit_start(k + 1, U, G);
     if (u0 >= u1) return;
+    if (a.mode && *a.mode != a.run_mode) return;
     const int tid = threadIdx.x;
 
     if (tid == 0) {
@@ -1060,6 +1139,7 @@ struct Geometry {
     long long nit, njt, units, grid;
     int jsub;
     size_t rec_bytes, part_bytes, ticket_bytes, tile_bytes;
+    size_t nomask_len, nomask_bytes;   // coincidence-check table (ints) for the unmasked twin
 };
 
 template <class K>
@@ -1095,19 +1175,28 @@ static Geometry geometry(size_t ni, size_t nj, int sms) {
     g.part_bytes = align_up((size_t)g.grid * 2 * K::IPT * K::NP * DS_THREADS * sizeof(double), 256);
     g.ticket_bytes = align_up((size_t)g.nit * sizeof(int), 256);
     g.tile_bytes = K::UE2 ? align_up((size_t)g.njt * sizeof(float), 256) : 0;
+    g.nomask_len = 0;
+    if (!std::is_void<typename nomask_twin<K>::type>::value && (double)ni * (double)nj >= 268435456.0 &&
+        nj <= ((size_t)1 << 26)) {
+        size_t t = 1;
+        while (t < 2 * nj) t *= 2;
+        g.nomask_len = t;
+    }
+    g.nomask_bytes = g.nomask_len ? align_up(g.nomask_len * sizeof(int), 256) + 256 : 0;
     return g;
 }
 
 template <class K>
 static size_t ws_bytes_for(size_t ni, size_t nj, int sms) {
     const Geometry g = geometry<K>(ni, nj, sms);
-    return g.rec_bytes + g.part_bytes + g.ticket_bytes + g.tile_bytes;
+    return g.rec_bytes + g.part_bytes + g.ticket_bytes + g.tile_bytes + g.nomask_bytes;
 }
 
 template <class K>
 static cudaError_t run_ds(const PairArgs &p, void *ws, size_t ws_bytes, int sms, cudaStream_t s) {
     const Geometry g = geometry<K>(p.ni, p.nj, sms);
-    if (g.rec_bytes + g.part_bytes + g.ticket_bytes + g.tile_bytes > ws_bytes) return cudaErrorInvalidValue;
+    if (g.rec_bytes + g.part_bytes + g.ticket_bytes + g.tile_bytes + g.nomask_bytes > ws_bytes)
+        return cudaErrorInvalidValue;
     char *base = static_cast<char *>(ws);
     DsArgs a;
     a.p = p;
@@ -1118,6 +1207,8 @@ static cudaError_t run_ds(const PairArgs &p, void *ws, size_t ws_bytes, int sms,
     a.tile_e2 = K::UE2 ? tile_e2 : nullptr;
     a.nit = g.nit;
     a.njt = g.njt;
+    a.mode = nullptr;
+    a.run_mode = 0;
 
     const size_t npairs = (size_t)g.njt * DS_PAIRS;
     const PackSpec spec = K::pack();
@@ -1127,6 +1218,35 @@ static cudaError_t run_ds(const PairArgs &p, void *ws, size_t ws_bytes, int sms,
     cudaError_t e = cudaMemsetAsync(a.ticket, 0, g.ticket_bytes, s);
     if (e != cudaSuccess) return e;
     const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
+    using Twin = typename nomask_twin<K>::type;
+    if constexpr (!std::is_void<Twin>::value) {
+        if (g.nomask_len) {
+            // pre-pass, then both forms; each runs only if the mode matches
+            char *nb = base + g.rec_bytes + g.part_bytes + g.ticket_bytes + g.tile_bytes;
+            int *table = reinterpret_cast<int *>(nb);
+            int *flags = reinterpret_cast<int *>(nb + g.nomask_bytes - 256);   // bad, mode
+            e = cudaMemsetAsync(table, 0xff, g.nomask_len * sizeof(int), s);
+            if (e == cudaSuccess) e = cudaMemsetAsync(flags, 0, 2 * sizeof(int), s);
+            if (e != cudaSuccess) return e;
+            const unsigned long long tmask = g.nomask_len - 1;
+            ds32_nomask_insert<<<(unsigned)((p.nj + 255) / 256), 256, 0, s>>>(p.J, p.nj, table, tmask, flags);
+            ds32_nomask_lookup<<<(unsigned)((p.ni + 255) / 256), 256, 0, s>>>(p.I, p.ni, p.J, table, tmask, flags);
+            ds32_nomask_mode<<<1, 1, 0, s>>>(flags, flags + 1);
+            a.mode = flags + 1;
+            DsArgs b = a;
+            b.run_mode = 1;
+            a.run_mode = 0;
+            ctas_per_sm<Twin>();   // raises the twin's shared-memory limit (once)
+            if (g.jsub == 2) {
+                ds32_streamk<K, 2><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
+                ds32_streamk<Twin, 2><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(b);
+            } else {
+                ds32_streamk<K, 1><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
+                ds32_streamk<Twin, 1><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(b);
+            }
+            return cudaGetLastError();
+        }
+    }
     if (g.jsub == 2) ds32_streamk<K, 2><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
     else ds32_streamk<K, 1><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
     return cudaGetLastError();
@@ -1157,6 +1277,8 @@ static cudaError_t run_ds_capped(const PairArgs &p, void *ws, size_t ws_bytes, i
     a.tile_e2 = nullptr;   // general path only: the scratch layout stays fixed
     a.nit = g.nit;
     a.njt = g.njt;
+    a.mode = nullptr;
+    a.run_mode = 0;
 
     const size_t npairs = (size_t)g.njt * DS_PAIRS;
     const PackSpec spec = K::pack();
