@@ -243,7 +243,9 @@ def test_acc_jerk_unmasked_form_gate(ext, case):
         I.n = n // 2
     got = run_kernel(ext, "acc_jerk", "ds32", I, P, ())
     want = run_kernel(ext, "acc_jerk", "float64", I, P, ())
-    assert rel_err("acc_jerk", got, want) <= DS32_TOL["acc_jerk"], case
+    # the split-FP32 jerk error grows with N (max ~7e-6 at N = 16384..65536);
+    # an unexcluded coincident pair would be off by orders of magnitude
+    assert rel_err("acc_jerk", got, want) <= 2e-5, case
 
 
 def test_ds32_is_deterministic(ext):
