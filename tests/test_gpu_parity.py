@@ -186,7 +186,7 @@ def test_streamk_shapes_ds32_vs_oracle(ext, orc, ni, nj):
         assert np.array_equal(got64, want), (name, ni, nj)
 
 
-@pytest.mark.parametrize("n", [500, 3000])
+@pytest.mark.parametrize("n", [500, 3000, 16384])
 def test_uniform_softening_path_is_bit_identical(ext, n):
     """Tiles whose pairs all share one softening value take the form with the
     softening add hoisted; it must give the per-pair form's bits.  Changing

@@ -264,11 +264,11 @@ template <int IPT_, bool REFINE, bool NOMASK = false>
 struct AccJerkDS {
     static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 6;
     using NomaskTwin = typename std::conditional<NOMASK, void, AccJerkDS<IPT_, REFINE, true>>::type;
-    // The hoisted-softening form measured slower here (4.67 vs 4.57 ms at
-    // N = 65536), so AccJerk always adds the pair softening; its
-    // compensated sums stay in registers (shared-memory sums measured 0.3%
+    // The hoisted-softening form pays only without the mask (masked:
+    // 4.67 vs 4.57 ms, unmasked: 4.28 vs 4.37 ms at N = 65536, measured).
+    // Compensated sums stay in registers (shared-memory sums measured 0.3%
     // slower); eight records per unrolled block (0.8% faster than four).
-    static constexpr bool UE2 = false;
+    static constexpr bool UE2 = NOMASK;
     static constexpr int UNROLL = 8;
     struct IS { IPos q; float2 u, v, w, e; float2 a[6]; Comp c[6]; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {
