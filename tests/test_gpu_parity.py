@@ -186,7 +186,7 @@ def test_streamk_shapes_ds32_vs_oracle(ext, orc, ni, nj):
         assert np.array_equal(got64, want), (name, ni, nj)
 
 
-@pytest.mark.parametrize("n", [500, 3000, 16384])
+@pytest.mark.parametrize("n", [500, 3000, 32768])
 def test_uniform_softening_path_is_bit_identical(ext, n):
     """Tiles whose pairs all share one softening value take the form with the
     softening add hoisted; it must give the per-pair form's bits.  Changing
@@ -226,7 +226,7 @@ def test_acc_jerk_unmasked_form_gate(ext, case):
     otherwise the masked form.  Either way the results follow the
     reference's r = 0 exclusion: a coincident pair with different
     velocities would otherwise add a huge jerk."""
-    n = 16384
+    n = 40000
     d = plummer(n, seed=31)
     if case == "coincident":
         for f in ("rx", "ry", "rz"):
@@ -235,12 +235,13 @@ def test_acc_jerk_unmasked_form_gate(ext, case):
     if case == "zero_eps":
         d["eps2"][5] = 0.0
     P = PS(d)
-    I = PS({f: d[f][: n // 2] for f in FIELDS}) if case == "prefix" else P
+    ni = 3 * n // 4
+    I = PS({f: d[f][:ni] for f in FIELDS}) if case == "prefix" else P
     if case == "prefix":
-        # i-set = first half of the very same arrays (its particles are j's too)
+        # i-set = the first 3/4 of the very same arrays (its particles are j's too)
         for f in FIELDS:
-            setattr(I, f, getattr(P, f)[: n // 2])
-        I.n = n // 2
+            setattr(I, f, getattr(P, f)[:ni])
+        I.n = ni
     got = run_kernel(ext, "acc_jerk", "ds32", I, P, ())
     want = run_kernel(ext, "acc_jerk", "float64", I, P, ())
     # the split-FP32 jerk error grows with N (max ~7e-6 at N = 16384..65536);

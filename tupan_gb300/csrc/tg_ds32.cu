@@ -1176,7 +1176,8 @@ static Geometry geometry(size_t ni, size_t nj, int sms) {
     g.ticket_bytes = align_up((size_t)g.nit * sizeof(int), 256);
     g.tile_bytes = K::UE2 ? align_up((size_t)g.njt * sizeof(float), 256) : 0;
     g.nomask_len = 0;
-    if (!std::is_void<typename nomask_twin<K>::type>::value && (double)ni * (double)nj >= 268435456.0 &&
+    // the pre-pass costs ~50 us (hash insert + lookup): worth it from 2^30 pairs
+    if (!std::is_void<typename nomask_twin<K>::type>::value && (double)ni * (double)nj >= 1073741824.0 &&
         nj <= ((size_t)1 << 26)) {
         size_t t = 1;
         while (t < 2 * nj) t *= 2;
