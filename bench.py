@@ -48,7 +48,7 @@ FLOP_ACC = 20       # tupan/lib/src/acc_kernel_common.h:38
 FLOP_ACC_JERK = 42  # tupan/lib/src/acc_jerk_kernel_common.h:56
 # DRAM bytes (read + write) of one split-FP32 AccJerk launch on this workload,
 # from an ncu capture (profiles/ds32_acc_jerk_n65536.txt)
-TRAFFIC_ACC_JERK_N65536 = 6.86e6
+TRAFFIC_ACC_JERK_N65536 = 6.88e6
 METRIC = "Gint/s Acc+AccJerk split-FP32 (N=65536 Plummer-Salpeter, eps2=1e-6)"
 # library kernels per step: Acc = pack + softening flags + stream-K;
 # AccJerk = pack + coincidence check (insert, lookup, mode) + the masked and
