@@ -189,6 +189,10 @@ void host_call(const HostCall &h, F launch) {
         di[f] = p; p += h.ni;
     }
     for (int f = 0; f < nf && e == cudaSuccess; ++f) {
+        if (h.nj == h.ni && h.in_j[f] == h.in_i[f]) {   // the same host array: one copy serves both
+            dj[f] = di[f];
+            continue;
+        }
         if (h.nj) e = cudaMemcpyAsync(p, h.in_j[f], h.nj * sizeof(double), cudaMemcpyHostToDevice, st.stream);
         dj[f] = p; p += h.nj;
     }
