@@ -50,10 +50,11 @@ FLOP_ACC_JERK = 42  # tupan/lib/src/acc_jerk_kernel_common.h:56
 # from an ncu capture (profiles/ds32_acc_jerk_n65536.txt)
 TRAFFIC_ACC_JERK_N65536 = 6.88e6
 METRIC = "Gint/s Acc+AccJerk split-FP32 (N=65536 Plummer-Salpeter, eps2=1e-6)"
-# library kernels per step: Acc = pack + softening flags + stream-K;
-# AccJerk = pack + coincidence check (insert, lookup, mode) + the masked and
-# unmasked stream-K forms (the one not selected exits at entry)
-LAUNCHES_PER_STEP = 9
+# library kernels per step: Acc = prepare (records, softening flags,
+# zeroed tickets) + stream-K; AccJerk = prepare + coincidence check (insert,
+# lookup, mode) + the masked and unmasked stream-K forms (the one not
+# selected exits at entry)
+LAUNCHES_PER_STEP = 8
 SMALL_SIZES = (4096, 16384)
 P5 = ("mass", "rx", "ry", "rz", "eps2")
 P8 = P5 + ("vx", "vy", "vz")

@@ -120,6 +120,62 @@ __global__ void ds32_pack(PSet J, size_t nj, size_t npairs, PackSpec ps, float *
     }
 }
 
+// Fused per-call preparation, one CTA per j-tile: the tile's records (as
+// ds32_pack), its softening flag (tile_e2[t]: the common float e2 of its
+// valid particles or NaN; skipped if tile_e2 is null), and, grid-stride, the
+// zeroed stream-K tickets, the cleared coincidence table (-1) and flags.
+struct PrepArgs {
+    int *ticket; long long nticket;
+    int *table; size_t ntable;
+    int *flags; int nflags;
+};
+__global__ void __launch_bounds__(256) ds32_prepare(PSet J, size_t nj, PackSpec ps, float *rec, float *tile_e2,
+                                                    PrepArgs z) {
+    const size_t tile = blockIdx.x;
+    for (int q = threadIdx.x; q < DS_TILE; q += blockDim.x) {
+        const size_t p = tile * DS_PAIRS + (q >> 1);
+        const int lane = q & 1;
+        const size_t j = 2 * p + lane;
+        const bool valid = j < nj;
+        float *r = rec + p * (size_t)(2 * ps.jf);
+        float h, l;
+        for (int c = 0; c < 3; ++c) {
+            split_ds(valid ? J.f[F_RX + c][j] : 0.0, h, l);
+            r[2 * (R_XH + c) + lane] = h;
+            r[2 * (R_XL + c) + lane] = l;
+        }
+        for (int e = 0; e < ps.nextra; ++e) {
+            const int f = ps.extra[e];
+            float v;
+            if (f == -1) v = valid ? 1.0f : 0.0f;
+            else if (f == -2) v = 0.0f;
+            else if (f == F_E2) v = valid ? __double2float_rn(J.f[f][j]) : 1.0f;
+            else v = valid ? __double2float_rn(J.f[f][j]) : 0.0f;
+            r[2 * (6 + e) + lane] = v;
+        }
+    }
+    if (tile_e2 != nullptr) {   // uniform softening of the tile (block-uniform branch)
+        __shared__ unsigned first;
+        const size_t j0 = tile * DS_TILE;
+        if (threadIdx.x == 0) first = __float_as_uint(__double2float_rn(J.f[F_E2][j0]));
+        __syncthreads();
+        bool same = true;
+        for (int q = threadIdx.x; q < DS_TILE; q += blockDim.x) {
+            const size_t j = j0 + q;
+            if (j < nj) same &= __float_as_uint(__double2float_rn(J.f[F_E2][j])) == first;
+        }
+        same = __syncthreads_and(same);
+        if (threadIdx.x == 0) {
+            const float v = __uint_as_float(first);
+            tile_e2[tile] = (same && v == v) ? v : __uint_as_float(0x7fc00000u);
+        }
+    }
+    const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t x = g; x < (size_t)z.nticket; x += stride) z.ticket[x] = 0;
+    for (size_t x = g; x < z.ntable; x += stride) z.table[x] = -1;
+    for (size_t x = g; x < (size_t)z.nflags; x += stride) z.flags[x] = 0;
+}
+
 // ---------------------------------------------------------------------------
 // i-side state helpers
 // ---------------------------------------------------------------------------
@@ -611,24 +667,6 @@ __device__ __forceinline__ void kzero(Comp *c) {
         for (int k = 0; k < K::NP; ++k) c[k * DS_THREADS] = Comp{0.f, 0.f};
 }
 
-// Per j-tile softening: tile_e2[t] = float(e2_j) if every valid j of tile t
-// has the same float value (bit pattern), else NaN.  One CTA per tile.
-__global__ void ds32_tile_e2(const double *e2, size_t nj, float *tile_e2) {
-    __shared__ unsigned first;
-    const size_t j0 = (size_t)blockIdx.x * DS_TILE;
-    if (threadIdx.x == 0) first = __float_as_uint(__double2float_rn(e2[j0]));
-    __syncthreads();
-    bool same = true;
-    for (int q = threadIdx.x; q < DS_TILE; q += blockDim.x) {
-        const size_t j = j0 + q;
-        if (j < nj) same &= __float_as_uint(__double2float_rn(e2[j])) == first;
-    }
-    same = __syncthreads_and(same);
-    if (threadIdx.x == 0) {
-        const float v = __uint_as_float(first);
-        tile_e2[blockIdx.x] = (same && v == v) ? v : __uint_as_float(0x7fc00000u);
-    }
-}
 
 // ---------------------------------------------------------------------------
 // Pre-pass for the unmasked forms: *bad becomes nonzero if some particle has
@@ -1211,24 +1249,17 @@ static cudaError_t run_ds(const PairArgs &p, void *ws, size_t ws_bytes, int sms,
     a.mode = nullptr;
     a.run_mode = 0;
 
-    const size_t npairs = (size_t)g.njt * DS_PAIRS;
-    const PackSpec spec = K::pack();
-    const unsigned pack_blocks = (unsigned)((npairs * 2 + 255) / 256);
-    ds32_pack<<<pack_blocks, 256, 0, s>>>(p.J, p.nj, npairs, spec, reinterpret_cast<float *>(base));
-    if (K::UE2) ds32_tile_e2<<<(unsigned)g.njt, 256, 0, s>>>(p.J.f[F_E2], p.nj, tile_e2);
-    cudaError_t e = cudaMemsetAsync(a.ticket, 0, g.ticket_bytes, s);
-    if (e != cudaSuccess) return e;
     const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
     using Twin = typename nomask_twin<K>::type;
+    char *nb = base + g.rec_bytes + g.part_bytes + g.ticket_bytes + g.tile_bytes;
+    int *table = reinterpret_cast<int *>(nb);
+    int *flags = g.nomask_len ? reinterpret_cast<int *>(nb + g.nomask_bytes - 256) : nullptr;   // bad, mode
+    PrepArgs z{a.ticket, g.nit, table, g.nomask_len, flags, g.nomask_len ? 2 : 0};
+    ds32_prepare<<<(unsigned)g.njt, 256, 0, s>>>(p.J, p.nj, K::pack(), reinterpret_cast<float *>(base),
+                                                 K::UE2 ? tile_e2 : nullptr, z);
     if constexpr (!std::is_void<Twin>::value) {
         if (g.nomask_len) {
             // pre-pass, then both forms; each runs only if the mode matches
-            char *nb = base + g.rec_bytes + g.part_bytes + g.ticket_bytes + g.tile_bytes;
-            int *table = reinterpret_cast<int *>(nb);
-            int *flags = reinterpret_cast<int *>(nb + g.nomask_bytes - 256);   // bad, mode
-            e = cudaMemsetAsync(table, 0xff, g.nomask_len * sizeof(int), s);
-            if (e == cudaSuccess) e = cudaMemsetAsync(flags, 0, 2 * sizeof(int), s);
-            if (e != cudaSuccess) return e;
             const unsigned long long tmask = g.nomask_len - 1;
             ds32_nomask_insert<<<(unsigned)((p.nj + 255) / 256), 256, 0, s>>>(p.J, p.nj, table, tmask, flags);
             ds32_nomask_lookup<<<(unsigned)((p.ni + 255) / 256), 256, 0, s>>>(p.I, p.ni, p.J, table, tmask, flags);
