@@ -481,12 +481,15 @@ struct SnapCrackleDS {
             float2 ga = fma2(fma2(f2(3.0f), vA, rJ), q2v, mul2(al, fnma2(f2(4.0f), al2, be)));
             al = mul2(al, f2(3.0f));
             ga = mul2(ga, f2(3.0f));
+            // the reference's A - (2 al v + be r) and J - (al A + be v + ga r)
+            // as chains of fused negated multiply-adds (two and three
+            // operations per component instead of three and four)
             for (int k = 0; k < 3; ++k) v[k] = fnma2(al, r[k], v[k]);
             const float2 two_al = mul2(f2(2.0f), al);
-            for (int k = 0; k < 3; ++k) A[k] = sub2(A[k], fma2(two_al, v[k], mul2(be, r[k])));
+            for (int k = 0; k < 3; ++k) A[k] = fnma2(two_al, v[k], fnma2(be, r[k], A[k]));
             al = mul2(al, f2(3.0f));
             be = mul2(be, f2(3.0f));
-            for (int k = 0; k < 3; ++k) J[k] = sub2(J[k], fma2(al, A[k], fma2(be, v[k], mul2(ga, r[k]))));
+            for (int k = 0; k < 3; ++k) J[k] = fnma2(al, A[k], fnma2(be, v[k], fnma2(ga, r[k], J[k])));
             const float2 mr3 = mul2(mul2(hi2(q7), y), q2v);
             for (int k = 0; k < 3; ++k) {
                 s.o[k] = fnma2(mr3, A[k], s.o[k]);
