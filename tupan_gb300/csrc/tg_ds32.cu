@@ -636,39 +636,19 @@ __device__ __forceinline__ void kstep(typename K::IS (&st)[K::IPT], const float4
     else K::step(st, R);
 }
 
-// Compensated sums in registers (IS member) or, for kernels that set
-// SMEM_COMP, in shared memory at comp[(q * NP + k) * DS_THREADS + tid].
-template <class K, class = void>
-struct smem_comp : std::false_type {};
-template <class K>
-struct smem_comp<K, decltype(void(K::SMEM_COMP))> : std::integral_constant<bool, K::SMEM_COMP> {};
-
 // Kernels with an unmasked twin (the masked form sets NOMASK_TWIN to it).
 template <class K, class = void>
 struct nomask_twin { using type = void; };
 template <class K>
 struct nomask_twin<K, std::void_t<typename K::NomaskTwin>> { using type = typename K::NomaskTwin; };
 
+// j-records per unrolled block: K::UNROLL if the kernel sets it, else
+// TG_DS32_UNROLL.
 template <class K, class = void>
 struct kunroll : std::integral_constant<int, TG_DS32_UNROLL> {};
 template <class K>
 struct kunroll<K, decltype(void(K::UNROLL))> : std::integral_constant<int, K::UNROLL> {};
 
-template <class K>
-__device__ __forceinline__ void kfold(typename K::IS &st, Comp *c) {
-    if constexpr (smem_comp<K>::value) K::fold(st, c);
-    else K::fold(st);
-}
-template <class K>
-__device__ __forceinline__ void kpartials(const typename K::IS &st, const Comp *c, double *p) {
-    if constexpr (smem_comp<K>::value) K::partials(st, c, p);
-    else K::partials(st, p);
-}
-template <class K>
-__device__ __forceinline__ void kzero(Comp *c) {
-    if constexpr (smem_comp<K>::value)
-        for (int k = 0; k < K::NP; ++k) c[k * DS_THREADS] = Comp{0.f, 0.f};
-}
 
 
 // ---------------------------------------------------------------------------
@@ -749,8 +729,6 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
     constexpr int TILE_Q = DS_PAIRS * K::NQ;
     constexpr int BI = DS_THREADS * IPT;   // i-particles per i-tile
     constexpr int UNR = kunroll<K>::value;
-    __shared__ Comp s_comp[smem_comp<K>::value ? IPT * K::NP * DS_THREADS : 1];
-    auto comp = [&](int q) { return s_comp + q * K::NP * DS_THREADS + threadIdx.x; };
     // JSUB parts per j-tile (1 or 2): a unit is an i-tile x one part
     constexpr int PART_PAIRS = DS_PAIRS / JSUB;
     constexpr int PART_Q = PART_PAIRS * K::NQ;
@@ -786,7 +764,6 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
     for (int q = 0; q < IPT; ++q) {
         const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
         K::load(st[q], a.p, i < a.p.ni ? i : last);
-        kzero<K>(comp(q));
     }
     // i-tile softening: the common float(ie2) of the tile, or NaN
     __shared__ unsigned s_ie2;
@@ -831,7 +808,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
 #pragma unroll UNR
                 for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, true>(st, R + (fb + pp) * K::NQ, E);
 #pragma unroll
-                for (int q = 0; q < IPT; ++q) kfold<K>(st[q], comp(q));
+                for (int q = 0; q < IPT; ++q) K::fold(st[q]);
             }
         } else {
 #pragma unroll 1
@@ -839,7 +816,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
 #pragma unroll UNR
                 for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, false>(st, R + (fb + pp) * K::NQ, f2(0.f));
 #pragma unroll
-                for (int q = 0; q < IPT; ++q) kfold<K>(st[q], comp(q));
+                for (int q = 0; q < IPT; ++q) K::fold(st[q]);
             }
         }
         __syncthreads();   // stage s fully consumed
@@ -857,7 +834,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
             for (int q = 0; q < IPT; ++q) {
                 const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
                 double p[K::NP];
-                kpartials<K>(st[q], comp(q), p);
+                K::partials(st[q], p);
                 if (i < a.p.ni) K::store(p, a.p, i);
             }
         } else {
@@ -866,7 +843,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
 #pragma unroll
             for (int q = 0; q < IPT; ++q) {
                 double p[K::NP];
-                kpartials<K>(st[q], comp(q), p);
+                K::partials(st[q], p);
                 for (int v = 0; v < K::NP; ++v) mine[(q * K::NP + v) * DS_THREADS + tid] = p[v];
             }
             __threadfence();
@@ -922,7 +899,6 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
             for (int q = 0; q < IPT; ++q) {
                 const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
                 K::load(st[q], a.p, i < a.p.ni ? i : last);
-                kzero<K>(comp(q));
             }
             ie2 = tile_ie2();
         }
@@ -1040,15 +1016,12 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
     long long t = tile_of(c, u0);
     const long long git_first = a.itile_off[c] + t;
     typename K::IS st[IPT];
-    __shared__ Comp s_comp[smem_comp<K>::value ? IPT * K::NP * DS_THREADS : 1];
-    auto comp = [&](int q) { return s_comp + q * K::NP * DS_THREADS + threadIdx.x; };
     auto load_tile = [&](long long cl, long long tt) {
 #pragma unroll
         for (int q = 0; q < IPT; ++q) {
             const long long li = tt * BI + q * DS_THREADS + tid;
             const size_t i = (size_t)(a.seg_start[cl] + (li < a.seg_n[cl] ? li : 0));
             K::load(st[q], a.p, i);
-            kzero<K>(comp(q));
         }
     };
     load_tile(c, t);
@@ -1071,7 +1044,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
 #pragma unroll UNR
             for (int pp = 0; pp < DS_FOLD_PAIRS; ++pp) kstep<K, false>(st, R + (fb + pp) * K::NQ, f2(0.f));
 #pragma unroll
-            for (int q = 0; q < IPT; ++q) kfold<K>(st[q], comp(q));
+            for (int q = 0; q < IPT; ++q) K::fold(st[q]);
         }
         __syncthreads();
         if (tid == 0 && u + DS_STAGES < u1) {
@@ -1094,7 +1067,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
             for (int q = 0; q < IPT; ++q) {
                 const long long li = t * BI + q * DS_THREADS + tid;
                 double p[K::NP];
-                kpartials<K>(st[q], comp(q), p);
+                K::partials(st[q], p);
                 if (li < a.seg_n[c]) K::store(p, a.p, (size_t)(a.seg_start[c] + li));
             }
         } else {
@@ -1103,7 +1076,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
 #pragma unroll
             for (int q = 0; q < IPT; ++q) {
                 double p[K::NP];
-                kpartials<K>(st[q], comp(q), p);
+                K::partials(st[q], p);
                 for (int v = 0; v < K::NP; ++v) mine[(q * K::NP + v) * DS_THREADS + tid] = p[v];
             }
             __threadfence();
