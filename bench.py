@@ -206,8 +206,8 @@ def rel_errors(got, want):
 
 def small_sizes(dev, sp):
     """Acc and AccJerk at N = 4096 and 16384 (same workload family): median
-    CUDA-event time of split FP32 and FP64 calls and the split-FP32 force
-    error against FP64."""
+    CUDA-event time of 21 split FP32 and 21 FP64 calls (after one untimed
+    call) and the split-FP32 force error against FP64."""
     import torch
     from tupan_gb300 import _native
     out = {}
@@ -217,7 +217,7 @@ def small_sizes(dev, sp):
         rec = {}
         res = {}
         for name, fields, no in (("acc", P5, 3), ("acc_jerk", P8, 6)):
-            for prec, pname, reps in ((_native.PREC_DS32, "ds32", 7), (_native.PREC_FP64, "fp64", 3)):
+            for prec, pname, reps in ((_native.PREC_DS32, "ds32", 21), (_native.PREC_FP64, "fp64", 21)):
                 o = [torch.empty(n, dtype=torch.float64, device=dev) for _ in range(no)]
 
                 def call():
@@ -387,6 +387,9 @@ def ours(args, rank, world, dist):
                    "path": "acc_kernel + acc_jerk_kernel (libtupan.h signatures), pinned host buffers"}
     if rank == 0:
         line["cpu_baseline"] = cpu_sample(d, args.cpu_seconds, os.cpu_count() or 1)
+        one = cpu_sample(d, min(args.cpu_seconds, 2.0), 1)
+        line["cpu_baseline"]["single_core"] = {"value": one["value"], "unit": one["unit"],
+                                               "sample": one["sample"]}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
