@@ -1180,9 +1180,16 @@ static Geometry geometry(size_t ni, size_t nj, int sms) {
     g.nit = (long long)((ni + bi - 1) / bi);
     g.njt = (long long)((nj + DS_TILE - 1) / DS_TILE);
     const long long slots = (long long)sms * ctas_per_sm<K>();
-    // split j-tiles until there are at least two units per CTA slot
+    // Split j-tiles in two when there are fewer than two units per CTA slot,
+    // or when halving the units evens out the CTAs' shares by 10% or more:
+    // a CTA's time is its whole-unit count, ceil(U / slots) units of size
+    // 1 / jsub (N = 16384, AccJerk: 4 whole units per CTA, or 7 halves).
     g.jsub = 1;
-    if (TG_DS32_MAX_JSUB >= 2 && g.nit * g.njt < 2 * slots) g.jsub = 2;
+    if (TG_DS32_MAX_JSUB >= 2) {
+        const long long u = g.nit * g.njt;
+        const double t1 = (double)((u + slots - 1) / slots), t2 = 0.5 * (double)((2 * u + slots - 1) / slots);
+        if (u < 2 * slots || t2 <= 0.9 * t1) g.jsub = 2;
+    }
     g.units = g.nit * g.njt * g.jsub;
     g.grid = g.units < slots ? g.units : slots;
     g.rec_bytes = align_up((size_t)g.njt * DS_PAIRS * K::NQ * sizeof(float4), 256);
