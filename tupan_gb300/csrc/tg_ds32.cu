@@ -120,52 +120,49 @@ __global__ void ds32_pack(PSet J, size_t nj, size_t npairs, PackSpec ps, float *
     }
 }
 
-// Fused per-call preparation, one CTA per j-tile: the tile's records (as
-// ds32_pack), its softening flag (tile_e2[t]: the common float e2 of its
-// valid particles or NaN; skipped if tile_e2 is null), and, grid-stride, the
-// zeroed stream-K tickets, the cleared coincidence table (-1) and flags.
+// Fused per-call preparation, one CTA of DS_TILE threads per j-tile, one j
+// per thread: the tile's records (as ds32_pack), its softening flag
+// (tile_e2[t]: the common float e2 of its valid particles or NaN; skipped if
+// tile_e2 is null), and, grid-stride, the zeroed stream-K tickets, the
+// cleared coincidence table (-1) and flags.  Every thread issues its loads
+// at once, so the launch costs about one memory round trip.
 struct PrepArgs {
     int *ticket; long long nticket;
     int *table; size_t ntable;
     int *flags; int nflags;
 };
-__global__ void __launch_bounds__(256) ds32_prepare(PSet J, size_t nj, PackSpec ps, float *rec, float *tile_e2,
-                                                    PrepArgs z) {
+__global__ void __launch_bounds__(DS_TILE) ds32_prepare(PSet J, size_t nj, PackSpec ps, float *rec, float *tile_e2,
+                                                        PrepArgs z) {
     const size_t tile = blockIdx.x;
-    for (int q = threadIdx.x; q < DS_TILE; q += blockDim.x) {
-        const size_t p = tile * DS_PAIRS + (q >> 1);
-        const int lane = q & 1;
-        const size_t j = 2 * p + lane;
-        const bool valid = j < nj;
-        float *r = rec + p * (size_t)(2 * ps.jf);
-        float h, l;
-        for (int c = 0; c < 3; ++c) {
-            split_ds(valid ? J.f[F_RX + c][j] : 0.0, h, l);
-            r[2 * (R_XH + c) + lane] = h;
-            r[2 * (R_XL + c) + lane] = l;
-        }
-        for (int e = 0; e < ps.nextra; ++e) {
-            const int f = ps.extra[e];
-            float v;
-            if (f == -1) v = valid ? 1.0f : 0.0f;
-            else if (f == -2) v = 0.0f;
-            else if (f == F_E2) v = valid ? __double2float_rn(J.f[f][j]) : 1.0f;
-            else v = valid ? __double2float_rn(J.f[f][j]) : 0.0f;
-            r[2 * (6 + e) + lane] = v;
-        }
+    const int q = threadIdx.x;
+    const size_t p = tile * DS_PAIRS + (q >> 1);
+    const int lane = q & 1;
+    const size_t j = 2 * p + lane;
+    const bool valid = j < nj;
+    float *r = rec + p * (size_t)(2 * ps.jf);
+    float h, l;
+    for (int c = 0; c < 3; ++c) {
+        split_ds(valid ? J.f[F_RX + c][j] : 0.0, h, l);
+        r[2 * (R_XH + c) + lane] = h;
+        r[2 * (R_XL + c) + lane] = l;
+    }
+    for (int e = 0; e < ps.nextra; ++e) {
+        const int f = ps.extra[e];
+        float v;
+        if (f == -1) v = valid ? 1.0f : 0.0f;
+        else if (f == -2) v = 0.0f;
+        else if (f == F_E2) v = valid ? __double2float_rn(J.f[f][j]) : 1.0f;
+        else v = valid ? __double2float_rn(J.f[f][j]) : 0.0f;
+        r[2 * (6 + e) + lane] = v;
     }
     if (tile_e2 != nullptr) {   // uniform softening of the tile (block-uniform branch)
+        // the tile's first particle, j = tile * DS_TILE, is always valid
         __shared__ unsigned first;
-        const size_t j0 = tile * DS_TILE;
-        if (threadIdx.x == 0) first = __float_as_uint(__double2float_rn(J.f[F_E2][j0]));
+        const unsigned mine = valid ? __float_as_uint(__double2float_rn(J.f[F_E2][j])) : 0u;
+        if (q == 0) first = mine;
         __syncthreads();
-        bool same = true;
-        for (int q = threadIdx.x; q < DS_TILE; q += blockDim.x) {
-            const size_t j = j0 + q;
-            if (j < nj) same &= __float_as_uint(__double2float_rn(J.f[F_E2][j])) == first;
-        }
-        same = __syncthreads_and(same);
-        if (threadIdx.x == 0) {
+        const bool same = __syncthreads_and(!valid || mine == first);
+        if (q == 0) {
             const float v = __uint_as_float(first);
             tile_e2[tile] = (same && v == v) ? v : __uint_as_float(0x7fc00000u);
         }
@@ -1238,7 +1235,7 @@ static cudaError_t run_ds(const PairArgs &p, void *ws, size_t ws_bytes, int sms,
     int *table = reinterpret_cast<int *>(nb);
     int *flags = g.nomask_len ? reinterpret_cast<int *>(nb + g.nomask_bytes - 256) : nullptr;   // bad, mode
     PrepArgs z{a.ticket, g.nit, table, g.nomask_len, flags, g.nomask_len ? 2 : 0};
-    ds32_prepare<<<(unsigned)g.njt, 256, 0, s>>>(p.J, p.nj, K::pack(), reinterpret_cast<float *>(base),
+    ds32_prepare<<<(unsigned)g.njt, DS_TILE, 0, s>>>(p.J, p.nj, K::pack(), reinterpret_cast<float *>(base),
                                                  K::UE2 ? tile_e2 : nullptr, z);
     if constexpr (!std::is_void<Twin>::value) {
         if (g.nomask_len) {
@@ -1383,15 +1380,35 @@ static cudaError_t run_ds_seg(const PairArgs &p, const SegGeometry &g, void *ws,
 constexpr bool REF = TG_DS32_REFINE != 0;
 constexpr int IPT2 = TG_DS32_IPT;
 
+// Small problems take the one-i-per-thread instance K1 (256-particle
+// i-tiles) of a kernel whose default instance K2 holds two: when even
+// half-size units leave CTA slots empty, smaller i-tiles give twice the
+// units, each half as long (N = 4096: 256 units instead of 128).
+template <class K2, class K1>
+static bool small_pick(size_t ni, size_t nj, int sms) {
+    if (K2::IPT == K1::IPT) return false;
+    const Geometry g = geometry<K2>(ni, nj, sms);
+    return g.units < (long long)sms * ctas_per_sm<K2>();
+}
+template <class K2, class K1>
+static size_t ws_pick(size_t ni, size_t nj, int sms) {
+    return small_pick<K2, K1>(ni, nj, sms) ? ws_bytes_for<K1>(ni, nj, sms) : ws_bytes_for<K2>(ni, nj, sms);
+}
+template <class K2, class K1>
+static cudaError_t run_pick(const PairArgs &a, void *ws, size_t ws_bytes, int sms, cudaStream_t s) {
+    return small_pick<K2, K1>(a.ni, a.nj, sms) ? run_ds<K1>(a, ws, ws_bytes, sms, s)
+                                               : run_ds<K2>(a, ws, ws_bytes, sms, s);
+}
+
 bool ds32_supported(int kernel) { return kernel != K_SAKURA && kernel >= 0 && kernel < K_COUNT; }
 
 size_t ds32_workspace_bytes(int kernel, size_t ni, size_t nj, int sms) {
     switch (kernel) {
-        case K_PHI: return ws_bytes_for<PhiDS<IPT2, REF>>(ni, nj, sms);
-        case K_ACC: return ws_bytes_for<AccDS<IPT2, REF>>(ni, nj, sms);
-        case K_ACC_JERK: return ws_bytes_for<AccJerkDS<IPT2, REF>>(ni, nj, sms);
+        case K_PHI: return ws_pick<PhiDS<IPT2, REF>, PhiDS<1, REF>>(ni, nj, sms);
+        case K_ACC: return ws_pick<AccDS<IPT2, REF>, AccDS<1, REF>>(ni, nj, sms);
+        case K_ACC_JERK: return ws_pick<AccJerkDS<IPT2, REF>, AccJerkDS<1, REF>>(ni, nj, sms);
         case K_SNAP_CRACKLE: return ws_bytes_for<SnapCrackleDS<1, REF>>(ni, nj, sms);
-        case K_TSTEP: return ws_bytes_for<TstepDS<IPT2, REF>>(ni, nj, sms);
+        case K_TSTEP: return ws_pick<TstepDS<IPT2, REF>, TstepDS<1, REF>>(ni, nj, sms);
         case K_PNACC: return ws_bytes_for<PNAccDS<1, REF>>(ni, nj, sms);
         case K_ACC_VJP: return ws_bytes_for<AccVjpDS<IPT2, REF>>(ni, nj, sms);
         default: return 0;
@@ -1400,11 +1417,11 @@ size_t ds32_workspace_bytes(int kernel, size_t ni, size_t nj, int sms) {
 
 cudaError_t launch_ds32(int kernel, const PairArgs &a, void *ws, size_t ws_bytes, int sms, cudaStream_t s) {
     switch (kernel) {
-        case K_PHI: return run_ds<PhiDS<IPT2, REF>>(a, ws, ws_bytes, sms, s);
-        case K_ACC: return run_ds<AccDS<IPT2, REF>>(a, ws, ws_bytes, sms, s);
-        case K_ACC_JERK: return run_ds<AccJerkDS<IPT2, REF>>(a, ws, ws_bytes, sms, s);
+        case K_PHI: return run_pick<PhiDS<IPT2, REF>, PhiDS<1, REF>>(a, ws, ws_bytes, sms, s);
+        case K_ACC: return run_pick<AccDS<IPT2, REF>, AccDS<1, REF>>(a, ws, ws_bytes, sms, s);
+        case K_ACC_JERK: return run_pick<AccJerkDS<IPT2, REF>, AccJerkDS<1, REF>>(a, ws, ws_bytes, sms, s);
         case K_SNAP_CRACKLE: return run_ds<SnapCrackleDS<1, REF>>(a, ws, ws_bytes, sms, s);
-        case K_TSTEP: return run_ds<TstepDS<IPT2, REF>>(a, ws, ws_bytes, sms, s);
+        case K_TSTEP: return run_pick<TstepDS<IPT2, REF>, TstepDS<1, REF>>(a, ws, ws_bytes, sms, s);
         case K_PNACC: return run_ds<PNAccDS<1, REF>>(a, ws, ws_bytes, sms, s);
         case K_ACC_VJP: return run_ds<AccVjpDS<IPT2, REF>>(a, ws, ws_bytes, sms, s);
         default: return cudaErrorInvalidValue;
