@@ -70,6 +70,14 @@ int tg_device_sms(void);
  * with scalar FFMA (which = 2); negative on error.  It is
  * the measured denominator of the pairwise kernels' FP32 roofline. */
 double tg_probe_fma_tflops(int which, int iters, void *stream);
+/* Failure-detection check with no counterpart in the reference: one CTA
+ * waits on a shared-memory barrier with the bounded poll the split-FP32
+ * kernels use for their j-tile copies (`polls` polls; the kernels use
+ * 2^18, about one second), and the barrier completes only if `arrive` is nonzero.  Returns the
+ * status bits the wait raised (TG_ST_MBAR_TIMEOUT if it gave up, else 0) or
+ * a negative TG_E* code, and stores the kernel time in *ms.  Synchronous,
+ * default stream. */
+int tg_check_bounded_wait(unsigned polls, int arrive, double *ms);
 
 /* ---------------------------------------------------------------------- */
 /* Device entry points (device pointers, asynchronous on `stream`)         */

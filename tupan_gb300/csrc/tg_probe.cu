@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/tupan_gb300.h"
+#include "tg_device.cuh"
 
 namespace {
 
@@ -60,9 +61,50 @@ __global__ void probe_fp64(double *sink, int iters, double a, double b) {
     if (s == 12345.678) sink[blockIdx.x] = s;
 }
 
+// One CTA waits, with the pairwise kernels' bounded poll, on an mbarrier
+// that expects one arrival; thread 0 arrives only if `arrive` is set.  A wait
+// that gives up raises TG_ST_MBAR_TIMEOUT in *status, as the split-FP32
+// kernels do when a j-tile copy never completes.
+__global__ void bounded_wait(unsigned polls, int arrive, unsigned *status) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        tg::mbar_init(&bar, 1);
+        tg::fence_mbar_init();
+    }
+    __syncthreads();
+    if (arrive && threadIdx.x == 0) tg::mbar_expect_tx(&bar, 0);   // an arrival with no bytes
+    const bool ok = tg::mbar_wait(&bar, 0, polls);
+    if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicOr(status, TG_ST_MBAR_TIMEOUT);
+}
+
 }  // namespace
 
 extern "C" {
+
+// Runs bounded_wait once on the current device and returns the status bits
+// it raised (0 or TG_ST_MBAR_TIMEOUT), or a negative TG_E* code; *ms gets
+// the kernel's duration.
+int tg_check_bounded_wait(unsigned polls, int arrive, double *ms) {
+    unsigned *d = nullptr, h = 0;
+    if (cudaMalloc(&d, sizeof(unsigned)) != cudaSuccess) return TG_ENOMEM;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaMemset(d, 0, sizeof(unsigned));
+    cudaEventRecord(e0, 0);
+    bounded_wait<<<1, 32>>>(polls, arrive, d);
+    cudaEventRecord(e1, 0);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float t = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+    if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d);
+    if (e != cudaSuccess) return TG_ECUDA;
+    if (ms) *ms = t;
+    return (int)h;
+}
 
 // Measured dense FMA throughput in TFLOP/s (2 flops per FMA) for FP32
 // (which = 0) or FP64 (which = 1) on the current device; negative on error.
