@@ -62,6 +62,12 @@ int tg_sync_status(void *stream);
 /* Precision used by the drop-in host entry points (process-wide). */
 int tg_set_host_precision(int prec);
 int tg_get_host_precision(void);
+/* Sakura evaluation (no counterpart in the reference; process-wide): 1, the
+ * default, solves the pairs that take the universal-variable Kepler solver
+ * apart from the others (flags -1 and +1, ni * nj <= 2^30; uses the grow-only
+ * workspace); 0 evaluates every pair in one pass and allocates nothing.  Both
+ * return the same bits.  Returns the previous setting. */
+int tg_set_sakura_split(int on);
 /* Streaming multiprocessors of the current device (0 if none). */
 int tg_device_sms(void);
 /* Measurement helper with no counterpart in the reference: dense FMA issue

@@ -91,6 +91,8 @@ def _load():
     lib.tg_acc_vjp.argtypes = [ctypes.c_size_t] + [_DP] * 12 + [ctypes.c_int, _DP]
     lib.tg_probe_fma_tflops.restype = ctypes.c_double
     lib.tg_probe_fma_tflops.argtypes = [ctypes.c_int, ctypes.c_int, _DP]
+    lib.tg_set_sakura_split.restype = ctypes.c_int
+    lib.tg_set_sakura_split.argtypes = [ctypes.c_int]
     lib.tg_check_bounded_wait.restype = ctypes.c_int
     lib.tg_check_bounded_wait.argtypes = [ctypes.c_uint, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
     lib.tg_div3.restype = ctypes.c_int

@@ -5,6 +5,7 @@
 // the drop-in host entry points with the reference's libtupan.h signatures.
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <algorithm>
 #include <string>
@@ -40,6 +41,8 @@ struct DevCtx {
     unsigned *status = nullptr;   // device word, sticky until tg_sync_status
 };
 DevCtx g_dev[MAX_DEV];
+// Sakura evaluation: 1 = Kepler pairs solved apart, 0 = one pass (tg_set_sakura_split)
+std::atomic<int> g_sakura_split{1};
 
 int current_ctx(DevCtx **out) {
     int dev = 0;
@@ -103,7 +106,13 @@ int run(int kernel, tg::PairArgs &a, int prec, void *stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     a.status = c->status;
     cudaError_t e;
-    if (prec == TG_PREC_FP64 || !tg::ds32_supported(kernel) || a.nj == 0) {
+    if (kernel == tg::K_SAKURA && g_sakura_split.load() && tg::sakura_split_applies(a)) {
+        // FP64 whatever `prec` asks; the Kepler pairs are solved apart
+        std::lock_guard<std::mutex> lk(c->mu);
+        rc = ensure_ws(*c, tg::sakura_split_ws_bytes(a.ni, a.nj), s);
+        if (rc != TG_OK) return rc;
+        e = tg::launch_sakura_split(a, c->ws, c->ws_bytes, c->sms, s);
+    } else if (prec == TG_PREC_FP64 || !tg::ds32_supported(kernel) || a.nj == 0) {
         e = tg::launch_fp64(kernel, a, c->sms, s);
     } else {
         std::lock_guard<std::mutex> lk(c->mu);
@@ -245,6 +254,8 @@ int tg_set_host_precision(int prec) {
     return TG_OK;
 }
 int tg_get_host_precision(void) { return g_host_prec; }
+
+int tg_set_sakura_split(int on) { return g_sakura_split.exchange(on ? 1 : 0); }
 
 int tg_phi(size_t ni, const double *im, const double *irx, const double *iry, const double *irz,
            const double *ie2, size_t nj, const double *jm, const double *jrx, const double *jry,

@@ -234,19 +234,42 @@ struct Sakura64 {
         for (int k = 0; k < 8; ++k) s.f[k] = a.I.f[k][i];
         for (int k = 0; k < NT; ++k) s.acc[k] = 0.0;
     }
-    // A pair that reaches a retry bound raises its status bit here (rare).
-    __device__ static void terms(const St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a, double *t) {
-        double r0[3], v0[3], r1[3], v1[3];
+    // The pair state (i minus j) and the mass-weighted deltas of one pair;
+    // a pair that reaches a retry bound raises its status bit (rare).
+    __device__ static void state(const double *fi, const double *fj, double r0[3], double v0[3],
+                                 double &e2, double &m) {
         for (int k = 0; k < 3; ++k) {
-            r0[k] = dsub(s.f[F_RX + k], sj[F_RX + k][jj]);
-            v0[k] = dsub(s.f[F_VX + k], sj[F_VX + k][jj]);
+            r0[k] = dsub(fi[F_RX + k], fj[F_RX + k]);
+            v0[k] = dsub(fi[F_VX + k], fj[F_VX + k]);
         }
-        double e2 = dadd(s.f[F_E2], sj[F_E2][jj]);
-        double m = dadd(s.f[F_M], sj[F_M][jj]);
+        e2 = dadd(fi[F_E2], fj[F_E2]);
+        m = dadd(fi[F_M], fj[F_M]);
+    }
+    __device__ static void pair_terms(const double *fi, const double *fj, const PairArgs &a, double *t) {
+        double r0[3], v0[3], r1[3], v1[3], e2, m;
+        state(fi, fj, r0, v0, e2, m);
         KepBudget b;
         pair_evolve(a.dt, a.flag, m, e2, r0, v0, r1, v1, b);
         if (b.flags) atomicOr(a.status, b.flags);
-        double w = ddiv(sj[F_M][jj], m);
+        double w = ddiv(fj[F_M], m);
+        for (int k = 0; k < 3; ++k) {
+            t[k] = dmul(w, dsub(r1[k], r0[k]));
+            t[3 + k] = dmul(w, dsub(v1[k], v0[k]));
+        }
+    }
+    __device__ static void terms(const St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a, double *t) {
+        double fj[8];
+        for (int k = 0; k < 8; ++k) fj[k] = sj[k][jj];
+        pair_terms(s.f, fj, a, t);
+    }
+    // pair_terms of a pair known to take the leapfrog branch (flag -1 or +1)
+    __device__ static void terms_leapfrog(const St &s, const double (*sj)[F64_TILE], int jj, const PairArgs &a,
+                                          double *t) {
+        double fj[8], r0[3], v0[3], r1[3], v1[3], e2, m;
+        for (int k = 0; k < 8; ++k) fj[k] = sj[k][jj];
+        state(s.f, fj, r0, v0, e2, m);
+        pair_evolve_leapfrog(a.dt, a.flag, m, e2, r0, v0, r1, v1);
+        double w = ddiv(fj[F_M], m);
         for (int k = 0; k < 3; ++k) {
             t[k] = dmul(w, dsub(r1[k], r0[k]));
             t[3 + k] = dmul(w, dsub(v1[k], v0[k]));
@@ -604,6 +627,209 @@ static cudaError_t run(const PairArgs &a, int sms, cudaStream_t s) {
     const unsigned t = fp64_threads(a.ni, sms);
     const size_t blocks = (a.ni + t - 1) / t;
     fp64_pairwise<K><<<(unsigned)blocks, t, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Sakura with its Kepler pairs solved apart (flags -1 and +1).
+//
+// The pairs whose two-body step takes the universal-variable solver (the
+// branch of sakura_kernel_common.h:111-122) are a few percent of all pairs,
+// but in the warp engine each one holds the 31 other lanes of its round for
+// the whole solve.  Here
+//   1. sakura_mark tests every pair (twobody_uses_kepler, the solver's own
+//      test) and writes one bitmap row of j per i and the row's count;
+//   2. sakura_scan turns the counts into row offsets;
+//   3. sakura_solve evolves the marked pairs, one per thread, and stores
+//      their six terms in row order;
+//   4. sakura_fold walks j in order like the warp engine, evolving leapfrog
+//      pairs inline and reading the marked pairs' terms back,
+// so every output is the same sum, in the same order, of the same terms as
+// the one-pass kernel: bit-identical.  Marked pairs beyond the term buffer's
+// capacity are evolved inline in step 4.
+// ---------------------------------------------------------------------------
+constexpr int SAK_WARPS = F64W_THREADS / 32;
+
+__global__ void __launch_bounds__(F64W_THREADS) sakura_mark(PairArgs a, unsigned *bits, size_t W,
+                                                           long long *count) {
+    const int warp = threadIdx.x / 32, l = threadIdx.x % 32;
+    const size_t i = (size_t)blockIdx.x * SAK_WARPS + warp;
+    if (i >= a.ni) return;   // warp-uniform
+    double fi[8], fj[8];
+    for (int k = 0; k < 8; ++k) fi[k] = a.I.f[k][i];
+    long long cnt = 0;
+    for (size_t w = 0; w < W; ++w) {
+        const size_t j = w * 32 + l;
+        bool kep = false;
+        if (j < a.nj) {
+            for (int k = 0; k < 8; ++k) fj[k] = a.J.f[k][j];
+            double r0[3], v0[3], e2, m;
+            Sakura64::state(fi, fj, r0, v0, e2, m);
+            kep = sakura_uses_kepler(a.dt, a.flag, m, r0, v0);
+        }
+        const unsigned b = __ballot_sync(0xffffffffu, kep);
+        if (l == 0) bits[i * W + w] = b;
+        cnt += __popc(b);
+    }
+    if (l == 0) count[i] = cnt;
+}
+
+// Exclusive scan of count[0, n) into off[0, n]; one CTA, each thread a
+// contiguous chunk.
+__global__ void __launch_bounds__(1024) sakura_scan(const long long *count, size_t n, long long *off) {
+    __shared__ long long part[1024];
+    const size_t chunk = (n + blockDim.x - 1) / blockDim.x;
+    const size_t a0 = threadIdx.x * chunk, a1 = (a0 + chunk < n) ? a0 + chunk : n;
+    long long sum = 0;
+    for (size_t q = a0; q < a1; ++q) sum += count[q];
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (int d = 1; d < (int)blockDim.x; d *= 2) {   // inclusive Hillis-Steele scan
+        const long long v = threadIdx.x >= (unsigned)d ? part[threadIdx.x - d] : 0;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    long long run = part[threadIdx.x] - sum;
+    for (size_t q = a0; q < a1; ++q) { off[q] = run; run += count[q]; }
+    if (threadIdx.x == blockDim.x - 1) off[n] = part[threadIdx.x];
+}
+
+// Marked pair number e (row i, rank e - off[i] within the row), one per
+// thread, grid-stride; entries from `cap` on are left to sakura_fold.
+__global__ void sakura_solve(PairArgs a, const unsigned *bits, size_t W, const long long *off,
+                             double *terms, long long cap) {
+    const long long total = off[a.ni];
+    const long long n = total < cap ? total : cap;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        size_t lo = 0, hi = a.ni;   // last row with off[row] <= e
+        while (hi - lo > 1) {
+            const size_t mid = (lo + hi) / 2;
+            if (off[mid] <= e) lo = mid; else hi = mid;
+        }
+        const size_t i = lo;
+        long long rank = e - off[i];
+        size_t j = 0;
+        for (size_t w = 0; w < W; ++w) {
+            unsigned b = bits[i * W + w];
+            const int p = __popc(b);
+            if (rank < p) {
+                for (long long q = 0; q < rank; ++q) b &= b - 1u;   // drop the lower set bits
+                j = w * 32 + (size_t)(__ffs(b) - 1);
+                break;
+            }
+            rank -= p;
+        }
+        double fi[8], fj[8], t[6];
+        for (int k = 0; k < 8; ++k) { fi[k] = a.I.f[k][i]; fj[k] = a.J.f[k][j]; }
+        Sakura64::pair_terms(fi, fj, a, t);
+        for (int k = 0; k < 6; ++k) terms[e * 6 + k] = t[k];
+    }
+}
+
+// The warp engine with one i per warp (32 consecutive j per round, one
+// bitmap word), the marked pairs' terms read back in row order.
+#ifndef TG_SAKURA_FOLD_MINB
+#define TG_SAKURA_FOLD_MINB 3
+#endif
+__global__ void __launch_bounds__(F64W_THREADS, TG_SAKURA_FOLD_MINB) sakura_fold(PairArgs a, const unsigned *bits, size_t W,
+                                                           const long long *off, const double *terms,
+                                                           long long cap) {
+    using K = Sakura64;
+    __shared__ double sj[K::NF][F64_TILE];
+    __shared__ double tt[SAK_WARPS][K::NT][33];
+    const int warp = threadIdx.x / 32, l = threadIdx.x % 32;
+    const size_t i = (size_t)blockIdx.x * SAK_WARPS + warp;
+    const bool live = i < a.ni;
+    K::St st;
+    K::init(st, a, live ? i : 0);
+    double acc = 0.0;
+    long long e = live ? off[i] : 0;   // the row's next marked pair
+    for (size_t j0 = 0; j0 < a.nj; j0 += F64_TILE) {
+        const int nt = (int)((a.nj - j0) < (size_t)F64_TILE ? (a.nj - j0) : F64_TILE);
+        for (int q = threadIdx.x; q < K::NF * F64_TILE; q += blockDim.x) {
+            const int f = q / F64_TILE, jj = q % F64_TILE;
+            if (jj < nt) sj[f][jj] = a.J.f[f][j0 + jj];
+        }
+        __syncthreads();
+        for (int r = 0; r < nt; r += 32) {
+            const unsigned word = live ? bits[i * W + (j0 + r) / 32] : 0u;
+            if (r + l < nt) {
+                double t[K::NT];
+                const long long mine = e + __popc(word & ((1u << l) - 1u));
+                if (!((word >> l) & 1u)) {
+                    K::terms_leapfrog(st, sj, r + l, a, t);
+                } else if (mine < cap) {
+#pragma unroll
+                    for (int c = 0; c < K::NT; ++c) t[c] = terms[mine * 6 + c];
+                } else {
+                    K::terms(st, sj, r + l, a, t);   // beyond the buffer: evolved here
+                }
+#pragma unroll
+                for (int c = 0; c < K::NT; ++c) tt[warp][c][l] = t[c];
+            }
+            e += __popc(word);
+            __syncwarp();
+            const int m = (nt - r) < 32 ? (nt - r) : 32;
+            if (l < K::NT)
+                for (int q = 0; q < m; ++q) acc = K::accum(l, acc, tt[warp][l][q]);
+            __syncwarp();
+        }
+        __syncthreads();
+    }
+    double res[K::NT];
+#pragma unroll
+    for (int c = 0; c < K::NT; ++c) res[c] = __shfl_sync(0xffffffffu, acc, c);
+    if (l == 0 && live) K::store_acc(res, st, a, i);
+}
+
+namespace {
+struct SakuraSplit {
+    size_t W, bits_b, count_b, off_b, cap, terms_b;
+};
+size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+SakuraSplit sakura_split_layout(size_t ni, size_t nj) {
+    SakuraSplit L;
+    L.W = (nj + 31) / 32;
+    L.bits_b = align256(ni * L.W * sizeof(unsigned));
+    L.count_b = align256(ni * sizeof(long long));
+    L.off_b = align256((ni + 1) * sizeof(long long));
+    // room for 1/32 of the pairs (65536 to 2^21 entries): Kepler pairs are a
+    // few percent of a cluster's pairs; any excess is evolved inline
+    size_t cap = ni * nj / 32;
+    if (cap < 65536) cap = 65536;
+    if (cap > ((size_t)1 << 21)) cap = (size_t)1 << 21;
+    if (cap > ni * nj) cap = ni * nj;
+    L.cap = cap;
+    L.terms_b = align256(cap * 6 * sizeof(double));
+    return L;
+}
+}  // namespace
+
+bool sakura_split_applies(const PairArgs &a) {
+    return (a.flag == 1 || a.flag == -1) && a.ni > 0 && a.nj > 0 &&
+           (double)a.ni * (double)a.nj <= 1073741824.0;
+}
+
+size_t sakura_split_ws_bytes(size_t ni, size_t nj) {
+    const SakuraSplit L = sakura_split_layout(ni, nj);
+    return L.bits_b + L.count_b + L.off_b + L.terms_b;
+}
+
+cudaError_t launch_sakura_split(const PairArgs &a, void *ws, size_t ws_bytes, int sms, cudaStream_t s) {
+    const SakuraSplit L = sakura_split_layout(a.ni, a.nj);
+    if (L.bits_b + L.count_b + L.off_b + L.terms_b > ws_bytes) return cudaErrorInvalidValue;
+    char *base = static_cast<char *>(ws);
+    unsigned *bits = reinterpret_cast<unsigned *>(base);
+    long long *count = reinterpret_cast<long long *>(base + L.bits_b);
+    long long *off = reinterpret_cast<long long *>(base + L.bits_b + L.count_b);
+    double *terms = reinterpret_cast<double *>(base + L.bits_b + L.count_b + L.off_b);
+    const unsigned blocks = (unsigned)((a.ni + SAK_WARPS - 1) / SAK_WARPS);
+    sakura_mark<<<blocks, F64W_THREADS, 0, s>>>(a, bits, L.W, count);
+    sakura_scan<<<1, 1024, 0, s>>>(count, a.ni, off);
+    sakura_solve<<<(unsigned)(sms > 0 ? sms * 8 : 1024), 128, 0, s>>>(a, bits, L.W, off, terms, (long long)L.cap);
+    sakura_fold<<<blocks, F64W_THREADS, 0, s>>>(a, bits, L.W, off, terms, (long long)L.cap);
     return cudaGetLastError();
 }
 

@@ -52,6 +52,12 @@ struct PairArgs {
 
 // Launchers (stream-ordered, asynchronous).  Return a cudaError_t.
 cudaError_t launch_fp64(int kernel, const PairArgs &a, int sms, cudaStream_t s);
+// Sakura with its Kepler pairs solved apart (bit-identical to launch_fp64's
+// Sakura); applies to flags -1 and +1 and ni * nj <= 2^30.  Workspace:
+// sakura_split_ws_bytes(ni, nj).
+bool sakura_split_applies(const PairArgs &a);
+size_t sakura_split_ws_bytes(size_t ni, size_t nj);
+cudaError_t launch_sakura_split(const PairArgs &a, void *ws, size_t ws_bytes, int sms, cudaStream_t s);
 
 // Kepler pair solver: pair p = particles 2p and 2p+1 of `in` (F_M..F_VZ);
 // writes r, v after dt to out[0..5] (which may alias the inputs).

@@ -223,9 +223,10 @@ __device__ __forceinline__ void rel_acc(double m, double e2, const double r[3], 
     for (int k = 0; k < 3; ++k) a[k] = dmul(-mq, r[k]);
 }
 
+// dt / 2 as dt * 0.5 here and below: both round the same exact value.
 __device__ __forceinline__ void pair_leapfrog(double dt, double m, double e2, const double r0[3],
                                               const double v0[3], double r[3], double v[3]) {
-    double h = ddiv(dt, 2.0);
+    double h = dmul(dt, 0.5);
     double a[3];
     for (int k = 0; k < 3; ++k) r[k] = dadd(r0[k], dmul(v0[k], h));
     rel_acc(m, e2, r, a);
@@ -233,14 +234,32 @@ __device__ __forceinline__ void pair_leapfrog(double dt, double m, double e2, co
     for (int k = 0; k < 3; ++k) r[k] = dadd(r[k], dmul(v[k], h));
 }
 
-__device__ __forceinline__ void pair_twobody(double dt, double m, double e2, const double r0[3],
-                                             const double v0[3], double r[3], double v[3],
-                                             KepBudget &b) {
+// twobody_solver's branch (sakura_kernel_common.h:111-122): the
+// universal-variable solver unless r^2 > (64 m / v^2)^2.
+__device__ __forceinline__ bool twobody_uses_kepler(double m, const double r0[3], const double v0[3]) {
     double r2 = ddot3(r0[0], r0[1], r0[2], r0[0], r0[1], r0[2]);
     double v2 = ddot3(v0[0], v0[1], v0[2], v0[0], v0[1], v0[2]);
     double R = dmul(64.0, ddiv(m, v2));
-    if (r2 > dmul(R, R)) pair_leapfrog(dt, m, e2, r0, v0, r, v);
+    return !(r2 > dmul(R, R));
+}
+
+__device__ __forceinline__ void pair_twobody(double dt, double m, double e2, const double r0[3],
+                                             const double v0[3], double r[3], double v[3],
+                                             KepBudget &b) {
+    if (!twobody_uses_kepler(m, r0, v0)) pair_leapfrog(dt, m, e2, r0, v0, r, v);
     else kep_solve(dt, m, e2, r0, v0, r, v, b);
+}
+
+// Whether pair_evolve with flag -1 or +1 (one two-body step) takes the
+// universal-variable solver; the test is pair_twobody's on the same state.
+__device__ __forceinline__ bool sakura_uses_kepler(double dt, long long flag, double m, const double r0[3],
+                                                   const double v0[3]) {
+    if (flag == -1) {
+        double r[3];
+        for (int k = 0; k < 3; ++k) r[k] = dsub(r0[k], dmul(v0[k], dt));
+        return twobody_uses_kepler(m, r, v0);
+    }
+    return twobody_uses_kepler(m, r0, v0);
 }
 
 // Sakura's four flags (sakura_kernel_common.h:126-191); others are a no-op.
@@ -257,12 +276,12 @@ __device__ void pair_evolve(double dt, long long flag, double m, double e2, cons
         for (int k = 0; k < 3; ++k) { r[k] = rt[k]; v[k] = vt[k]; }
         for (int k = 0; k < 3; ++k) r[k] = dsub(r[k], dmul(v[k], dt));
     } else if (flag == -2) {
-        for (int k = 0; k < 3; ++k) r[k] = dsub(r[k], ddiv(dmul(v[k], dt), 2.0));
+        for (int k = 0; k < 3; ++k) r[k] = dsub(r[k], dmul(dmul(v[k], dt), 0.5));
         pair_twobody(dt, m, e2, r, v, rt, vt, b);
         for (int k = 0; k < 3; ++k) { r[k] = rt[k]; v[k] = vt[k]; }
-        for (int k = 0; k < 3; ++k) r[k] = dsub(r[k], ddiv(dmul(v[k], dt), 2.0));
+        for (int k = 0; k < 3; ++k) r[k] = dsub(r[k], dmul(dmul(v[k], dt), 0.5));
     } else if (flag == 2) {
-        double h = ddiv(dt, 2.0);
+        double h = dmul(dt, 0.5);
         pair_twobody(h, m, e2, r, v, rt, vt, b);
         for (int k = 0; k < 3; ++k) { r[k] = rt[k]; v[k] = vt[k]; }
         for (int k = 0; k < 3; ++k) r[k] = dsub(r[k], dmul(v[k], dt));
@@ -270,6 +289,22 @@ __device__ void pair_evolve(double dt, long long flag, double m, double e2, cons
         for (int k = 0; k < 3; ++k) { r[k] = rt[k]; v[k] = vt[k]; }
     }
     for (int k = 0; k < 3; ++k) { r1[k] = r[k]; v1[k] = v[k]; }
+}
+
+// pair_evolve for flag -1 or +1 when the pair is known to take the
+// leapfrog branch of its two-body step (sakura_uses_kepler is false): the
+// same operations without the test.
+__device__ __forceinline__ void pair_evolve_leapfrog(double dt, long long flag, double m, double e2,
+                                                     const double r0[3], const double v0[3], double r1[3],
+                                                     double v1[3]) {
+    double r[3], rt[3], vt[3];
+    if (flag == -1) {
+        for (int k = 0; k < 3; ++k) r[k] = dsub(r0[k], dmul(v0[k], dt));
+        pair_leapfrog(dt, m, e2, r, v0, r1, v1);
+    } else {
+        pair_leapfrog(dt, m, e2, r0, v0, rt, vt);
+        for (int k = 0; k < 3; ++k) { r1[k] = dsub(rt[k], dmul(vt[k], dt)); v1[k] = vt[k]; }
+    }
 }
 
 }  // namespace tg
