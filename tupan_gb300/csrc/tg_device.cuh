@@ -49,8 +49,8 @@ __device__ __forceinline__ float2 fnma2(float2 a, float2 b, float2 c) {
     return __ffma2_rn(make_float2(-a.x, -a.y), b, c);
 }
 
-// Hardware reciprocal square root (MUFU.RSQ), then one Newton step
-// y <- y + y*(1/2 - (s/2) y^2): relative error ~1 ulp instead of ~2 ulp.
+// Hardware reciprocal square root (MUFU.RSQ, ~2 ulp); the kernels may add
+// one Newton step y <- y + y*(1/2 - (s/2) y^2) for ~1 ulp.
 __device__ __forceinline__ float rsqrt_hw(float s) {
     float y;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(s));

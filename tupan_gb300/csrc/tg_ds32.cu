@@ -1,6 +1,6 @@
 // tg_ds32.cu -- split-FP32 ("double-single") pairwise kernels.
 //
-// Data layout in HBM (workspace, written by ds32_pack once per call):
+// Data layout in HBM (workspace, written by ds32_prepare once per call):
 //   the j-set as pair-interleaved float records.  Record p holds j = 2p and
 //   j = 2p+1; field f occupies floats [2f, 2f+1] of the record, so one
 //   16-byte shared-memory load returns two fields for both j.  Positions are
@@ -22,10 +22,13 @@
 // of each j-tile into a 3-stage shared-memory ring completing on an mbarrier;
 // all threads wait with a bounded poll and raise a status bit on timeout.
 //
-// Arithmetic: one i-particle per thread, two j-particles per packed f32x2
-// instruction (FADD2/FMUL2/FFMA2); 1/sqrt is MUFU.RSQ plus one Newton step;
-// per-thread sums run in FP32 over 64 j and are then folded into Kahan-
-// compensated accumulators.  The roofline is the FP32 pipe (FFMA2 issue).
+// Arithmetic: two i-particles per thread (one for small problems and for
+// SnapCrackle and PNAcc), two j-particles per packed f32x2 instruction
+// (FADD2/FMUL2/FFMA2); 1/sqrt from MUFU.RSQ and, where used, 1/s from
+// MUFU.RCP (a Newton step on rsqrt is a compile-time option,
+// TG_DS32_REFINE); per-thread sums run in FP32 over 64 j and are then folded
+// into Kahan-compensated accumulators.  The roofline is the FP32 pipe (FFMA2
+// issue).
 #include <type_traits>
 
 #include "tg_device.cuh"
@@ -193,7 +196,7 @@ __device__ __forceinline__ void pair_dr(const IPos &q, float2 jxh, float2 jyh, f
     dy = add2(sub2(q.yh, jyh), sub2(q.yl, jyl));
     dz = add2(sub2(q.zh, jzh), sub2(q.zl, jzl));
 }
-// Masked, Newton-refined 1/sqrt(s) per lane; zero where dr == 0.
+// Masked 1/sqrt(s) per lane (Newton-refined if REFINE); zero where dr == 0.
 // 1/sqrt(s) and 1/s per lane from the XU pipe; both zero where dr == 0
 // (the excluded lane gets s = +inf, whose reciprocal and rsqrt are 0).
 __device__ __forceinline__ void inv_r_r2(float2 s, float2 dx, float2 dy, float2 dz, float2 &y, float2 &y2) {
