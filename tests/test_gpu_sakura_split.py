@@ -61,6 +61,7 @@ def run(native, ext, d, dt, flag, split):
     return np.stack([o.cpu().numpy() for o in out]), status
 
 
+@pytest.mark.filterwarnings("ignore:sakura. Kepler retry bound")
 @pytest.mark.parametrize("name", ["binary", "sweep", "plummer", "cold"])
 @pytest.mark.parametrize("flag", [-1, 1])
 def test_split_sakura_is_bit_identical_to_one_pass(mods, name, flag):
