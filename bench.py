@@ -18,6 +18,8 @@ Printed JSON line (rank 0):
   fp64         the FP64 GPU kernels on the same workload (bit-identical to the
                reference C backend) and the split-FP32 speed-up over them
   force_error  per-particle |a_ds32 - a_fp64| / |a_fp64| (and jerk)
+  other_kernels  split-FP32 Phi, SnapCrackle, Tstep and PNAcc on the same
+               workload, FP64 Sakura on its first 4096 particles (device time)
   cpu_baseline the CPU oracle port (same algorithm and operation order as the
                reference C backend) on the host cores, bounded sample
   clocks       nvidia-smi SM clock and throttle reasons during the timed region
@@ -241,6 +243,54 @@ def small_sizes(dev, sp):
     return out
 
 
+# reference flop counts per interaction (<kernel>_kernel_common.h)
+FLOP_OTHER = {"phi": 14, "snap_crackle": 114, "tstep": 42}
+
+
+def other_kernels(dev, sp, T, outs, n, peak32):
+    """The other hot-path kernels on the same workload: split-FP32 Phi,
+    SnapCrackle (a, j from the split-FP32 AccJerk above), Tstep (eta 1/1024)
+    and PNAcc (order 5, c = 1e4) at N = n, and FP64 Sakura (flag -1,
+    dt = 1/1024) on the workload's first 4096 particles: median CUDA-event
+    time of 5 calls after one untimed call."""
+    import torch
+    from tupan_gb300 import _native
+    T = dict(T)
+    for k, x in zip(("ax", "ay", "az", "jx", "jy", "jz"), outs[3:9]):
+        T[k] = x
+    c = 1e4
+    pn = (5,) + tuple(c ** -k for k in range(1, 8))
+    jobs = [("phi", n, _native.PREC_DS32, ()), ("snap_crackle", n, _native.PREC_DS32, ()),
+            ("tstep", n, _native.PREC_DS32, (1.0 / 1024,)), ("pnacc", n, _native.PREC_DS32, pn),
+            ("sakura", 4096, _native.PREC_FP64, (1.0 / 1024, -1))]
+    res = {}
+    for name, m, prec, sc in jobs:
+        fields, _, names = _native.SPECS[name]
+        ptrs = [T[k].data_ptr() for k in fields]
+        o = [torch.empty(m, dtype=torch.float64, device=dev) for _ in names]
+
+        def call():
+            _native.call_device(name, m, ptrs, m, ptrs, sc, [x.data_ptr() for x in o], prec, sp)
+        call()
+        ms = []
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            call()
+            e1.record()
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        med = float(np.median(ms))
+        rec = {"n": m, "precision": "ds32" if prec == _native.PREC_DS32 else "fp64", "ms": med,
+               "gint_s": m * m / (med * 1e-3) / 1e9}
+        if name in FLOP_OTHER and peak32 > 0:
+            rec["frac"] = FLOP_OTHER[name] * m * m / (med * 1e-3) / 1e12 / peak32
+        res[name] = rec
+    st = _native.sync_status(sp)
+    res["status"] = st
+    return res
+
+
 def ours(args, rank, world, dist):
     import torch
     from tupan_gb300 import _native
@@ -356,6 +406,7 @@ def ours(args, rank, world, dist):
     # ---- the smaller sizes of the same workload (parity/measurement only) --
     if rank == 0 and not args.no_fp64:
         line["sizes"] = small_sizes(dev, sp)
+        line["other_kernels"] = other_kernels(dev, sp, T, outs, n, peak32)
 
     # ---- end to end through the drop-in host entry points ---------------
     pin = {k: torch.tensor(d[k], dtype=torch.float64).pin_memory() for k in P8}
