@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 SIZES = [5, 0, 1, 2, 63, 64, 65, 255, 256, 511, 1000, 1300]
 OUTS = {"phi": ("phi",), "acc": ("ax", "ay", "az"), "acc_jerk": ("ax", "ay", "az", "jx", "jy", "jz"),
         "snap_crackle": ("sx", "sy", "sz", "cx", "cy", "cz")}
-TOL = {"phi": 2e-6, "acc": 4e-6, "acc_jerk": 4e-6, "snap_crackle": 2e-4}
+TOL = {"phi": 2e-6, "acc": 4e-6, "acc_jerk": 4e-6, "snap_crackle": 5e-5}
 
 
 @pytest.fixture(scope="module")

@@ -10,7 +10,16 @@ Tolerances:
     log differ from glibc by an ulp; the Laguerre iteration then stops on a
     slightly different iterate within its 2^-42 tolerance).
   * split FP32 (ds32): per particle |out_gpu - out_ref| / |out_ref| (vector
-    norm over the components of one output quantity) below DS32_TOL[kernel].
+    norm over the components of one output quantity).  On the golden
+    fixtures (the reference test's shapes and prefix sweeps, a Plummer set
+    and a binary-rich set) the bound is DS32_TOL_FIXTURE: 1e-6 for Phi, Acc,
+    AccJerk (acceleration and jerk) and Tstep, the accuracy asked of the
+    split form; measured maxima 7.8e-7 (jerk), 7.1e-7 (Acc).  The larger
+    synthetic Plummer sets (ragged shapes up to 5000 x 4097) use DS32_TOL:
+    there a few particles whose net force is much smaller than the sum of
+    its terms reach 1.1e-6 (Acc) and 2.1e-6 (jerk), the FP32 rounding floor
+    of such sums.  The kernels are deterministic, so these maxima do not
+    vary between runs.
 """
 import numpy as np
 import pytest
@@ -21,8 +30,10 @@ pytestmark = pytest.mark.gpu
 
 from golden_io import CASES, FIELDS, PREFIXES, load, typed_scalars  # noqa: E402
 
-DS32_TOL = {"phi": 2e-6, "acc": 4e-6, "acc_jerk": 4e-6, "snap_crackle": 2e-4,
-            "tstep": 2e-5, "pnacc": 2e-4}
+DS32_TOL_FIXTURE = {"phi": 1e-6, "acc": 1e-6, "acc_jerk": 1e-6, "snap_crackle": 1e-5,
+                    "tstep": 1e-6, "pnacc": 1e-5}
+DS32_TOL = {"phi": 2e-6, "acc": 4e-6, "acc_jerk": 4e-6, "snap_crackle": 5e-5,
+            "tstep": 2e-6, "pnacc": 2e-5}
 GROUPS = {"phi": [(0,)], "acc": [(0, 1, 2)], "acc_jerk": [(0, 1, 2), (3, 4, 5)],
           "snap_crackle": [(0, 1, 2), (3, 4, 5)], "tstep": [(0,), (1,)],
           "pnacc": [(0, 1, 2)], "sakura": [(0, 1, 2), (3, 4, 5)]}
@@ -128,7 +139,7 @@ def test_ds32_against_golden(ext, case):
         P = PS(ps)
         got = run_kernel(ext, name, "ds32", P, P, sc)
         err = rel_err(name, got, z["out_" + key])
-        assert err <= DS32_TOL[name], "%s %s ds32 error %.3e" % (case, name, err)
+        assert err <= DS32_TOL_FIXTURE[name], "%s %s ds32 error %.3e" % (case, name, err)
 
 
 def test_ds32_prefix_sweeps(ext):
@@ -140,10 +151,10 @@ def test_ds32_prefix_sweeps(ext):
         for p in PREFIXES:
             P, S = PS(ps), PS({f: ps[f][:p] for f in FIELDS})
             err = rel_err(name, run_kernel(ext, name, "ds32", P, S, sc), z["outJ%d_" % p + key])
-            assert err <= DS32_TOL[name], (name, p, err)
+            assert err <= DS32_TOL_FIXTURE[name], (name, p, err)
             P, S = PS(ps), PS({f: ps[f][:p] for f in FIELDS})
             err = rel_err(name, run_kernel(ext, name, "ds32", S, P, sc), z["outI%d_" % p + key])
-            assert err <= DS32_TOL[name], (name, p, err)
+            assert err <= DS32_TOL_FIXTURE[name], (name, p, err)
 
 
 def plummer(n, seed, e2=1e-4):
