@@ -10,13 +10,17 @@ protocol (cty, set_gsize, set_args, map_buffers, run; cffi_backend.py:90-126).
 
 Precision ("prec") is "float64" (FP64 kernels, bit-identical to the reference
 for Phi/Acc/AccJerk/SnapCrackle/Tstep) or "ds32" (split FP32; "float32" is
-accepted as an alias).  The default comes from TUPAN_GB300_PREC, else float64.
+accepted as an alias).  The default is "ds32" when `--use_sp` is on the
+command line (as the reference selects single precision), else
+TUPAN_GB300_PREC, else float64; `--use_cl` (the reference's OpenCL switch)
+selects nothing: the only backend is CUDA.
 
 Particle arrays may be float64 CUDA torch tensors (used in place, no copies)
 or numpy arrays (copied to the GPU, results copied back into the registered
 numpy outputs, like the reference's OpenCL backend, opencl_backend.py:117-164).
 """
 import os
+import sys
 import warnings
 from collections import namedtuple
 
@@ -181,11 +185,21 @@ class CUDAKernel(object):
         return arrays
 
 
+def default_precision():
+    """Precision of kernels made without an explicit `prec`: "ds32" when
+    `--use_sp` is on the command line (the reference's single-precision
+    switch, tupan/lib/utils/ctype.py:13-18), else TUPAN_GB300_PREC, else
+    "float64"."""
+    if "--use_sp" in sys.argv:
+        return "ds32"
+    return os.environ.get("TUPAN_GB300_PREC", "float64")
+
+
 def get_kernel(name, backend="CUDA", prec=None):
     if backend not in ("CUDA", "C", "CL"):
         raise ValueError("Inappropriate 'backend': %s. Supported values: ['CUDA']" % backend)
     if prec is None:
-        prec = os.environ.get("TUPAN_GB300_PREC", "float64")
+        prec = default_precision()
     return CUDAKernel(prec, name)
 
 
