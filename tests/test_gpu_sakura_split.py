@@ -73,3 +73,25 @@ def test_split_sakura_is_bit_identical_to_one_pass(mods, name, flag):
         assert s1 == s2, (name, flag, dt)
         bad = np.argwhere(one.view(np.int64) != two.view(np.int64))
         assert bad.size == 0, (name, flag, dt, bad[:3].tolist())
+
+
+@pytest.mark.filterwarnings("ignore:sakura. Kepler retry bound")
+@pytest.mark.parametrize("flag", [-1, 1])
+def test_split_sakura_with_distinct_i_and_j_sets(mods, flag):
+    """i-set a prefix of the j-set, and the reverse (ragged bitmap rows,
+    rows shorter and longer than the j-range of a word)."""
+    native, ext = mods
+    from tupan_gb300.ics import Salpeter, plummer_arrays
+    d = plummer_arrays(700, 1e-3, imf=Salpeter(0.1, 100.0), seed=13)
+    for ni, nj in ((70, 700), (700, 45), (33, 33)):
+        I = {f: np.asarray(d[f][:ni]) for f in F8}
+        J = {f: np.asarray(d[f][:nj]) for f in F8}
+        outs = []
+        for split in (0, 1):
+            native.lib.tg_set_sakura_split(split)
+            native.sync_status()
+            out = ext.Sakura("CUDA", "float64").calc(PS(I), PS(J), 1.0 / 256, flag)
+            torch.cuda.synchronize()
+            outs.append((np.stack([o.cpu().numpy() for o in out]), native.sync_status()))
+        assert outs[0][1] == outs[1][1]
+        assert np.array_equal(outs[0][0].view(np.int64), outs[1][0].view(np.int64)), (ni, nj)
