@@ -29,6 +29,7 @@
 // TG_DS32_REFINE); per-thread sums run in FP32 over 64 j and are then folded
 // into Kahan-compensated accumulators.  The roofline is the FP32 pipe (FFMA2
 // issue).
+#include <atomic>
 #include <type_traits>
 
 #include "tg_device.cuh"
@@ -1156,19 +1157,23 @@ struct Geometry {
     size_t nomask_len, nomask_bytes;   // coincidence-check table (ints) for the unmasked twin
 };
 
+// Resident CTAs per SM of kernel K (computed once; concurrent first calls
+// compute the same value, so the atomic only makes the publication safe).
 template <class K>
 static int ctas_per_sm() {
-    static int cached = -1;
-    if (cached < 0) {
+    static std::atomic<int> cached{-1};
+    int c = cached.load(std::memory_order_acquire);
+    if (c < 0) {
         const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
         cudaFuncSetAttribute(ds32_streamk<K, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(ds32_streamk<K, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int n = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ds32_streamk<K, 1>, DS_THREADS, smem) != cudaSuccess || n < 1)
             n = 1;
-        cached = n;
+        cached.store(n, std::memory_order_release);
+        c = n;
     }
-    return cached;
+    return c;
 }
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -1319,16 +1324,18 @@ static int ds32_bi() { return DS_THREADS * K::IPT; }
 
 template <class K>
 static int ctas_per_sm_seg() {
-    static int cached = -1;
-    if (cached < 0) {
+    static std::atomic<int> cached{-1};
+    int c = cached.load(std::memory_order_acquire);
+    if (c < 0) {
         const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
         cudaFuncSetAttribute(ds32_streamk_seg<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int n = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ds32_streamk_seg<K>, DS_THREADS, smem) != cudaSuccess || n < 1)
             n = 1;
-        cached = n;
+        cached.store(n, std::memory_order_release);
+        c = n;
     }
-    return cached;
+    return c;
 }
 
 template <class K>
