@@ -133,6 +133,17 @@ def sync_status(stream=None):
     return rc
 
 
+def current_stream():
+    """Handle of torch's current CUDA stream on the current device: the
+    value of torch.cuda.current_stream().cuda_stream, without building the
+    Stream object (the integrators ask for it before every launch)."""
+    import torch
+    raw = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+    if raw is not None:
+        return raw(torch.cuda.current_device())
+    return torch.cuda.current_stream().cuda_stream
+
+
 def psum(t):
     """float(sum of a float64 CUDA tensor) in numpy's pairwise order (tg_sum),
     so the value equals numpy.sum of the same array bit for bit."""
@@ -141,7 +152,7 @@ def psum(t):
     if not (t.is_cuda and t.dtype == torch.float64):
         raise TypeError("psum expects a float64 CUDA tensor")
     out = torch.empty(1, dtype=torch.float64, device=t.device)
-    check(lib.tg_sum(t.numel(), t.data_ptr(), out.data_ptr(), torch.cuda.current_stream().cuda_stream),
+    check(lib.tg_sum(t.numel(), t.data_ptr(), out.data_ptr(), current_stream()),
           "tg_sum")
     return float(out.item())
 

@@ -22,7 +22,7 @@ PREC = {"float64": _native.PREC_FP64, "ds32": _native.PREC_DS32, "float32": _nat
 
 
 def _stream():
-    return torch.cuda.current_stream().cuda_stream
+    return _native.current_stream()
 
 
 def _check_set(r, m, e2):

@@ -73,7 +73,7 @@ class Ensemble(object):
 
     @staticmethod
     def _stream():
-        return torch.cuda.current_stream().cuda_stream
+        return _native.current_stream()
 
     def _call(self, name, ps, inputs, outputs):
         fn = getattr(_lib, name)

@@ -30,7 +30,7 @@ def set_derivatives(ps, order):
 
 
 def _stream():
-    return torch.cuda.current_stream().cuda_stream
+    return _native.current_stream()
 
 
 def predict(ps1, ps0, tau, order):

@@ -26,7 +26,7 @@ from . import Base
 def _div3(x, y, z, mx, my, mz, d):
     _native.check(_native.lib.tg_div3(x.numel(), x.data_ptr(), y.data_ptr(), z.data_ptr(), mx.data_ptr(),
                                       my.data_ptr(), mz.data_ptr(), float(d),
-                                      torch.cuda.current_stream().cuda_stream), "tg_div3")
+                                      _native.current_stream()), "tg_div3")
 
 
 def nreg_x(ps, dt):

@@ -14,7 +14,7 @@ from .sia import drift
 
 
 def _stream():
-    return torch.cuda.current_stream().cuda_stream
+    return _native.current_stream()
 
 
 def apply_increments(ps):

@@ -69,7 +69,7 @@ def palindrome(first, second):
 
 
 def _stream():
-    return torch.cuda.current_stream().cuda_stream
+    return _native.current_stream()
 
 
 def drift(ps, tau):
@@ -110,10 +110,14 @@ class FewBody(object):
 
 
 def split(ps, condition):
-    """sia.py:24-43: (slow, fast); a set of at most two particles stays whole."""
+    """sia.py:24-43: (slow, fast); a set of at most two particles stays whole.
+    Each part keeps the particles' order; the partition takes one host
+    synchronisation (the count), the stable sort and gathers none."""
     if ps.n <= 2:
         return ps, type(ps)(0)
-    return ps[condition], ps[~condition]
+    order = torch.argsort((~condition).to(torch.int8), stable=True)
+    k = int(condition.sum())
+    return ps.take(order[:k]), ps.take(order[k:])
 
 
 def join(slow, fast):

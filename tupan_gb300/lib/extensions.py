@@ -98,11 +98,18 @@ def _device():
     return torch.device("cuda", torch.cuda.current_device())
 
 
+def _ptr(arg):
+    """Device address of a converted array argument."""
+    return arg.data_ptr() if isinstance(arg, torch.Tensor) else arg.ptr
+
+
 def _to_device_arg(x, output):
-    """Convert one array argument (numpy or torch) to a _DeviceArg."""
+    """Convert one array argument (numpy or torch): a float64 contiguous CUDA
+    tensor is used as it is, anything else becomes a _DeviceArg staging
+    copy."""
     if isinstance(x, torch.Tensor):
         if x.is_cuda and x.dtype == torch.float64 and x.is_contiguous():
-            return _DeviceArg(x)
+            return x
         t = x.detach().to(device=_device(), dtype=torch.float64).contiguous()
         return _DeviceArg(t, writeback=x if output else None)
     a = np.asarray(x)
@@ -147,13 +154,13 @@ class CUDAKernel(object):
         nf, ns, no = len(fields), len(scal), len(outs)
         a = self.args
         ni = int(a[0])
-        iptr = [x.ptr for x in a[1:1 + nf]]
+        iptr = [_ptr(x) for x in a[1:1 + nf]]
         nj = int(a[1 + nf])
-        jptr = [x.ptr for x in a[2 + nf:2 + 2 * nf]]
+        jptr = [_ptr(x) for x in a[2 + nf:2 + 2 * nf]]
         sc = a[2 + 2 * nf:2 + 2 * nf + ns]
-        optr = [x.ptr for x in a[2 + 2 * nf + ns:]]
+        optr = [_ptr(x) for x in a[2 + 2 * nf + ns:]]
         assert len(optr) == no
-        stream = torch.cuda.current_stream().cuda_stream
+        stream = _native.current_stream()
         _native.call_device(self.name, ni, iptr, nj, jptr, sc, optr, PRECISIONS[self.prec], stream)
         if self.name == "sakura":
             st = _native.sync_status(stream)
@@ -164,12 +171,12 @@ class CUDAKernel(object):
     def _run_kepler(self):
         # args: m, rx, ry, rz, e2, vx, vy, vz, dt, then the six outputs
         a = self.args
-        n = a[0].tensor.numel()
+        n = (a[0] if isinstance(a[0], torch.Tensor) else a[0].tensor).numel()
         if n % 2:
             raise ValueError("kepler_solver: the particle set must hold whole pairs (n = %d)" % n)
-        stream = torch.cuda.current_stream().cuda_stream
-        rc = _native.lib.tg_kepler_solver(n // 2, *[x.ptr for x in a[:8]], float(a[8]),
-                                          *[x.ptr for x in a[9:15]], stream)
+        stream = _native.current_stream()
+        rc = _native.lib.tg_kepler_solver(n // 2, *[_ptr(x) for x in a[:8]], float(a[8]),
+                                          *[_ptr(x) for x in a[9:15]], stream)
         _native.check(rc, "tg_kepler_solver")
         st = _native.sync_status(stream)
         if st:
@@ -178,6 +185,8 @@ class CUDAKernel(object):
 
     def map_buffers(self, arrays, buffers):
         for arr, buf in zip(arrays, buffers):
+            if isinstance(buf, torch.Tensor):   # written in place
+                continue
             if buf.host is not None:
                 buf.host[...] = buf.tensor.cpu().numpy()
             elif buf.writeback is not None:
@@ -209,7 +218,7 @@ def prepare_args(args, argtypes):
 
 def _register(ips, names):
     for n in names:
-        if n not in ips.__dict__:
+        if not hasattr(ips, n):
             ips.register_auxiliary_attribute(n, "real")
 
 

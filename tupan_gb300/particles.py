@@ -17,8 +17,26 @@ REAL_ATTRS = ("mass", "eps2", "rx", "ry", "rz", "vx", "vy", "vz", "time", "tstep
 INT_ATTRS = ("id", "nstep")
 
 
+SPARE_ROWS = 24   # room for kernel outputs registered later, without reallocation
+
+
+def _layout(rnames, inames):
+    """attribute name -> (block, row)"""
+    lay = {k: ("_real", r) for r, k in enumerate(rnames)}
+    lay.update({k: ("_int", r) for r, k in enumerate(inames)})
+    return lay
+
+
 class ParticleSystem(object):
-    """n particles; every attribute is a length-n tensor on `device`."""
+    """n particles; every attribute is a length-n tensor on `device`.
+
+    Storage: all float64 attributes are the rows of one 2-D tensor and the
+    int64 ones (id, nstep) of another, each with spare rows for attributes
+    registered later; an attribute is a contiguous row view.  Selecting,
+    copying or concatenating particles is then one gather or one cat per
+    block instead of one per attribute, which is what keeps the
+    hierarchical integrators' many small subsets cheap.  Assigning a tensor
+    to an attribute copies it into the attribute's row."""
 
     include_pn_corrections = False
     t_curr = 0.0
@@ -26,14 +44,79 @@ class ParticleSystem(object):
     def __init__(self, n=0, device=None, **arrays):
         if device is None:
             device = torch.device("cuda", torch.cuda.current_device()) if torch.cuda.is_available() else torch.device("cpu")
-        self.__dict__["_device"] = torch.device(device)
-        self.n = int(n)
-        for a in REAL_ATTRS:
-            setattr(self, a, torch.zeros(self.n, dtype=torch.float64, device=self._device))
-        self.id = torch.arange(self.n, dtype=torch.int64, device=self._device)
-        self.nstep = torch.zeros(self.n, dtype=torch.int64, device=self._device)
+        d = self.__dict__
+        d["_device"] = torch.device(device)
+        d["n"] = int(n)
+        d["_rnames"] = list(REAL_ATTRS)
+        d["_inames"] = list(INT_ATTRS)
+        d["_real"] = torch.zeros(len(REAL_ATTRS) + SPARE_ROWS, d["n"], dtype=torch.float64, device=d["_device"])
+        d["_int"] = torch.zeros(len(INT_ATTRS) + 2, d["n"], dtype=torch.int64, device=d["_device"])
+        d["_int"][INT_ATTRS.index("id")] = torch.arange(d["n"], dtype=torch.int64, device=d["_device"])
+        d["_layout"] = _layout(d["_rnames"], d["_inames"])
         for k, v in arrays.items():
             self.set_array(k, v)
+
+    @classmethod
+    def _from_blocks(cls, device, n, rnames, inames, real, int_, layout=None):
+        # the name lists and the layout are shared with the source set: they
+        # are replaced, never changed in place
+        new = cls.__new__(cls)
+        d = new.__dict__
+        d["_device"] = device
+        d["n"] = int(n)
+        d["_rnames"] = rnames
+        d["_inames"] = inames
+        d["_real"] = real
+        d["_int"] = int_
+        d["_layout"] = layout if layout is not None else _layout(rnames, inames)
+        return new
+
+    def __getattr__(self, name):
+        # only reached for names not in __dict__: an attribute's row view is
+        # made on first use and cached
+        d = self.__dict__
+        lay = d.get("_layout")
+        if lay is not None and name in lay:
+            key, r = lay[name]
+            v = d[key][r]
+            d[name] = v
+            return v
+        raise AttributeError(name)
+
+    def _rebind(self):
+        # the blocks were replaced: drop the cached row views
+        d = self.__dict__
+        for k in d["_layout"]:
+            d.pop(k, None)
+
+    def _add_row(self, name, value):
+        d = self.__dict__
+        is_int = value.dtype in (torch.int64, torch.int32, torch.bool)
+        nkey, key = ("_inames", "_int") if is_int else ("_rnames", "_real")
+        names = d[nkey]
+        blk = d[key]
+        if len(names) == blk.shape[0]:   # no spare row left: grow the block
+            grown = torch.zeros(blk.shape[0] + SPARE_ROWS, d["n"], dtype=blk.dtype, device=blk.device)
+            grown[:blk.shape[0]] = blk
+            self._rebind()
+            d[key] = blk = grown
+        blk[len(names)].copy_(value)
+        d[nkey] = names + [name]
+        d["_layout"] = _layout(d["_rnames"], d["_inames"])
+
+    def __setattr__(self, name, value):
+        d = self.__dict__
+        if isinstance(value, torch.Tensor) and not name.startswith("_"):
+            if value.dim() != 1 or value.shape[0] != d["n"]:
+                raise ValueError("%s must have shape (%d,)" % (name, d["n"]))
+            if name in d["_layout"]:
+                row = getattr(self, name)
+                if value.data_ptr() != row.data_ptr():
+                    row.copy_(value)
+            else:
+                self._add_row(name, value)
+            return
+        d[name] = value
 
     # ---- construction helpers -------------------------------------------------
     @classmethod
@@ -50,44 +133,65 @@ class ParticleSystem(object):
         setattr(self, name, t)
 
     def register_auxiliary_attribute(self, attr, sctype):
-        if attr in self.__dict__:
+        if attr in self.__dict__ or attr in self.__dict__["_layout"]:
             raise ValueError("'{0}' is already a registered attribute.".format(attr))
         dtype = torch.float64 if sctype == "real" else torch.int64
-        setattr(self, attr, torch.zeros(self.n, dtype=dtype, device=self._device))
+        self._add_row(attr, torch.zeros(self.n, dtype=dtype, device=self._device))
 
     def _arrays(self):
-        return {k: v for k, v in self.__dict__.items() if isinstance(v, torch.Tensor)}
+        d = self.__dict__
+        return {k: getattr(self, k) for k in d["_rnames"] + d["_inames"]}
 
     def copy(self):
-        new = ParticleSystem.__new__(ParticleSystem)
-        new.__dict__["_device"] = self._device
-        new.n = self.n
-        for k, v in self._arrays().items():
-            setattr(new, k, v.clone())
-        return new
+        return ParticleSystem._from_blocks(self._device, self.n, self._rnames, self._inames,
+                                           self._real.clone(), self._int.clone(), self._layout)
 
     def append(self, other):
         """Concatenate `other`'s particles after these (body.py:641-645); an
         attribute present on one side only is zero-filled on the other."""
         if not other.n:
             return
-        mine, theirs = self._arrays(), other._arrays()
-        for k in set(mine) | set(theirs):
-            a, b = mine.get(k), theirs.get(k)
-            if a is None:
-                a = torch.zeros(self.n, dtype=b.dtype, device=b.device)
-            if b is None:
-                b = torch.zeros(other.n, dtype=a.dtype, device=a.device)
-            setattr(self, k, torch.cat((a, b)))
-        self.n += other.n
+        d = self.__dict__
+        if (other._rnames == d["_rnames"] and other._inames == d["_inames"]
+                and other._real.shape[0] == d["_real"].shape[0] and other._int.shape[0] == d["_int"].shape[0]):
+            self._rebind()
+            d["_real"] = torch.cat((d["_real"], other._real), dim=1)
+            d["_int"] = torch.cat((d["_int"], other._int), dim=1)
+        else:
+            mine, theirs = self._arrays(), other._arrays()
+            rn = d["_rnames"] + [k for k in other._rnames if k not in d["_rnames"]]
+            inn = d["_inames"] + [k for k in other._inames if k not in d["_inames"]]
+            n = d["n"] + other.n
+            real = torch.zeros(len(rn) + SPARE_ROWS, n, dtype=torch.float64, device=self._device)
+            int_ = torch.zeros(len(inn) + 2, n, dtype=torch.int64, device=self._device)
+            for blk, names in ((real, rn), (int_, inn)):
+                for r, k in enumerate(names):
+                    if k in mine:
+                        blk[r, :d["n"]] = mine[k]
+                    if k in theirs:
+                        blk[r, d["n"]:] = theirs[k]
+            self._rebind()
+            d["_real"], d["_int"], d["_rnames"], d["_inames"] = real, int_, rn, inn
+            d["_layout"] = _layout(rn, inn)
+        d["n"] += other.n
 
     def __getitem__(self, slc):
-        new = ParticleSystem.__new__(ParticleSystem)
-        new.__dict__["_device"] = self._device
-        for k, v in self._arrays().items():
-            setattr(new, k, v[slc].contiguous())
-        new.n = int(new.mass.shape[0])
-        return new
+        if isinstance(slc, torch.Tensor) and slc.dtype == torch.bool:
+            # one index computation (one host sync) instead of one per attribute
+            return self.take(torch.nonzero(slc).flatten())
+        if isinstance(slc, torch.Tensor):
+            return self.take(slc.to(device=self._device, dtype=torch.int64))
+        real = self._real[:, slc].contiguous()
+        int_ = self._int[:, slc].contiguous()
+        return ParticleSystem._from_blocks(self._device, real.shape[1], self._rnames, self._inames, real, int_,
+                                           self._layout)
+
+    def take(self, idx):
+        """The particles at device indices `idx`, in that order (one gather per
+        block, no host synchronisation)."""
+        return ParticleSystem._from_blocks(self._device, idx.numel(), self._rnames, self._inames,
+                                           self._real.index_select(1, idx), self._int.index_select(1, idx),
+                                           self._layout)
 
     def __len__(self):
         return self.n
