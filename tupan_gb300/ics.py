@@ -98,9 +98,12 @@ def plummer_arrays(n, eps, imf=None, seed=0, mfrac=0.999):
     """Host-only Plummer sphere (numpy arrays) for benchmarks and CPU tests.
 
     Same sampling as make_plummer, but the potential used for the velocity
-    magnitudes is the smooth Plummer potential -1/sqrt(1 + r^2) and the
+    magnitudes is the smooth Plummer potential -1/sqrt(1 + r^2), the
     scaling to Henon units is the analytic one (length 3 pi / 16, velocity
-    its inverse square root), so no O(N^2) pass is needed.
+    its inverse square root), and the speeds are then scaled so that the
+    kinetic energy is the model's 1/4 (virial ratio 1/2 against its
+    potential energy -1/2, the role of make_plummer's scale_to_virial), so
+    no O(N^2) pass is needed.
     """
     rng = np.random.default_rng(seed)
     imf = imf or EqualMass()
@@ -118,4 +121,9 @@ def plummer_arrays(n, eps, imf=None, seed=0, mfrac=0.999):
     for k, (r, u) in zip("xyz", ((rx, vx), (ry, vy), (rz, vz))):
         d["r" + k] = (r - np.dot(mass, r)) * s
         d["v" + k] = (u - np.dot(mass, u)) / np.sqrt(s)
+    ke = 0.5 * np.dot(mass, d["vx"] ** 2 + d["vy"] ** 2 + d["vz"] ** 2)
+    if ke > 0:
+        f = np.sqrt(0.25 / ke)
+        for k in "xyz":
+            d["v" + k] = d["v" + k] * f
     return d
