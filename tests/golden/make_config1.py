@@ -4,7 +4,7 @@ Plummer N = 4096 (tupan_gb300.ics.plummer_arrays, seed 4096, eps = 0.01 so
 per-particle eps2 = 5e-5 and pair e2 = 1e-4), ahermite4 with eta = 0.01 from
 t = 0 to t = 1/8, integrated by the CPU restatement of the reference
 integrator (oracle/integrators.py, bit-identical to tupan/integrator/
-hermite.py with the reference C kernels).  About 4500 block steps; ~10 min
+hermite.py with the reference C kernels).  About 4100 block steps; ~11 min
 on 8 cores.
 
     python tests/golden/make_config1.py
