@@ -94,6 +94,68 @@ __device__ __forceinline__ double comp_value(const Comp &k) {
 }
 
 // ---------------------------------------------------------------------------
+// Double-single ("float-float") arithmetic: a value is hi + lo with
+// |lo| <= ulp(hi)/2, about 48 significant bits.  Built from the error-free
+// transformations of Knuth (TwoSum), Dekker (Fast2Sum) and the FMA form of
+// TwoProduct; every operation is an explicit round-to-nearest intrinsic so
+// the compiler cannot contract or reassociate them.
+// ---------------------------------------------------------------------------
+struct DS {
+    float hi, lo;
+};
+__device__ __forceinline__ DS ds_from(double x) {
+    DS r;
+    r.hi = __double2float_rn(x);
+    r.lo = __double2float_rn(x - (double)r.hi);
+    return r;
+}
+// s + e = a + b exactly (any magnitudes)
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// s + e = a + b exactly, given |a| >= |b| (or a == 0)
+__device__ __forceinline__ void fast_two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+__device__ __forceinline__ DS ds_add(DS a, DS b) {
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    DS r;
+    fast_two_sum(s, e, r.hi, r.lo);
+    return r;
+}
+__device__ __forceinline__ DS ds_neg(DS a) { return DS{-a.hi, -a.lo}; }
+__device__ __forceinline__ DS ds_mul(DS a, DS b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    DS r;
+    fast_two_sum(p, e, r.hi, r.lo);
+    return r;
+}
+// 1/sqrt(s) for s > 0: the hardware estimate refined by one Newton step
+// whose residual 1 - s y0^2 is formed in double-single (error ~2^-43).
+__device__ __forceinline__ DS ds_rsqrt(DS s) {
+    float y0;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y0) : "f"(s.hi));
+    DS y2;
+    y2.hi = __fmul_rn(y0, y0);
+    y2.lo = __fmaf_rn(y0, y0, -y2.hi);
+    const DS q = ds_mul(s, y2);
+    const DS r = ds_add(DS{1.0f, 0.0f}, ds_neg(q));
+    const float corr = __fmul_rn(__fmul_rn(y0, r.hi), 0.5f);
+    DS y;
+    fast_two_sum(y0, corr, y.hi, y.lo);
+    return y;
+}
+__device__ __forceinline__ double ds_value(DS a) { return (double)a.hi + (double)a.lo; }
+
+// ---------------------------------------------------------------------------
 // mbarrier / bulk-copy PTX (sm_90+ forms, valid on sm_103a).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {

@@ -721,6 +721,81 @@ __device__ __forceinline__ long long unit_owner(long long u, long long U, long l
 #ifndef TG_DS32_MINB
 #define TG_DS32_MINB 2
 #endif
+
+// i-tile t is finished for CTA k (units [u0, u1) of U, nju units per
+// i-tile, G CTAs).  If the CTA covered all of the tile's units it stores the
+// results; otherwise it hands its FP64 partials over (slot 0 for the tile it
+// started in, 1 for the tile it ends in) and the last contributor to arrive,
+// told by an atomic ticket (no waiting), sums every contributor's partials in
+// CTA order -- a deterministic result.  store(q, p) writes the final values of
+// the thread's q-th i-particle.
+template <class K, class Store>
+__device__ __forceinline__ void finish_itile(typename K::IS (&st)[K::IPT], long long t, long long nju, long long u0,
+                                             long long u1, long long U, long long G, long long k, double *part,
+                                             int *ticket, int *s_last, Store store) {
+    constexpr int IPT = K::IPT;
+    const int tid = threadIdx.x;
+    const long long ta = t * nju, tb = ta + nju;
+    if (ta >= u0 && tb <= u1) {
+#pragma unroll
+        for (int q = 0; q < IPT; ++q) {
+            double p[K::NP];
+            K::partials(st[q], p);
+            store(q, p);
+        }
+        return;
+    }
+    const int slot = (t == u0 / nju) ? 0 : 1;
+    double *mine = part + ((k * 2 + slot) * IPT * K::NP) * DS_THREADS;
+#pragma unroll
+    for (int q = 0; q < IPT; ++q) {
+        double p[K::NP];
+        K::partials(st[q], p);
+        for (int v = 0; v < K::NP; ++v) mine[(q * K::NP + v) * DS_THREADS + tid] = p[v];
+    }
+    __threadfence();
+    __syncthreads();
+    const long long klo = unit_owner(ta, U, G), khi = unit_owner(tb - 1, U, G);
+    if (tid == 0) {
+        const int prev = atomicAdd(&ticket[t], 1);
+        *s_last = (prev == (int)(khi - klo));
+    }
+    __syncthreads();
+    if (!*s_last) return;
+    // Sum the contributors' partials in CTA order; two contributors' loads
+    // are in flight per step.
+    __threadfence();
+    auto slot_ptr = [&](long long kk) {
+        const int sl = (t == unit_start(kk, U, G) / nju) ? 0 : 1;
+        return part + ((kk * 2 + sl) * IPT * K::NP) * DS_THREADS + tid;
+    };
+    double acc[IPT][K::NP];
+    {
+        const double *s0 = slot_ptr(klo);
+#pragma unroll
+        for (int q = 0; q < IPT; ++q)
+#pragma unroll
+            for (int w = 0; w < K::NP; ++w) acc[q][w] = __ldcg(s0 + (q * K::NP + w) * DS_THREADS);
+    }
+    for (long long kk = klo + 1; kk <= khi; kk += 2) {
+        const bool two = kk + 1 <= khi;
+        const double *s0 = slot_ptr(kk);
+        const double *s1 = two ? slot_ptr(kk + 1) : s0;
+#pragma unroll
+        for (int q = 0; q < IPT; ++q) {
+            double v0[K::NP], v1[K::NP];
+#pragma unroll
+            for (int w = 0; w < K::NP; ++w) {
+                v0[w] = __ldcg(s0 + (q * K::NP + w) * DS_THREADS);
+                v1[w] = __ldcg(s1 + (q * K::NP + w) * DS_THREADS);
+            }
+            K::combine(acc[q], v0);
+            if (two) K::combine(acc[q], v1);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < IPT; ++q) store(q, acc[q]);
+}
 template <class K, int JSUB>
 __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs a) {
     extern __shared__ __align__(128) float4 ring[];   // [DS_STAGES][DS_PAIRS * NQ]
@@ -829,71 +904,11 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
         if (tn == t) continue;
 
         // ---- i-tile t is done for this CTA: store or hand over partials ----
-        const long long ta = t * nju, tb = ta + nju;
-        if (ta >= u0 && tb <= u1) {
-#pragma unroll
-            for (int q = 0; q < IPT; ++q) {
-                const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
-                double p[K::NP];
-                K::partials(st[q], p);
-                if (i < a.p.ni) K::store(p, a.p, i);
-            }
-        } else {
-            const int slot = (t == u0 / nju) ? 0 : 1;
-            double *mine = a.part + ((k * 2 + slot) * IPT * K::NP) * DS_THREADS;
-#pragma unroll
-            for (int q = 0; q < IPT; ++q) {
-                double p[K::NP];
-                K::partials(st[q], p);
-                for (int v = 0; v < K::NP; ++v) mine[(q * K::NP + v) * DS_THREADS + tid] = p[v];
-            }
-            __threadfence();
-            __syncthreads();
-            const long long klo = unit_owner(ta, U, G), khi = unit_owner(tb - 1, U, G);
-            if (tid == 0) {
-                const int prev = atomicAdd(&a.ticket[t], 1);
-                s_last = (prev == (int)(khi - klo));
-            }
-            __syncthreads();
-            if (s_last) {
-                // Sum the contributors' partials in CTA order (deterministic);
-                // two contributors' loads are in flight per step.
-                __threadfence();
-                auto slot_ptr = [&](long long kk) {
-                    const int sl = (t == unit_start(kk, U, G) / nju) ? 0 : 1;
-                    return a.part + ((kk * 2 + sl) * IPT * K::NP) * DS_THREADS + tid;
-                };
-                double acc[IPT][K::NP];
-                {
-                    const double *s0 = slot_ptr(klo);
-#pragma unroll
-                    for (int q = 0; q < IPT; ++q)
-#pragma unroll
-                        for (int w = 0; w < K::NP; ++w) acc[q][w] = __ldcg(s0 + (q * K::NP + w) * DS_THREADS);
-                }
-                for (long long kk = klo + 1; kk <= khi; kk += 2) {
-                    const bool two = kk + 1 <= khi;
-                    const double *s0 = slot_ptr(kk);
-                    const double *s1 = two ? slot_ptr(kk + 1) : s0;
-#pragma unroll
-                    for (int q = 0; q < IPT; ++q) {
-                        double v0[K::NP], v1[K::NP];
-#pragma unroll
-                        for (int w = 0; w < K::NP; ++w) {
-                            v0[w] = __ldcg(s0 + (q * K::NP + w) * DS_THREADS);
-                            v1[w] = __ldcg(s1 + (q * K::NP + w) * DS_THREADS);
-                        }
-                        K::combine(acc[q], v0);
-                        if (two) K::combine(acc[q], v1);
-                    }
-                }
-#pragma unroll
-                for (int q = 0; q < IPT; ++q) {
-                    const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
-                    if (i < a.p.ni) K::store(acc[q], a.p, i);
-                }
-            }
-        }
+        finish_itile<K>(st, t, nju, u0, u1, U, G, k, a.part, a.ticket, &s_last,
+                        [&](int q, const double *p) {
+                            const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
+                            if (i < a.p.ni) K::store(p, a.p, i);
+                        });
         if (tn >= 0) {
             t = tn;
 #pragma unroll
@@ -916,6 +931,601 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
     }
 }
 
+
+
+// ===========================================================================
+// Ordered split-FP32 Acc and AccJerk (single-set calls of >= 2^24 pairs).
+//
+// Per call, tg_order.cu sorts the j-set (light particles in Morton order,
+// then the heavy ones, mass > max(m) / 32) and the i-set (Morton order), and
+// ds32_ord_prepare writes the j-records in that order with positions
+// relative to the centre c_b of their 64-j block.  The pairwise kernel then
+// decides per 64-j block, from the block's and the i-tile's bounding boxes:
+//   * far (box distance >= the block's half-extent): dx = fl(xi - c_b) - x'h,
+//     one subtraction per component; its error is at most
+//     eps (|xi - c_b| + |xj - c_b|) <= 3 eps |dx|;
+//   * near: the hi/lo difference (xi - c_b) - (xj - c_b), as accurate as
+//     the global hi/lo form;
+//   * heavy (the block holds heavy j): the near form with a Newton-refined
+//     1/sqrt and the compensated sums folded after every record, so the
+//     large terms of massive particles never sit in an FP32 lane sum.
+// The acceleration's FP32 lane sums are folded into Kahan sums every
+// 2 ORD_ACC_FOLD_PAIRS j, the jerk's every 64 j.  A per-i proxy of the sum
+// of term magnitudes (the sum of |folded lane sums|) travels with the
+// partials; particles whose proxy exceeds ORD_TAU |a| (strong cancellation)
+// are listed and their acceleration is recomputed in double-single
+// arithmetic (ds32_refine_acc).
+// ===========================================================================
+constexpr int ORD_BLOCK = 64;                              // j per block
+constexpr int ORD_BLOCK_PAIRS = ORD_BLOCK / 2;
+constexpr int ORD_BLOCKS_PER_TILE = DS_TILE / ORD_BLOCK;
+#ifndef TG_ORD_ACC_FOLD_PAIRS
+#define TG_ORD_ACC_FOLD_PAIRS 8
+#endif
+constexpr int ORD_ACC_FOLD_PAIRS = TG_ORD_ACC_FOLD_PAIRS;  // records per acceleration fold
+constexpr float ORD_THETA = 1.0f;
+constexpr float ORD_TAU = 20.0f;
+
+struct OrdInfo {
+    float4 c;    // block centre (x, y, z), half-extent
+    float4 lo;   // box minimum (x, y, z), heavy flag (1 or 0)
+    float4 hi;   // box maximum (x, y, z), unused
+};
+
+// x - c as a hi/lo pair from x = xh + xl (split_ds) and a float c: the same
+// float operations on the i-side and on the j-side, so one particle's two
+// relative positions are bit-identical and its self pair has dx = +0.
+__device__ __forceinline__ void rel_split(float xh, float xl, float c, float &h, float &l) {
+    float e;
+    two_sum(xh, -c, h, e);
+    l = __fadd_rn(e, xl);
+    h = fzero_norm(h);
+    l = fzero_norm(l);
+}
+// x - c rounded to one float (far blocks).
+__device__ __forceinline__ float rel_single(float xh, float xl, float c) {
+    return __fadd_rn(__fsub_rn(xh, c), xl);
+}
+
+// FORM of a 64-j block in the ordered kernels.
+enum : int { ORD_FAR = 0, ORD_NEAR = 1, ORD_HEAVY = 2 };
+
+template <int IPT_>
+struct AccJerkOrd {
+    static constexpr bool ORDERED = true;
+    static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 7, PX = 6;
+    static constexpr bool UE2 = true;
+    struct IS { float2 dh[3], dl[3]; float2 u, v, w, e; float2 a[3], j[3]; Comp ca[3], cj[3]; float px; };
+    __device__ static void load(IS &s, const PairArgs &a, size_t i) {
+        s.u = f2(__double2float_rn(a.I.f[F_VX][i]));
+        s.v = f2(__double2float_rn(a.I.f[F_VY][i]));
+        s.w = f2(__double2float_rn(a.I.f[F_VZ][i]));
+        s.e = f2(__double2float_rn(a.I.f[F_E2][i]));
+        for (int k = 0; k < 3; ++k) {
+            s.a[k] = f2(0.f); s.j[k] = f2(0.f);
+            s.ca[k] = Comp{0.f, 0.f}; s.cj[k] = Comp{0.f, 0.f};
+        }
+        s.px = 0.f;
+    }
+    // record: {x'h,y'h} {z'h,m} {vx,vy} {vz,e2} {x'l,y'l} {z'l,pad}
+    __device__ static void write_record(float *r, int lane, const float h[3], const float l[3], const PSet &J,
+                                        size_t j, bool valid) {
+        r[0 + lane] = h[0]; r[2 + lane] = h[1]; r[4 + lane] = h[2];
+        r[6 + lane] = valid ? __double2float_rn(J.f[F_M][j]) : 0.f;
+        r[8 + lane] = valid ? __double2float_rn(J.f[F_VX][j]) : 0.f;
+        r[10 + lane] = valid ? __double2float_rn(J.f[F_VY][j]) : 0.f;
+        r[12 + lane] = valid ? __double2float_rn(J.f[F_VZ][j]) : 0.f;
+        r[14 + lane] = valid ? __double2float_rn(J.f[F_E2][j]) : 1.f;
+        r[16 + lane] = l[0]; r[18 + lane] = l[1]; r[20 + lane] = l[2];
+        r[22 + lane] = 0.f;
+    }
+    template <int FORM, bool UE>
+    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R, float2 E) {
+        const float4 q0 = R[0], q1 = R[1], q2 = R[2], q3 = R[3];
+        float4 q4 = q0, q5 = q0;
+        if (FORM != ORD_FAR) { q4 = R[4]; q5 = R[5]; }
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+            IS &s = S[u];
+            float2 dx, dy, dz;
+            if (FORM == ORD_FAR) {
+                dx = sub2(s.dh[0], lo2(q0)); dy = sub2(s.dh[1], hi2(q0)); dz = sub2(s.dh[2], lo2(q1));
+            } else {
+                dx = add2(sub2(s.dh[0], lo2(q0)), sub2(s.dl[0], lo2(q4)));
+                dy = add2(sub2(s.dh[1], hi2(q0)), sub2(s.dl[1], hi2(q4)));
+                dz = add2(sub2(s.dh[2], lo2(q1)), sub2(s.dl[2], lo2(q5)));
+            }
+            const float2 du = sub2(s.u, lo2(q2)), dv = sub2(s.v, hi2(q2)), dw = sub2(s.w, lo2(q3));
+            const float2 e2 = UE ? E : add2(s.e, hi2(q3));
+            const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
+            float2 y, y2;
+            if (FORM == ORD_FAR) {   // far blocks hold no pair at r = 0
+                y = make_float2(rsqrt_hw(ss.x), rsqrt_hw(ss.y));
+                y2 = make_float2(rcp_hw(ss.x), rcp_hw(ss.y));
+            } else if (FORM == ORD_NEAR) {
+                inv_r_r2(ss, dx, dy, dz, y, y2);
+            } else {
+                y = inv_r<true>(ss, dx, dy, dz);
+                y2 = mul2(y, y);
+            }
+            const float2 mr3 = mul2(mul2(hi2(q1), y), y2);
+            const float2 rv = fma2(dx, du, fma2(dy, dv, mul2(dz, dw)));
+            const float2 al = mul2(mul2(rv, y2), f2(3.0f));
+            const float2 tu = fnma2(al, dx, du), tv = fnma2(al, dy, dv), tw = fnma2(al, dz, dw);
+            s.a[0] = fnma2(mr3, dx, s.a[0]);
+            s.a[1] = fnma2(mr3, dy, s.a[1]);
+            s.a[2] = fnma2(mr3, dz, s.a[2]);
+            s.j[0] = fnma2(mr3, tu, s.j[0]);
+            s.j[1] = fnma2(mr3, tv, s.j[1]);
+            s.j[2] = fnma2(mr3, tw, s.j[2]);
+        }
+    }
+    __device__ static void fold_acc(IS &s) {
+        for (int k = 0; k < 3; ++k) {
+            const float x = __fadd_rn(s.a[k].x, s.a[k].y);
+            comp_add(s.ca[k], x);
+            s.px = __fadd_rn(s.px, fabsf(x));
+            s.a[k] = f2(0.f);
+        }
+    }
+    __device__ static void fold_jerk(IS &s) {
+        for (int k = 0; k < 3; ++k) { comp_add(s.cj[k], __fadd_rn(s.j[k].x, s.j[k].y)); s.j[k] = f2(0.f); }
+    }
+    __device__ static void partials(const IS &s, double *p) {
+        for (int k = 0; k < 3; ++k) { p[k] = comp_value(s.ca[k]); p[3 + k] = comp_value(s.cj[k]); }
+        p[6] = (double)s.px;
+    }
+    __device__ static void combine(double *acc, const double *p) { for (int k = 0; k < NP; ++k) acc[k] += p[k]; }
+    __device__ static void store(const double *p, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 6; ++k) a.out[k][i] = p[k];
+    }
+};
+
+template <int IPT_>
+struct AccOrd {
+    static constexpr bool ORDERED = true;
+    static constexpr int IPT = IPT_, JF = 8, NQ = 4, NP = 4, PX = 3;
+    static constexpr bool UE2 = true;
+    struct IS { float2 dh[3], dl[3]; float2 e; float2 a[3]; Comp ca[3]; float px; };
+    __device__ static void load(IS &s, const PairArgs &a, size_t i) {
+        s.e = f2(__double2float_rn(a.I.f[F_E2][i]));
+        for (int k = 0; k < 3; ++k) { s.a[k] = f2(0.f); s.ca[k] = Comp{0.f, 0.f}; }
+        s.px = 0.f;
+    }
+    // record: {x'h,y'h} {z'h,m} {x'l,y'l} {z'l,e2}
+    __device__ static void write_record(float *r, int lane, const float h[3], const float l[3], const PSet &J,
+                                        size_t j, bool valid) {
+        r[0 + lane] = h[0]; r[2 + lane] = h[1]; r[4 + lane] = h[2];
+        r[6 + lane] = valid ? __double2float_rn(J.f[F_M][j]) : 0.f;
+        r[8 + lane] = l[0]; r[10 + lane] = l[1]; r[12 + lane] = l[2];
+        r[14 + lane] = valid ? __double2float_rn(J.f[F_E2][j]) : 1.f;
+    }
+    template <int FORM, bool UE>
+    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R, float2 E) {
+        const float4 q0 = R[0], q1 = R[1];
+        float4 q2 = q0, q3 = q1;
+        if (FORM != ORD_FAR || !UE) q3 = R[3];
+        if (FORM != ORD_FAR) q2 = R[2];
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+            IS &s = S[u];
+            float2 dx, dy, dz;
+            if (FORM == ORD_FAR) {
+                dx = sub2(s.dh[0], lo2(q0)); dy = sub2(s.dh[1], hi2(q0)); dz = sub2(s.dh[2], lo2(q1));
+            } else {
+                dx = add2(sub2(s.dh[0], lo2(q0)), sub2(s.dl[0], lo2(q2)));
+                dy = add2(sub2(s.dh[1], hi2(q0)), sub2(s.dl[1], hi2(q2)));
+                dz = add2(sub2(s.dh[2], lo2(q1)), sub2(s.dl[2], lo2(q3)));
+            }
+            const float2 e2 = UE ? E : add2(s.e, hi2(q3));
+            const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
+            // far blocks hold no pair at r = 0; with a uniform softening
+            // E > 1e-20 a pair at r = 0 has dx = +0 and adds exactly nothing
+            float2 y;
+            if (FORM == ORD_FAR || (FORM == ORD_NEAR && UE)) y = make_float2(rsqrt_hw(ss.x), rsqrt_hw(ss.y));
+            else y = inv_r<FORM == ORD_HEAVY>(ss, dx, dy, dz);
+            const float2 y2 = mul2(y, y);
+            const float2 mr3 = mul2(mul2(hi2(q1), y), y2);
+            s.a[0] = fnma2(mr3, dx, s.a[0]);
+            s.a[1] = fnma2(mr3, dy, s.a[1]);
+            s.a[2] = fnma2(mr3, dz, s.a[2]);
+        }
+    }
+    __device__ static void fold_acc(IS &s) {
+        for (int k = 0; k < 3; ++k) {
+            const float x = __fadd_rn(s.a[k].x, s.a[k].y);
+            comp_add(s.ca[k], x);
+            s.px = __fadd_rn(s.px, fabsf(x));
+            s.a[k] = f2(0.f);
+        }
+    }
+    __device__ static void fold_jerk(IS &) {}
+    __device__ static void partials(const IS &s, double *p) {
+        for (int k = 0; k < 3; ++k) p[k] = comp_value(s.ca[k]);
+        p[3] = (double)s.px;
+    }
+    __device__ static void combine(double *acc, const double *p) { for (int k = 0; k < NP; ++k) acc[k] += p[k]; }
+    __device__ static void store(const double *p, const PairArgs &a, size_t i) {
+        for (int k = 0; k < 3; ++k) a.out[k][i] = p[k];
+    }
+};
+
+// Records, block table, uniform-softening flags, the double-single j-data of
+// the recompute and zeroed counters; one CTA of DS_TILE threads per j-tile,
+// one sorted j per thread.  jd[3p..3p+2] = {xh, xl, yh, yl},
+// {zh, zl, mh, ml}, {e2h, e2l, 0, 0} of sorted j p.
+template <class K>
+__global__ void __launch_bounds__(DS_TILE) ds32_ord_prepare(PSet J, size_t nj, const int *pj, const unsigned *nlight,
+                                                            float *rec, OrdInfo *blk, float *tile_e2, int *ticket,
+                                                            long long nticket, int *flag_count, float4 *jd,
+                                                            int *ref_ticket, int nref_ticket) {
+    __shared__ float s_box[DS_TILE / 32][6];
+    __shared__ unsigned s_first;
+    const size_t tile = blockIdx.x;
+    const int q = threadIdx.x;
+    const size_t p = tile * DS_TILE + q;
+    const bool valid = p < nj;
+    const size_t j = valid ? (size_t)pj[p] : 0;
+    float xh[3], xl[3];
+    for (int c = 0; c < 3; ++c) split_ds(valid ? J.f[F_RX + c][j] : 0.0, xh[c], xl[c]);
+    // block box over the valid j (a block is two warps)
+    float lo[3], hi[3];
+    for (int c = 0; c < 3; ++c) {
+        lo[c] = (valid && isfinite(xh[c])) ? xh[c] : INFINITY;
+        hi[c] = (valid && isfinite(xh[c])) ? xh[c] : -INFINITY;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        for (int c = 0; c < 3; ++c) {
+            lo[c] = fminf(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+            hi[c] = fmaxf(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+        }
+    if ((q & 31) == 0)
+        for (int c = 0; c < 3; ++c) { s_box[q >> 5][c] = lo[c]; s_box[q >> 5][3 + c] = hi[c]; }
+    __syncthreads();
+    const int b = q / ORD_BLOCK, w0 = 2 * b;
+    float cc[3], ext = 0.f;
+    for (int c = 0; c < 3; ++c) {
+        lo[c] = fminf(s_box[w0][c], s_box[w0 + 1][c]);
+        hi[c] = fmaxf(s_box[w0][3 + c], s_box[w0 + 1][3 + c]);
+        if (!(lo[c] <= hi[c])) lo[c] = hi[c] = 0.f;   // no valid, finite coordinate
+        cc[c] = __fmul_rn(0.5f, __fadd_rn(lo[c], hi[c]));
+        if (!isfinite(cc[c])) cc[c] = 0.f;
+        ext = fmaxf(ext, fmaxf(__fsub_rn(hi[c], cc[c]), __fsub_rn(cc[c], lo[c])));
+    }
+    ext = __fmul_ru(ext, 1.0f + 0x1p-20f);
+    const size_t gb = tile * ORD_BLOCKS_PER_TILE + b;
+    if ((q % ORD_BLOCK) == 0) {
+        const size_t start = gb * ORD_BLOCK;
+        const bool heavy = start < nj && start + ORD_BLOCK > (size_t)*nlight;
+        OrdInfo info;
+        info.c = make_float4(cc[0], cc[1], cc[2], ext);
+        info.lo = make_float4(lo[0], lo[1], lo[2], heavy ? 1.f : 0.f);
+        info.hi = make_float4(hi[0], hi[1], hi[2], 0.f);
+        blk[gb] = info;
+    }
+    // the record: positions relative to the block centre
+    float h[3], l[3];
+    for (int c = 0; c < 3; ++c) {
+        if (valid) rel_split(xh[c], xl[c], cc[c], h[c], l[c]);
+        else { h[c] = 0.f; l[c] = 0.f; }
+    }
+    K::write_record(rec + (p >> 1) * (size_t)(2 * K::JF), (int)(p & 1), h, l, J, j, valid);
+    if (valid) {
+        float mh, ml, eh, el;
+        split_ds(J.f[F_M][j], mh, ml);
+        split_ds(J.f[F_E2][j], eh, el);
+        jd[3 * p] = make_float4(xh[0], xl[0], xh[1], xl[1]);
+        jd[3 * p + 1] = make_float4(xh[2], xl[2], mh, ml);
+        jd[3 * p + 2] = make_float4(eh, el, 0.f, 0.f);
+    }
+    if (tile_e2 != nullptr) {   // the tile's common float softening, or NaN
+        const unsigned mine = valid ? __float_as_uint(__double2float_rn(J.f[F_E2][j])) : 0u;
+        if (q == 0) s_first = mine;   // the tile's first j is always valid
+        __syncthreads();
+        const bool same = __syncthreads_and(!valid || mine == s_first);
+        if (q == 0) {
+            const float v = __uint_as_float(s_first);
+            tile_e2[tile] = (same && v == v) ? v : __uint_as_float(0x7fc00000u);
+        }
+    }
+    const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t x = g; x < (size_t)nticket; x += stride) ticket[x] = 0;
+    for (size_t x = g; x < (size_t)nref_ticket; x += stride) ref_ticket[x] = 0;
+    if (g == 0) *flag_count = 0;
+}
+
+// Float bounding box of each i-tile of blockDim.x sorted i-particles.
+__global__ void ds32_ord_ibox(PSet I, size_t ni, const int *pi, float4 *ibox) {
+    __shared__ float s_box[32][6];
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float lo[3], hi[3];
+    for (int c = 0; c < 3; ++c) {
+        const float x = p < ni ? __double2float_rn(I.f[F_RX + c][pi[p]]) : NAN;
+        lo[c] = isfinite(x) ? x : INFINITY;
+        hi[c] = isfinite(x) ? x : -INFINITY;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        for (int c = 0; c < 3; ++c) {
+            lo[c] = fminf(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+            hi[c] = fmaxf(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+        }
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+        for (int c = 0; c < 3; ++c) { s_box[w][c] = lo[c]; s_box[w][3 + c] = hi[c]; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int v = 1; v < nw; ++v)
+            for (int c = 0; c < 3; ++c) { lo[c] = fminf(lo[c], s_box[v][c]); hi[c] = fmaxf(hi[c], s_box[v][3 + c]); }
+        ibox[2 * blockIdx.x] = make_float4(lo[0], lo[1], lo[2], 0.f);
+        ibox[2 * blockIdx.x + 1] = make_float4(hi[0], hi[1], hi[2], 0.f);
+    }
+}
+
+struct DsOrdArgs {
+    DsArgs d;
+    const int *pi;          // sorted i position -> i index
+    const OrdInfo *blk;     // per 64-j block
+    const float4 *ibox;     // per i-tile: min, max
+    int *flag_count, *flag_list;
+};
+
+// One 64-j block of FORM against the thread's i-particles: acceleration
+// folds every ORD_ACC_FOLD_PAIRS records, jerk fold at the end (heavy
+// blocks: both after every record).
+template <class K, int FORM, bool UE>
+__device__ __forceinline__ void ord_block(typename K::IS (&st)[K::IPT], const float4 *R, float2 E) {
+    if constexpr (FORM == ORD_HEAVY) {
+#pragma unroll 1
+        for (int r = 0; r < ORD_BLOCK_PAIRS; ++r) {
+            K::template step<FORM, UE>(st, R + r * K::NQ, E);
+#pragma unroll
+            for (int q = 0; q < K::IPT; ++q) { K::fold_acc(st[q]); K::fold_jerk(st[q]); }
+        }
+    } else {
+#pragma unroll 1
+        for (int r0 = 0; r0 < ORD_BLOCK_PAIRS; r0 += ORD_ACC_FOLD_PAIRS) {
+#pragma unroll
+            for (int r = 0; r < ORD_ACC_FOLD_PAIRS; ++r) K::template step<FORM, UE>(st, R + (r0 + r) * K::NQ, E);
+#pragma unroll
+            for (int q = 0; q < K::IPT; ++q) K::fold_acc(st[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < K::IPT; ++q) K::fold_jerk(st[q]);
+    }
+}
+
+template <class K, int JSUB>
+__global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs oa) {
+    extern __shared__ __align__(128) float4 ring[];   // [DS_STAGES][DS_PAIRS * NQ]
+    __shared__ __align__(8) uint64_t full[DS_STAGES];
+    __shared__ int s_last;
+    __shared__ float s_xi[6][DS_THREADS * K::IPT];     // i-tile positions: hi x, y, z, lo x, y, z
+    const DsArgs &a = oa.d;
+    constexpr int IPT = K::IPT;
+    constexpr int TILE_Q = DS_PAIRS * K::NQ;
+    constexpr int BI = DS_THREADS * IPT;
+    constexpr int PART_PAIRS = DS_PAIRS / JSUB;
+    constexpr int PART_Q = PART_PAIRS * K::NQ;
+    constexpr int PART_BLOCKS = PART_PAIRS / ORD_BLOCK_PAIRS;
+    const long long nju = a.njt * JSUB;
+    const long long U = a.nit * nju;
+    const long long G = gridDim.x;
+    const long long k = blockIdx.x;
+    const long long u0 = unit_start(k, U, G), u1 = unit_start(k + 1, U, G);
+    if (u0 >= u1) return;
+    const int tid = threadIdx.x;
+
+    if (tid == 0) {
+        for (int s = 0; s < DS_STAGES; ++s) mbar_init(&full[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    auto issue = [&](long long u, int s) {
+        const long long jp = u % nju;
+        constexpr unsigned bytes = (unsigned)(PART_Q * sizeof(float4));
+        mbar_expect_tx(&full[s], bytes);
+        bulk_g2s(ring + s * TILE_Q, a.rec + jp * PART_Q, bytes, &full[s]);
+    };
+    if (tid == 0) {
+        for (int s = 0; s < DS_STAGES && u0 + s < u1; ++s) issue(u0 + s, s);
+    }
+
+    const size_t ni = a.p.ni;
+    long long t = u0 / nju;
+    typename K::IS st[IPT];
+    float4 ilo, ihi;
+    auto load_tile = [&](long long tt) {
+#pragma unroll
+        for (int q = 0; q < IPT; ++q) {
+            const size_t ii = (size_t)tt * BI + q * DS_THREADS + tid;
+            const size_t i = (size_t)oa.pi[ii < ni ? ii : ni - 1];
+            K::load(st[q], a.p, i);
+            for (int c = 0; c < 3; ++c) {
+                float h, l;
+                split_ds(a.p.I.f[F_RX + c][i], h, l);
+                s_xi[c][q * DS_THREADS + tid] = h;
+                s_xi[3 + c][q * DS_THREADS + tid] = l;
+            }
+        }
+        ilo = __ldg(oa.ibox + 2 * tt);
+        ihi = __ldg(oa.ibox + 2 * tt + 1);
+    };
+    load_tile(t);
+    __shared__ unsigned s_ie2;
+    auto tile_ie2 = [&]() -> float {
+        if (tid == 0) s_ie2 = __float_as_uint(st[0].e.x);
+        __syncthreads();
+        bool same = true;
+#pragma unroll
+        for (int q = 0; q < IPT; ++q) same &= __float_as_uint(st[q].e.x) == s_ie2;
+        same = __syncthreads_and(same);
+        return same ? __uint_as_float(s_ie2) : __uint_as_float(0x7fc00000u);
+    };
+    float ie2 = tile_ie2();
+    bool aborted = false;
+    long long abort_u = u1;
+    long long issued_to = (u0 + DS_STAGES < u1) ? u0 + DS_STAGES : u1;
+
+    for (long long u = u0, it = 0; u < u1; ++u, ++it) {
+        const int s = (int)(it % DS_STAGES);
+        const uint32_t parity = (uint32_t)((it / DS_STAGES) & 1);
+        if (!mbar_wait(&full[s], parity)) aborted = true;
+        if (__syncthreads_or(aborted)) {
+            aborted = true;
+            abort_u = u;
+            break;
+        }
+        const float4 *R = ring + s * TILE_Q;
+        const long long jp = u % nju, jt = jp / JSUB;
+        const float ue = __fadd_rn(ie2, __ldg(a.tile_e2 + jt));
+        const bool UEok = ue > 1e-20f;   // NaN (not uniform) takes the per-pair softening
+        const float2 E = f2(ue);
+#pragma unroll 1
+        for (int bl = 0; bl < PART_BLOCKS; ++bl) {
+            const long long gb = jt * ORD_BLOCKS_PER_TILE + (jp % JSUB) * PART_BLOCKS + bl;
+            const float4 bc = __ldg(&oa.blk[gb].c), blo = __ldg(&oa.blk[gb].lo), bhi = __ldg(&oa.blk[gb].hi);
+            const bool heavy = blo.w != 0.f;
+            bool far = false;
+            if (!heavy) {
+                const float gx = fmaxf(0.f, fmaxf(ilo.x - bhi.x, blo.x - ihi.x));
+                const float gy = fmaxf(0.f, fmaxf(ilo.y - bhi.y, blo.y - ihi.y));
+                const float gz = fmaxf(0.f, fmaxf(ilo.z - bhi.z, blo.z - ihi.z));
+                const float d2 = gx * gx + gy * gy + gz * gz;
+                const float cm = fmaxf(fabsf(bc.x), fmaxf(fabsf(bc.y), fabsf(bc.z)));
+                const float th = fmaxf(ORD_THETA * bc.w, cm * 0x1p-16f);
+                far = d2 > 0.f && d2 >= th * th;
+            }
+            const float cc[3] = {bc.x, bc.y, bc.z};
+            const float4 *Rb = R + bl * ORD_BLOCK_PAIRS * K::NQ;
+            if (far) {
+#pragma unroll
+                for (int q = 0; q < IPT; ++q)
+                    for (int c = 0; c < 3; ++c) {
+                        const int x = q * DS_THREADS + tid;
+                        st[q].dh[c] = f2(rel_single(s_xi[c][x], s_xi[3 + c][x], cc[c]));
+                    }
+                if (UEok) ord_block<K, ORD_FAR, true>(st, Rb, E);
+                else ord_block<K, ORD_FAR, false>(st, Rb, E);
+            } else {
+#pragma unroll
+                for (int q = 0; q < IPT; ++q)
+                    for (int c = 0; c < 3; ++c) {
+                        const int x = q * DS_THREADS + tid;
+                        float h, l;
+                        rel_split(s_xi[c][x], s_xi[3 + c][x], cc[c], h, l);
+                        st[q].dh[c] = f2(h);
+                        st[q].dl[c] = f2(l);
+                    }
+                if (heavy) ord_block<K, ORD_HEAVY, false>(st, Rb, E);
+                else if (UEok) ord_block<K, ORD_NEAR, true>(st, Rb, E);
+                else ord_block<K, ORD_NEAR, false>(st, Rb, E);
+            }
+        }
+        __syncthreads();   // stage s fully consumed
+        if (tid == 0 && u + DS_STAGES < u1) {
+            issue(u + DS_STAGES, s);
+            issued_to = u + DS_STAGES + 1;
+        }
+        const long long tn = (u + 1 < u1) ? (u + 1) / nju : -1;
+        if (tn == t) continue;
+        finish_itile<K>(st, t, nju, u0, u1, U, G, k, a.part, a.ticket, &s_last,
+                        [&](int q, const double *p) {
+                            const size_t ii = (size_t)t * BI + q * DS_THREADS + tid;
+                            if (ii >= ni) return;
+                            const size_t i = (size_t)oa.pi[ii];
+                            K::store(p, a.p, i);
+                            const double am = sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+                            if (!(p[K::PX] <= (double)ORD_TAU * am)) {
+                                const int f = atomicAdd(oa.flag_count, 1);
+                                oa.flag_list[f] = (int)i;
+                            }
+                        });
+        if (tn >= 0) {
+            t = tn;
+            load_tile(t);
+            ie2 = tile_ie2();
+        }
+    }
+
+    if (aborted && tid == 0) {
+        atomicOr(a.p.status, ST_MBAR_TIMEOUT);
+        for (long long u = abort_u; u < issued_to; ++u) {
+            const long long it = u - u0;
+            mbar_wait(&full[it % DS_STAGES], (uint32_t)((it / DS_STAGES) & 1));
+        }
+    }
+}
+
+// Acceleration of the listed i-particles against every j in double-single
+// arithmetic (~2^-43 per term), from the hi/lo floats ds32_ord_prepare
+// wrote (no FP64 operation in the loop).  With F listed particles and G
+// CTAs, each particle's j-range is cut into nch = clamp(G / F, 1,
+// REFINE_MAX_CHUNKS) chunks; a CTA reduces a chunk in a fixed-order tree,
+// and with nch > 1 the last chunk of a particle to finish (atomic ticket)
+// adds the chunk sums in chunk order: the result is deterministic.  Pairs
+// at r = 0 are excluded as in the reference (acc_kernel_common.h: r2 > 0).
+constexpr int REFINE_THREADS = 256;
+constexpr int REFINE_MAX_CHUNKS = 16;
+constexpr int REFINE_MAX_SPLIT = 512;   // particles that may be split (ticket and partial slots)
+__global__ void __launch_bounds__(REFINE_THREADS) ds32_refine_acc(PairArgs a, const float4 *jd, const int *flag_count,
+                                                                  const int *flag_list, double *partial,
+                                                                  int *ref_ticket) {
+    __shared__ double red[3][REFINE_THREADS];
+    __shared__ int s_last;
+    const int F = *flag_count;
+    if (F == 0) return;
+    const int G = gridDim.x, tid = threadIdx.x;
+    int nch = G / F;
+    nch = nch < 1 ? 1 : (nch > REFINE_MAX_CHUNKS ? REFINE_MAX_CHUNKS : nch);
+    if (F > REFINE_MAX_SPLIT) nch = 1;
+    const long long W = (long long)F * nch;
+    const size_t nj = a.nj;
+    for (long long w = blockIdx.x; w < W; w += G) {
+        const int f = (int)(w / nch), ch = (int)(w % nch);
+        const size_t i = (size_t)flag_list[f];
+        const size_t j0 = nj * ch / nch, j1 = nj * (ch + 1) / nch;
+        DS xi[3];
+        for (int c = 0; c < 3; ++c) xi[c] = ds_from(a.I.f[F_RX + c][i]);
+        const DS ie2 = ds_from(a.I.f[F_E2][i]);
+        DS acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        for (size_t p = j0 + tid; p < j1; p += REFINE_THREADS) {
+            const float4 A = __ldg(jd + 3 * p), B = __ldg(jd + 3 * p + 1), C = __ldg(jd + 3 * p + 2);
+            DS d[3];
+            d[0] = ds_add(xi[0], DS{-A.x, -A.y});
+            d[1] = ds_add(xi[1], DS{-A.z, -A.w});
+            d[2] = ds_add(xi[2], DS{-B.x, -B.y});
+            const DS r2 = ds_add(ds_add(ds_mul(d[0], d[0]), ds_mul(d[1], d[1])), ds_mul(d[2], d[2]));
+            if (!(r2.hi > 0.f)) continue;
+            const DS s2 = ds_add(r2, ds_add(ie2, DS{C.x, C.y}));
+            const DS y = ds_rsqrt(s2);
+            const DS mr3 = ds_mul(DS{B.z, B.w}, ds_mul(ds_mul(y, y), y));
+            for (int c = 0; c < 3; ++c) acc[c] = ds_add(acc[c], ds_neg(ds_mul(mr3, d[c])));
+        }
+        for (int c = 0; c < 3; ++c) red[c][tid] = ds_value(acc[c]);
+        __syncthreads();
+        for (int h = REFINE_THREADS / 2; h > 0; h >>= 1) {
+            if (tid < h)
+                for (int c = 0; c < 3; ++c) red[c][tid] += red[c][tid + h];
+            __syncthreads();
+        }
+        if (nch == 1) {
+            if (tid == 0)
+                for (int c = 0; c < 3; ++c) a.out[c][i] = red[c][0];
+        } else if (tid == 0) {
+            for (int c = 0; c < 3; ++c) partial[((size_t)f * REFINE_MAX_CHUNKS + ch) * 3 + c] = red[c][0];
+            __threadfence();
+            s_last = atomicAdd(ref_ticket + f, 1) == nch - 1;
+            if (s_last) {
+                __threadfence();
+                double v[3] = {0.0, 0.0, 0.0};
+                for (int r = 0; r < nch; ++r)
+                    for (int c = 0; c < 3; ++c) v[c] += __ldcg(partial + ((size_t)f * REFINE_MAX_CHUNKS + r) * 3 + c);
+                for (int c = 0; c < 3; ++c) a.out[c][i] = v[c];
+            }
+        }
+        __syncthreads();
+    }
+}
 
 // ---------------------------------------------------------------------------
 // Segmented (ensemble) form: many independent clusters in one launch.
@@ -1178,13 +1788,42 @@ static int ctas_per_sm() {
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+template <class K, class = void>
+struct is_ordered : std::false_type {};
+template <class K>
+struct is_ordered<K, std::void_t<decltype(K::ORDERED)>> : std::true_type {};
+
+// Resident CTAs per SM of the ordered kernel for K (as ctas_per_sm).
+template <class K>
+static int ctas_per_sm_ord() {
+    static std::atomic<int> cached{-1};
+    int c = cached.load(std::memory_order_acquire);
+    if (c < 0) {
+        const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
+        cudaFuncSetAttribute(ds32_ord<K, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(ds32_ord<K, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ds32_ord<K, 1>, DS_THREADS, smem) != cudaSuccess || n < 1)
+            n = 1;
+        cached.store(n, std::memory_order_release);
+        c = n;
+    }
+    return c;
+}
+
+template <class K>
+static int ctas_for() {
+    if constexpr (is_ordered<K>::value) return ctas_per_sm_ord<K>();
+    else return ctas_per_sm<K>();
+}
+
 template <class K>
 static Geometry geometry(size_t ni, size_t nj, int sms) {
     Geometry g;
     const size_t bi = (size_t)DS_THREADS * K::IPT;
     g.nit = (long long)((ni + bi - 1) / bi);
     g.njt = (long long)((nj + DS_TILE - 1) / DS_TILE);
-    const long long slots = (long long)sms * ctas_per_sm<K>();
+    const long long slots = (long long)sms * ctas_for<K>();
     // Split j-tiles in two when there are fewer than two units per CTA slot,
     // or when halving the units evens out the CTAs' shares by 10% or more:
     // a CTA's time is its whole-unit count, ceil(U / slots) units of size
@@ -1314,6 +1953,95 @@ static cudaError_t run_ds_capped(const PairArgs &p, void *ws, size_t ws_bytes, i
 
 
 // ---------------------------------------------------------------------------
+// Ordered launch (Acc, AccJerk): spatial order, records with block-relative
+// positions, block and i-tile boxes, the pairwise kernel, then the
+// double-single recompute of the particles it flagged.
+// ---------------------------------------------------------------------------
+struct OrdLayout {
+    Geometry g;
+    size_t blk_bytes, ibox_bytes, flag_bytes, jd_bytes, ref_bytes, order_bytes;
+    size_t total() const {
+        return g.rec_bytes + g.part_bytes + g.ticket_bytes + g.tile_bytes + blk_bytes + ibox_bytes + flag_bytes +
+               jd_bytes + ref_bytes + order_bytes;
+    }
+};
+
+template <class K>
+static OrdLayout ord_layout(size_t ni, size_t nj, int sms, bool same) {
+    OrdLayout L;
+    L.g = geometry<K>(ni, nj, sms);
+    L.blk_bytes = align_up((size_t)L.g.njt * ORD_BLOCKS_PER_TILE * sizeof(OrdInfo), 256);
+    L.ibox_bytes = align_up((size_t)L.g.nit * 2 * sizeof(float4), 256);
+    L.flag_bytes = align_up((ni + 64) * sizeof(int), 256);
+    L.jd_bytes = align_up(nj * 3 * sizeof(float4), 256);
+    L.ref_bytes = align_up((size_t)REFINE_MAX_SPLIT * (REFINE_MAX_CHUNKS * 3 * sizeof(double) + sizeof(int)), 256);
+    L.order_bytes = order_workspace_bytes(ni, nj, same);
+    return L;
+}
+
+// The ordered path serves calls of at least 2^24 pairs.
+static bool ord_applies(size_t ni, size_t nj) {
+    return ni >= 512 && nj >= 512 && (double)ni * (double)nj >= 16777216.0 && nj < ((size_t)1 << 30);
+}
+
+static bool same_sets(const PairArgs &p, int nfields) {
+    if (p.ni != p.nj) return false;
+    for (int f = 0; f < nfields; ++f)
+        if (p.I.f[f] != p.J.f[f]) return false;
+    return true;
+}
+
+template <class K>
+static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_bytes, int sms, cudaStream_t s) {
+    const bool same = same_sets(p, nfields);
+    const OrdLayout L = ord_layout<K>(p.ni, p.nj, sms, same);
+    const Geometry &g = L.g;
+    if (L.total() > ws_bytes) return cudaErrorInvalidValue;
+    char *q = static_cast<char *>(ws);
+    float *rec = reinterpret_cast<float *>(q); q += g.rec_bytes;
+    double *part = reinterpret_cast<double *>(q); q += g.part_bytes;
+    int *ticket = reinterpret_cast<int *>(q); q += g.ticket_bytes;
+    float *tile_e2 = reinterpret_cast<float *>(q); q += g.tile_bytes;
+    OrdInfo *blk = reinterpret_cast<OrdInfo *>(q); q += L.blk_bytes;
+    float4 *ibox = reinterpret_cast<float4 *>(q); q += L.ibox_bytes;
+    int *flags = reinterpret_cast<int *>(q); q += L.flag_bytes;   // [0] count, [64..] list
+    float4 *jd = reinterpret_cast<float4 *>(q); q += L.jd_bytes;
+    double *ref_part = reinterpret_cast<double *>(q);
+    int *ref_ticket = reinterpret_cast<int *>(ref_part + (size_t)REFINE_MAX_SPLIT * REFINE_MAX_CHUNKS * 3);
+    q += L.ref_bytes;
+    void *order_ws = q;
+
+    OrderOut o;
+    cudaError_t e = build_order(p.I, p.ni, p.J, p.nj, same, order_ws, L.order_bytes, o, s);
+    if (e != cudaSuccess) return e;
+    ds32_ord_prepare<K><<<(unsigned)g.njt, DS_TILE, 0, s>>>(p.J, p.nj, o.pj, o.nlight, rec, blk, tile_e2, ticket,
+                                                          g.nit, flags, jd, ref_ticket, REFINE_MAX_SPLIT);
+    constexpr int BI = DS_THREADS * K::IPT;
+    ds32_ord_ibox<<<(unsigned)g.nit, BI, 0, s>>>(p.I, p.ni, o.pi, ibox);
+
+    DsOrdArgs a;
+    a.d.p = p;
+    a.d.rec = reinterpret_cast<const float4 *>(rec);
+    a.d.part = part;
+    a.d.ticket = ticket;
+    a.d.tile_e2 = tile_e2;
+    a.d.nit = g.nit;
+    a.d.njt = g.njt;
+    a.d.mode = nullptr;
+    a.d.run_mode = 0;
+    a.pi = o.pi;
+    a.blk = blk;
+    a.ibox = ibox;
+    a.flag_count = flags;
+    a.flag_list = flags + 64;
+    const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
+    if (g.jsub == 2) ds32_ord<K, 2><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
+    else ds32_ord<K, 1><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
+    ds32_refine_acc<<<(unsigned)(sms * 4), REFINE_THREADS, 0, s>>>(p, jd, flags, flags + 64, ref_part, ref_ticket);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Segmented launch.  Host tables (per cluster, nondecreasing prefixes) are
 // built by the caller for this kernel's i-tile size; `dev` points to the
 // same tables on the device in the order unit_off[C+1], itile_off[C+1],
@@ -1415,8 +2143,12 @@ bool ds32_supported(int kernel) { return kernel != K_SAKURA && kernel >= 0 && ke
 size_t ds32_workspace_bytes(int kernel, size_t ni, size_t nj, int sms) {
     switch (kernel) {
         case K_PHI: return ws_pick<PhiDS<IPT2, REF>, PhiDS<1, REF>>(ni, nj, sms);
-        case K_ACC: return ws_pick<AccDS<IPT2, REF>, AccDS<1, REF>>(ni, nj, sms);
-        case K_ACC_JERK: return ws_pick<AccJerkDS<IPT2, REF>, AccJerkDS<1, REF>>(ni, nj, sms);
+        case K_ACC:
+            if (ord_applies(ni, nj)) return ord_layout<AccOrd<2>>(ni, nj, sms, false).total();
+            return ws_pick<AccDS<IPT2, REF>, AccDS<1, REF>>(ni, nj, sms);
+        case K_ACC_JERK:
+            if (ord_applies(ni, nj)) return ord_layout<AccJerkOrd<2>>(ni, nj, sms, false).total();
+            return ws_pick<AccJerkDS<IPT2, REF>, AccJerkDS<1, REF>>(ni, nj, sms);
         case K_SNAP_CRACKLE: return ws_bytes_for<SnapCrackleDS<1, REF>>(ni, nj, sms);
         case K_TSTEP: return ws_pick<TstepDS<IPT2, REF>, TstepDS<1, REF>>(ni, nj, sms);
         case K_PNACC: return ws_bytes_for<PNAccDS<1, REF>>(ni, nj, sms);
@@ -1428,8 +2160,12 @@ size_t ds32_workspace_bytes(int kernel, size_t ni, size_t nj, int sms) {
 cudaError_t launch_ds32(int kernel, const PairArgs &a, void *ws, size_t ws_bytes, int sms, cudaStream_t s) {
     switch (kernel) {
         case K_PHI: return run_pick<PhiDS<IPT2, REF>, PhiDS<1, REF>>(a, ws, ws_bytes, sms, s);
-        case K_ACC: return run_pick<AccDS<IPT2, REF>, AccDS<1, REF>>(a, ws, ws_bytes, sms, s);
-        case K_ACC_JERK: return run_pick<AccJerkDS<IPT2, REF>, AccJerkDS<1, REF>>(a, ws, ws_bytes, sms, s);
+        case K_ACC:
+            if (ord_applies(a.ni, a.nj)) return run_ord<AccOrd<2>>(a, 5, ws, ws_bytes, sms, s);
+            return run_pick<AccDS<IPT2, REF>, AccDS<1, REF>>(a, ws, ws_bytes, sms, s);
+        case K_ACC_JERK:
+            if (ord_applies(a.ni, a.nj)) return run_ord<AccJerkOrd<2>>(a, 8, ws, ws_bytes, sms, s);
+            return run_pick<AccJerkDS<IPT2, REF>, AccJerkDS<1, REF>>(a, ws, ws_bytes, sms, s);
         case K_SNAP_CRACKLE: return run_ds<SnapCrackleDS<1, REF>>(a, ws, ws_bytes, sms, s);
         case K_TSTEP: return run_pick<TstepDS<IPT2, REF>, TstepDS<1, REF>>(a, ws, ws_bytes, sms, s);
         case K_PNACC: return run_ds<PNAccDS<1, REF>>(a, ws, ws_bytes, sms, s);

@@ -91,6 +91,18 @@ cudaError_t launch_fp64_seg(int kernel, const PairArgs &a, long long C, long lon
                             const long long *block_off, const long long *seg_start, const long long *seg_n,
                             cudaStream_t s);
 
+// Spatial ordering of the particle sets for the ordered split-FP32 Acc and
+// AccJerk (tg_order.cu).  pj: sorted j position -> j index (light particles
+// in Morton order, then the heavy ones); pi: the same for the i-set (pj
+// itself when `same`); *nlight: number of light j (device).
+struct OrderOut {
+    const int *pi, *pj;
+    const unsigned *nlight;
+};
+size_t order_workspace_bytes(size_t ni, size_t nj, bool same);
+cudaError_t build_order(const PSet &I, size_t ni, const PSet &J, size_t nj, bool same, void *ws,
+                        size_t ws_bytes, OrderOut &out, cudaStream_t s);
+
 // Record `msg` as this thread's tg_last_error() text.
 void set_last_error(const char *msg);
 

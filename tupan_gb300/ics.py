@@ -6,7 +6,9 @@ set_vel: |v| = sqrt(-2 q phi) with q drawn from the triangular density
 2(1 - q) by pairwise rejection; per-particle eps2 = eps^2 / 2 for constant
 softening; then com_to_origin, to_nbody_units and scale_to_virial) and of
 tupan/ics/fewbody.py:13-50 (a two-body orbit of given a, e).  The potential
-used for the velocities and the unit scalings comes from the GPU Phi kernel.
+used by make_plummer for the velocities and the unit scalings comes from the
+GPU Phi kernel; plummer_arrays needs no GPU and imports nothing of the
+compiled library (the CPU baseline builds its workload with it).
 Random numbers come from numpy.random.Generator(PCG64(seed)).
 
 The Salpeter IMF draws dN/dm ~ m^-2.35 on [mlow, mhigh] by inverse CDF; the
@@ -14,9 +16,6 @@ reference's IMF class refuses mlow < 0.4 (ics/imf.py:85-88), so this one is
 used for the [0.1, 100] range of the precision workload.
 """
 import numpy as np
-import torch
-
-from .particles import ParticleSystem
 
 
 class Salpeter(object):
@@ -58,6 +57,7 @@ def triangular(n, rng):
 def make_plummer(n, eps, imf=None, seed=0, device=None, prec="float64"):
     """Plummer sphere in N-body (Henon) units: M = 1, E = -1/4, Q = 1/2."""
     from .lib import extensions
+    from .particles import ParticleSystem
     rng = np.random.default_rng(seed)
     imf = imf or EqualMass()
     mass = imf.sample(n, rng)
