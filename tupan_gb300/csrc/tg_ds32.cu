@@ -963,6 +963,13 @@ constexpr int ORD_BLOCKS_PER_TILE = DS_TILE / ORD_BLOCK;
 #define TG_ORD_ACC_FOLD_PAIRS 8
 #endif
 constexpr int ORD_ACC_FOLD_PAIRS = TG_ORD_ACC_FOLD_PAIRS;  // records per acceleration fold
+#ifndef TG_ORD_UNROLL
+#define TG_ORD_UNROLL 8    // records per unrolled body of the far and near forms
+#endif
+#ifndef TG_ORD_FAR_RCP
+#define TG_ORD_FAR_RCP 1   // far blocks take 1/s from MUFU.RCP (else y * y on the FMA pipe)
+#endif
+constexpr int ORD_UNROLL = TG_ORD_UNROLL;
 constexpr float ORD_THETA = 1.0f;
 constexpr float ORD_TAU = 20.0f;
 
@@ -1041,7 +1048,11 @@ struct AccJerkOrd {
             float2 y, y2;
             if (FORM == ORD_FAR) {   // far blocks hold no pair at r = 0
                 y = make_float2(rsqrt_hw(ss.x), rsqrt_hw(ss.y));
+#if TG_ORD_FAR_RCP
                 y2 = make_float2(rcp_hw(ss.x), rcp_hw(ss.y));
+#else
+                y2 = mul2(y, y);
+#endif
             } else if (FORM == ORD_NEAR) {
                 inv_r_r2(ss, dx, dy, dz, y, y2);
             } else {
@@ -1284,7 +1295,7 @@ __device__ __forceinline__ void ord_block(typename K::IS (&st)[K::IPT], const fl
     } else {
 #pragma unroll 1
         for (int r0 = 0; r0 < ORD_BLOCK_PAIRS; r0 += ORD_ACC_FOLD_PAIRS) {
-#pragma unroll
+#pragma unroll ORD_UNROLL
             for (int r = 0; r < ORD_ACC_FOLD_PAIRS; ++r) K::template step<FORM, UE>(st, R + (r0 + r) * K::NQ, E);
 #pragma unroll
             for (int q = 0; q < K::IPT; ++q) K::fold_acc(st[q]);
