@@ -729,9 +729,30 @@ __device__ __forceinline__ long long unit_owner(long long u, long long U, long l
 // told by an atomic ticket (no waiting), sums every contributor's partials in
 // CTA order -- a deterministic result.  store(q, p) writes the final values of
 // the thread's q-th i-particle.
-template <class K, class Store>
+// CTA k owns units [k U / G, (k + 1) U / G).
+struct EvenBounds {
+    long long U, G;
+    __device__ long long start(long long k) const { return unit_start(k, U, G); }
+    __device__ long long owner(long long u) const { return unit_owner(u, U, G); }
+};
+// CTA k owns units [s[k], s[k + 1]); s strictly increasing, s[0] = 0, s[G] = U.
+struct TableBounds {
+    const long long *s;
+    long long G;
+    __device__ long long start(long long k) const { return s[k]; }
+    __device__ long long owner(long long u) const {   // largest k with s[k] <= u
+        long long lo = 0, hi = G;
+        while (hi - lo > 1) {
+            const long long mid = (lo + hi) >> 1;
+            if (s[mid] <= u) lo = mid; else hi = mid;
+        }
+        return lo;
+    }
+};
+
+template <class K, class B, class Store>
 __device__ __forceinline__ void finish_itile(typename K::IS (&st)[K::IPT], long long t, long long nju, long long u0,
-                                             long long u1, long long U, long long G, long long k, double *part,
+                                             long long u1, const B &bounds, long long k, double *part,
                                              int *ticket, int *s_last, Store store) {
     constexpr int IPT = K::IPT;
     const int tid = threadIdx.x;
@@ -755,7 +776,7 @@ __device__ __forceinline__ void finish_itile(typename K::IS (&st)[K::IPT], long 
     }
     __threadfence();
     __syncthreads();
-    const long long klo = unit_owner(ta, U, G), khi = unit_owner(tb - 1, U, G);
+    const long long klo = bounds.owner(ta), khi = bounds.owner(tb - 1);
     if (tid == 0) {
         const int prev = atomicAdd(&ticket[t], 1);
         *s_last = (prev == (int)(khi - klo));
@@ -766,7 +787,7 @@ __device__ __forceinline__ void finish_itile(typename K::IS (&st)[K::IPT], long 
     // are in flight per step.
     __threadfence();
     auto slot_ptr = [&](long long kk) {
-        const int sl = (t == unit_start(kk, U, G) / nju) ? 0 : 1;
+        const int sl = (t == bounds.start(kk) / nju) ? 0 : 1;
         return part + ((kk * 2 + sl) * IPT * K::NP) * DS_THREADS + tid;
     };
     double acc[IPT][K::NP];
@@ -904,7 +925,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
         if (tn == t) continue;
 
         // ---- i-tile t is done for this CTA: store or hand over partials ----
-        finish_itile<K>(st, t, nju, u0, u1, U, G, k, a.part, a.ticket, &s_last,
+        finish_itile<K>(st, t, nju, u0, u1, EvenBounds{U, G}, k, a.part, a.ticket, &s_last,
                         [&](int q, const double *p) {
                             const size_t i = (size_t)t * BI + q * DS_THREADS + tid;
                             if (i < a.p.ni) K::store(p, a.p, i);
@@ -1001,6 +1022,7 @@ template <int IPT_>
 struct AccJerkOrd {
     static constexpr bool ORDERED = true;
     static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 7, PX = 6;
+    static constexpr int W_FAR = 4, W_NEAR = 5, W_HEAVY = 9;   // relative cost of a 64-j block
     static constexpr bool UE2 = true;
     struct IS { float2 dh[3], dl[3]; float2 u, v, w, e; float2 a[3], j[3]; Comp ca[3], cj[3]; float px; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {
@@ -1096,6 +1118,7 @@ template <int IPT_>
 struct AccOrd {
     static constexpr bool ORDERED = true;
     static constexpr int IPT = IPT_, JF = 8, NQ = 4, NP = 4, PX = 3;
+    static constexpr int W_FAR = 2, W_NEAR = 3, W_HEAVY = 6;   // relative cost of a 64-j block
     static constexpr bool UE2 = true;
     struct IS { float2 dh[3], dl[3]; float2 e; float2 a[3]; Comp ca[3]; float px; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {
@@ -1274,11 +1297,78 @@ __global__ void ds32_ord_ibox(PSet I, size_t ni, const int *pi, float4 *ibox) {
 
 struct DsOrdArgs {
     DsArgs d;
-    const int *pi;          // sorted i position -> i index
-    const OrdInfo *blk;     // per 64-j block
-    const float4 *ibox;     // per i-tile: min, max
+    const int *pi;                // sorted i position -> i index
+    const OrdInfo *blk;           // per 64-j block
+    const unsigned char *form;    // [i-tile][64-j block]: ORD_FAR, ORD_NEAR or ORD_HEAVY
+    const long long *start;       // CTA k owns units [start[k], start[k + 1])
     int *flag_count, *flag_list;
 };
+
+// Form of 64-j block `b` for an i-tile with float bounding box [ilo, ihi]:
+// heavy if it holds heavy j, far if the boxes are at least the block's
+// half-extent apart (and clearly separated relative to the coordinates'
+// magnitude), else near.
+__device__ __forceinline__ int block_form(float4 ilo, float4 ihi, const OrdInfo &b) {
+    if (b.lo.w != 0.f) return ORD_HEAVY;
+    const float gx = fmaxf(0.f, fmaxf(ilo.x - b.hi.x, b.lo.x - ihi.x));
+    const float gy = fmaxf(0.f, fmaxf(ilo.y - b.hi.y, b.lo.y - ihi.y));
+    const float gz = fmaxf(0.f, fmaxf(ilo.z - b.hi.z, b.lo.z - ihi.z));
+    const float d2 = gx * gx + gy * gy + gz * gz;
+    const float cm = fmaxf(fabsf(b.c.x), fmaxf(fabsf(b.c.y), fabsf(b.c.z)));
+    const float th = fmaxf(ORD_THETA * b.c.w, cm * 0x1p-16f);
+    return (d2 > 0.f && d2 >= th * th) ? ORD_FAR : ORD_NEAR;
+}
+
+// Plan: the form of every (i-tile, 64-j block) and the cost of every unit
+// (i-tile x one of the jsub parts of a j-tile), the sum of its blocks'
+// weights w_far, w_near, w_heavy.  One CTA per i-tile.
+__global__ void ds32_ord_plan(const float4 *ibox, const OrdInfo *blk, long long nblk, long long nju,
+                              int part_blocks, int w_far, int w_near, int w_heavy, unsigned char *form,
+                              int *ucost) {
+    const long long t = blockIdx.x;
+    const float4 ilo = ibox[2 * t], ihi = ibox[2 * t + 1];
+    unsigned char *row = form + t * nblk;
+    for (long long b = threadIdx.x; b < nblk; b += blockDim.x) row[b] = (unsigned char)block_form(ilo, ihi, blk[b]);
+    __syncthreads();
+    for (long long jp = threadIdx.x; jp < nju; jp += blockDim.x) {
+        int c = 0;
+        for (int q = 0; q < part_blocks; ++q) {
+            const int f = row[jp * part_blocks + q];
+            c += f == ORD_FAR ? w_far : (f == ORD_NEAR ? w_near : w_heavy);
+        }
+        ucost[t * nju + jp] = c;
+    }
+}
+
+// CTA boundaries at equal cost: ucum = inclusive prefix sums of the unit
+// costs; CTA k starts at the unit holding cost position k * total / G, moved
+// up where needed so that every CTA owns at least one unit.  One CTA.
+constexpr int ORD_MAX_GRID = 2048;
+__global__ void ds32_ord_bounds(const int *ucum, long long U, long long G, long long *start) {
+    __shared__ long long s[ORD_MAX_GRID + 1];
+    const long long total = ucum[U - 1];
+    for (long long k = threadIdx.x; k < G; k += blockDim.x) {
+        const long long target = total * k / G;   // first unit with ucum > target
+        long long lo = 0, hi = U;
+        while (lo < hi) {
+            const long long mid = (lo + hi) >> 1;
+            if ((long long)ucum[mid] > target) hi = mid; else lo = mid + 1;
+        }
+        s[k] = k == 0 ? 0 : lo;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        start[0] = 0;
+        long long prev = 0;
+        for (long long k = 1; k < G; ++k) {
+            long long v = s[k] > prev + 1 ? s[k] : prev + 1;
+            if (v > U - (G - k)) v = U - (G - k);
+            start[k] = v;
+            prev = v;
+        }
+        start[G] = U;
+    }
+}
 
 // One 64-j block of FORM against the thread's i-particles: acceleration
 // folds every ORD_ACC_FOLD_PAIRS records, jerk fold at the end (heavy
@@ -1319,11 +1409,12 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs o
     constexpr int PART_Q = PART_PAIRS * K::NQ;
     constexpr int PART_BLOCKS = PART_PAIRS / ORD_BLOCK_PAIRS;
     const long long nju = a.njt * JSUB;
-    const long long U = a.nit * nju;
     const long long G = gridDim.x;
     const long long k = blockIdx.x;
-    const long long u0 = unit_start(k, U, G), u1 = unit_start(k + 1, U, G);
+    const long long u0 = oa.start[k], u1 = oa.start[k + 1];
     if (u0 >= u1) return;
+    const TableBounds bounds{oa.start, G};
+    const long long nblk = a.njt * ORD_BLOCKS_PER_TILE;
     const int tid = threadIdx.x;
 
     if (tid == 0) {
@@ -1344,7 +1435,6 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs o
     const size_t ni = a.p.ni;
     long long t = u0 / nju;
     typename K::IS st[IPT];
-    float4 ilo, ihi;
     auto load_tile = [&](long long tt) {
 #pragma unroll
         for (int q = 0; q < IPT; ++q) {
@@ -1358,8 +1448,6 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs o
                 s_xi[3 + c][q * DS_THREADS + tid] = l;
             }
         }
-        ilo = __ldg(oa.ibox + 2 * tt);
-        ihi = __ldg(oa.ibox + 2 * tt + 1);
     };
     load_tile(t);
     __shared__ unsigned s_ie2;
@@ -1394,18 +1482,9 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs o
 #pragma unroll 1
         for (int bl = 0; bl < PART_BLOCKS; ++bl) {
             const long long gb = jt * ORD_BLOCKS_PER_TILE + (jp % JSUB) * PART_BLOCKS + bl;
-            const float4 bc = __ldg(&oa.blk[gb].c), blo = __ldg(&oa.blk[gb].lo), bhi = __ldg(&oa.blk[gb].hi);
-            const bool heavy = blo.w != 0.f;
-            bool far = false;
-            if (!heavy) {
-                const float gx = fmaxf(0.f, fmaxf(ilo.x - bhi.x, blo.x - ihi.x));
-                const float gy = fmaxf(0.f, fmaxf(ilo.y - bhi.y, blo.y - ihi.y));
-                const float gz = fmaxf(0.f, fmaxf(ilo.z - bhi.z, blo.z - ihi.z));
-                const float d2 = gx * gx + gy * gy + gz * gz;
-                const float cm = fmaxf(fabsf(bc.x), fmaxf(fabsf(bc.y), fabsf(bc.z)));
-                const float th = fmaxf(ORD_THETA * bc.w, cm * 0x1p-16f);
-                far = d2 > 0.f && d2 >= th * th;
-            }
+            const float4 bc = __ldg(&oa.blk[gb].c);
+            const int form = __ldg(oa.form + t * nblk + gb);
+            const bool far = form == ORD_FAR, heavy = form == ORD_HEAVY;
             const float cc[3] = {bc.x, bc.y, bc.z};
             const float4 *Rb = R + bl * ORD_BLOCK_PAIRS * K::NQ;
             if (far) {
@@ -1439,7 +1518,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs o
         }
         const long long tn = (u + 1 < u1) ? (u + 1) / nju : -1;
         if (tn == t) continue;
-        finish_itile<K>(st, t, nju, u0, u1, U, G, k, a.part, a.ticket, &s_last,
+        finish_itile<K>(st, t, nju, u0, u1, bounds, k, a.part, a.ticket, &s_last,
                         [&](int q, const double *p) {
                             const size_t ii = (size_t)t * BI + q * DS_THREADS + tid;
                             if (ii >= ni) return;
@@ -1970,10 +2049,11 @@ static cudaError_t run_ds_capped(const PairArgs &p, void *ws, size_t ws_bytes, i
 // ---------------------------------------------------------------------------
 struct OrdLayout {
     Geometry g;
-    size_t blk_bytes, ibox_bytes, flag_bytes, jd_bytes, ref_bytes, order_bytes;
+    size_t blk_bytes, ibox_bytes, flag_bytes, jd_bytes, ref_bytes, form_bytes, cost_bytes, scan_bytes, start_bytes,
+        order_bytes;
     size_t total() const {
         return g.rec_bytes + g.part_bytes + g.ticket_bytes + g.tile_bytes + blk_bytes + ibox_bytes + flag_bytes +
-               jd_bytes + ref_bytes + order_bytes;
+               jd_bytes + ref_bytes + form_bytes + 2 * cost_bytes + scan_bytes + start_bytes + order_bytes;
     }
 };
 
@@ -1986,6 +2066,10 @@ static OrdLayout ord_layout(size_t ni, size_t nj, int sms, bool same) {
     L.flag_bytes = align_up((ni + 64) * sizeof(int), 256);
     L.jd_bytes = align_up(nj * 3 * sizeof(float4), 256);
     L.ref_bytes = align_up((size_t)REFINE_MAX_SPLIT * (REFINE_MAX_CHUNKS * 3 * sizeof(double) + sizeof(int)), 256);
+    L.form_bytes = align_up((size_t)L.g.nit * L.g.njt * ORD_BLOCKS_PER_TILE, 256);
+    L.cost_bytes = align_up((size_t)L.g.units * sizeof(int), 256);
+    L.scan_bytes = align_up(inclusive_sum_bytes((size_t)L.g.units), 256);
+    L.start_bytes = align_up(((size_t)L.g.grid + 1) * sizeof(long long), 256);
     L.order_bytes = order_workspace_bytes(ni, nj, same);
     return L;
 }
@@ -2007,7 +2091,7 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
     const bool same = same_sets(p, nfields);
     const OrdLayout L = ord_layout<K>(p.ni, p.nj, sms, same);
     const Geometry &g = L.g;
-    if (L.total() > ws_bytes) return cudaErrorInvalidValue;
+    if (L.total() > ws_bytes || g.grid > ORD_MAX_GRID) return cudaErrorInvalidValue;
     char *q = static_cast<char *>(ws);
     float *rec = reinterpret_cast<float *>(q); q += g.rec_bytes;
     double *part = reinterpret_cast<double *>(q); q += g.part_bytes;
@@ -2020,6 +2104,11 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
     double *ref_part = reinterpret_cast<double *>(q);
     int *ref_ticket = reinterpret_cast<int *>(ref_part + (size_t)REFINE_MAX_SPLIT * REFINE_MAX_CHUNKS * 3);
     q += L.ref_bytes;
+    unsigned char *form = reinterpret_cast<unsigned char *>(q); q += L.form_bytes;
+    int *ucost = reinterpret_cast<int *>(q); q += L.cost_bytes;
+    int *ucum = reinterpret_cast<int *>(q); q += L.cost_bytes;
+    void *scan_ws = q; q += L.scan_bytes;
+    long long *start = reinterpret_cast<long long *>(q); q += L.start_bytes;
     void *order_ws = q;
 
     OrderOut o;
@@ -2029,6 +2118,12 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
                                                           g.nit, flags, jd, ref_ticket, REFINE_MAX_SPLIT);
     constexpr int BI = DS_THREADS * K::IPT;
     ds32_ord_ibox<<<(unsigned)g.nit, BI, 0, s>>>(p.I, p.ni, o.pi, ibox);
+    const long long nblk = g.njt * ORD_BLOCKS_PER_TILE, nju = g.njt * g.jsub;
+    ds32_ord_plan<<<(unsigned)g.nit, 256, 0, s>>>(ibox, blk, nblk, nju, ORD_BLOCKS_PER_TILE / g.jsub, K::W_FAR,
+                                                  K::W_NEAR, K::W_HEAVY, form, ucost);
+    e = inclusive_sum(ucost, ucum, (size_t)g.units, scan_ws, L.scan_bytes, s);
+    if (e != cudaSuccess) return e;
+    ds32_ord_bounds<<<1, 1024, 0, s>>>(ucum, g.units, g.grid, start);
 
     DsOrdArgs a;
     a.d.p = p;
@@ -2042,7 +2137,8 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
     a.d.run_mode = 0;
     a.pi = o.pi;
     a.blk = blk;
-    a.ibox = ibox;
+    a.form = form;
+    a.start = start;
     a.flag_count = flags;
     a.flag_list = flags + 64;
     const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);

@@ -102,6 +102,9 @@ struct OrderOut {
 size_t order_workspace_bytes(size_t ni, size_t nj, bool same);
 cudaError_t build_order(const PSet &I, size_t ni, const PSet &J, size_t nj, bool same, void *ws,
                         size_t ws_bytes, OrderOut &out, cudaStream_t s);
+// Inclusive prefix sum of n ints (cub::DeviceScan) in tmp_bytes of scratch.
+size_t inclusive_sum_bytes(size_t n);
+cudaError_t inclusive_sum(const int *in, int *out, size_t n, void *tmp, size_t tmp_bytes, cudaStream_t s);
 
 // Record `msg` as this thread's tg_last_error() text.
 void set_last_error(const char *msg);

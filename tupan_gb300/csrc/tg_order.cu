@@ -15,6 +15,7 @@
 #include <algorithm>
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
 #include "tg_internal.h"
 
@@ -145,6 +146,16 @@ size_t order_workspace_bytes(size_t ni, size_t nj, bool same) {
     if (!same) b += 4 * align256(ni * sizeof(unsigned)); // i keys in/out, values in/out
     b += align256(cub_bytes(n));
     return b;
+}
+
+size_t inclusive_sum_bytes(size_t n) {
+    size_t tmp = 0;
+    cub::DeviceScan::InclusiveSum(nullptr, tmp, (const int *)nullptr, (int *)nullptr, (int)n);
+    return tmp;
+}
+
+cudaError_t inclusive_sum(const int *in, int *out, size_t n, void *tmp, size_t tmp_bytes, cudaStream_t s) {
+    return cub::DeviceScan::InclusiveSum(tmp, tmp_bytes, in, out, (int)n, s);
 }
 
 cudaError_t build_order(const PSet &I, size_t ni, const PSet &J, size_t nj, bool same, void *ws,
