@@ -57,7 +57,8 @@ const char *tg_version(void);
 /* Text of the last error seen by this thread's calls ("" if none). */
 const char *tg_last_error(void);
 /* Synchronise `stream` and return (then clear) the status bits raised by
- * kernels on the current device since the last call; negative on error. */
+ * kernels on the current device since the last call, those of
+ * tg_acc_jerk_noalloc included; negative on error. */
 int tg_sync_status(void *stream);
 /* Precision used by the drop-in host entry points (process-wide). */
 int tg_set_host_precision(int prec);
@@ -281,16 +282,18 @@ int tg_hermite_correct(int order, size_t n, double tau, const double *const *rv0
                        const double *const *deriv0, const double *const *deriv1, double *const *rv1,
                        void *stream);
 
-/* No counterpart in the reference.  Split-FP32 AccJerk (same arithmetic as
- * tg_acc_jerk with TG_PREC_DS32) for callers that cannot let a library
- * allocate GPU memory -- applications whose own pool owns the GPU's memory,
- * or loops that must not stall other streams on cudaMalloc/cudaFree.  It
- * calls no allocator: its scratch is a fixed 24 MiB __device__ array that
- * every GPU loading the library holds until exit.  Limits: ni <= 2^20,
- * nj <= 2^17 (else TG_EINVAL).  The first call on a device looks up the
- * array's address with that device current; make it before any stream
- * capture.  Calls share the array, so calls that overlap on the GPU race:
- * order them on one stream.  Device pointers, asynchronous on `stream`. */
+/* No counterpart in the reference.  Split-FP32 AccJerk (the unordered
+ * stream-K kernels that tg_acc_jerk with TG_PREC_DS32 runs for calls below
+ * 2^24 pairs) for callers that cannot let a library allocate GPU memory --
+ * applications whose own pool owns the GPU's memory, or loops that must not
+ * stall other streams on cudaMalloc/cudaFree.  It calls no allocator: its
+ * scratch is a fixed 24 MiB __device__ array that every GPU loading the
+ * library holds until exit.  Limits: ni <= 2^20, nj <= 2^17 (else
+ * TG_EINVAL).  The first call on a device looks up the array's address with
+ * that device current; make it before any stream capture.  Calls share the
+ * array, so calls that overlap on the GPU race: order them on one stream.
+ * A device-side wait that gave up is reported by tg_sync_status.  Device
+ * pointers, asynchronous on `stream`. */
 int tg_acc_jerk_noalloc(size_t ni, const double *im, const double *irx, const double *iry,
                         const double *irz, const double *ie2,
                         const double *ivx, const double *ivy, const double *ivz,

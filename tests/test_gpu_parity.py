@@ -10,16 +10,16 @@ Tolerances:
     log differ from glibc by an ulp; the Laguerre iteration then stops on a
     slightly different iterate within its 2^-42 tolerance).
   * split FP32 (ds32): per particle |out_gpu - out_ref| / |out_ref| (vector
-    norm over the components of one output quantity).  On the golden
-    fixtures (the reference test's shapes and prefix sweeps, a Plummer set
-    and a binary-rich set) the bound is DS32_TOL_FIXTURE: 1e-6 for Phi, Acc,
-    AccJerk (acceleration and jerk) and Tstep, the accuracy asked of the
-    split form; measured maxima 7.8e-7 (jerk), 7.1e-7 (Acc).  The larger
-    synthetic Plummer sets (ragged shapes up to 5000 x 4097) use DS32_TOL:
-    there a few particles whose net force is much smaller than the sum of
-    its terms reach 1.1e-6 (Acc) and 2.1e-6 (jerk), the FP32 rounding floor
-    of such sums.  The kernels are deterministic, so these maxima do not
-    vary between runs.
+    norm over the components of one output quantity), bounds per output
+    group in DS32_TOL_FIXTURE (golden fixtures: the reference test's shapes
+    and prefix sweeps, a Plummer set and a binary-rich set) and DS32_TOL
+    (synthetic Plummer sets, ragged shapes).  The acceleration of Acc and
+    AccJerk is held to 1e-6 everywhere, the accuracy asked of the split
+    form.  The jerk is held to 1e-5: FP32 terms cannot give 1e-6 for a
+    particle whose jerk is hundreds of times smaller than the sum of its
+    terms' magnitudes (measured max 7.0e-6 on the N = 65536
+    Plummer-Salpeter workload, 4.6e-6 on 5000 x 4097).  The kernels are
+    deterministic, so these maxima do not vary between runs.
 """
 import numpy as np
 import pytest
@@ -30,9 +30,10 @@ pytestmark = pytest.mark.gpu
 
 from golden_io import CASES, FIELDS, PREFIXES, load, typed_scalars  # noqa: E402
 
-DS32_TOL_FIXTURE = {"phi": 1e-6, "acc": 1e-6, "acc_jerk": 1e-6, "snap_crackle": 1e-5,
+# per output group (GROUPS): AccJerk is (acceleration, jerk)
+DS32_TOL_FIXTURE = {"phi": 1e-6, "acc": 1e-6, "acc_jerk": (1e-6, 1e-6), "snap_crackle": 1e-5,
                     "tstep": 1e-6, "pnacc": 1e-5}
-DS32_TOL = {"phi": 2e-6, "acc": 4e-6, "acc_jerk": 4e-6, "snap_crackle": 5e-5,
+DS32_TOL = {"phi": 2e-6, "acc": 1e-6, "acc_jerk": (1e-6, 1e-5), "snap_crackle": 5e-5,
             "tstep": 2e-6, "pnacc": 2e-5}
 GROUPS = {"phi": [(0,)], "acc": [(0, 1, 2)], "acc_jerk": [(0, 1, 2), (3, 4, 5)],
           "snap_crackle": [(0, 1, 2), (3, 4, 5)], "tstep": [(0,), (1,)],
@@ -93,16 +94,28 @@ def assert_fp64(name, got, want):
         assert np.abs(got - want).max() <= tol * scale, name
 
 
-def rel_err(name, got, want):
-    worst = 0.0
+def group_errs(name, got, want):
+    """Max per-particle relative error of each output group of `name`."""
+    out = []
     for g in GROUPS[name]:
         d = np.sqrt(((got[list(g)] - want[list(g)]) ** 2).sum(0))
         n = np.sqrt((want[list(g)] ** 2).sum(0))
         ok = n > 0
-        if ok.any():
-            worst = max(worst, float((d[ok] / n[ok]).max()))
+        out.append(float((d[ok] / n[ok]).max()) if ok.any() else 0.0)
         assert np.all(d[~ok] <= 1e-300), name
-    return worst
+    return out
+
+
+def rel_err(name, got, want):
+    return max(group_errs(name, got, want))
+
+
+def within(name, got, want, tol):
+    """True when every output group is within its bound (tol: one bound
+    for all groups or one per group); also returns the errors."""
+    errs = group_errs(name, got, want)
+    tols = tol if isinstance(tol, tuple) else (tol,) * len(errs)
+    return all(e <= t for e, t in zip(errs, tols)), errs
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -138,8 +151,8 @@ def test_ds32_against_golden(ext, case):
         sc = typed_scalars(name, sc)
         P = PS(ps)
         got = run_kernel(ext, name, "ds32", P, P, sc)
-        err = rel_err(name, got, z["out_" + key])
-        assert err <= DS32_TOL_FIXTURE[name], "%s %s ds32 error %.3e" % (case, name, err)
+        ok, err = within(name, got, z["out_" + key], DS32_TOL_FIXTURE[name])
+        assert ok, "%s %s ds32 error %r" % (case, name, err)
 
 
 def test_ds32_prefix_sweeps(ext):
@@ -150,11 +163,13 @@ def test_ds32_prefix_sweeps(ext):
         sc = typed_scalars(name, sc)
         for p in PREFIXES:
             P, S = PS(ps), PS({f: ps[f][:p] for f in FIELDS})
-            err = rel_err(name, run_kernel(ext, name, "ds32", P, S, sc), z["outJ%d_" % p + key])
-            assert err <= DS32_TOL_FIXTURE[name], (name, p, err)
+            ok, err = within(name, run_kernel(ext, name, "ds32", P, S, sc), z["outJ%d_" % p + key],
+                             DS32_TOL_FIXTURE[name])
+            assert ok, (name, p, err)
             P, S = PS(ps), PS({f: ps[f][:p] for f in FIELDS})
-            err = rel_err(name, run_kernel(ext, name, "ds32", S, P, sc), z["outI%d_" % p + key])
-            assert err <= DS32_TOL_FIXTURE[name], (name, p, err)
+            ok, err = within(name, run_kernel(ext, name, "ds32", S, P, sc), z["outI%d_" % p + key],
+                             DS32_TOL_FIXTURE[name])
+            assert ok, (name, p, err)
 
 
 def plummer(n, seed, e2=1e-4):
@@ -192,7 +207,8 @@ def test_streamk_shapes_ds32_vs_oracle(ext, orc, ni, nj):
                      ("snap_crackle", ())]:
         want = np.stack(orc.calc(name, I, J, *sc, nthreads=4))
         got = run_kernel(ext, name, "ds32", PS(I), PS(J), sc)
-        assert rel_err(name, got, want) <= DS32_TOL[name], (name, ni, nj)
+        ok, err = within(name, got, want, DS32_TOL[name])
+        assert ok, (name, ni, nj, err)
         got64 = run_kernel(ext, name, "float64", PS(I), PS(J), sc)
         assert np.array_equal(got64, want), (name, ni, nj)
 
@@ -231,12 +247,11 @@ def test_fp64_engines_bit_identical_to_oracle(ext, orc):
 
 
 @pytest.mark.parametrize("case", ["plain", "coincident", "zero_eps", "prefix"])
-def test_acc_jerk_unmasked_form_gate(ext, case):
-    """Large AccJerk calls run an unmasked form when a pre-pass finds every
-    pair softening above 1e-20 and no two distinct coincident particles;
-    otherwise the masked form.  Either way the results follow the
-    reference's r = 0 exclusion: a coincident pair with different
-    velocities would otherwise add a huge jerk."""
+def test_acc_jerk_r0_exclusion(ext, case):
+    """Large AccJerk calls (the ordered path) follow the reference's r = 0
+    exclusion whatever the inputs: two distinct coincident particles with
+    different velocities (an unexcluded pair would add a huge jerk), a zero
+    softening, and an i-set that is a prefix of the very same j arrays."""
     n = 40000
     d = plummer(n, seed=31)
     if case == "coincident":
@@ -255,9 +270,9 @@ def test_acc_jerk_unmasked_form_gate(ext, case):
         I.n = ni
     got = run_kernel(ext, "acc_jerk", "ds32", I, P, ())
     want = run_kernel(ext, "acc_jerk", "float64", I, P, ())
-    # the split-FP32 jerk error grows with N (max ~7e-6 at N = 16384..65536);
     # an unexcluded coincident pair would be off by orders of magnitude
-    assert rel_err("acc_jerk", got, want) <= 2e-5, case
+    ok, err = within("acc_jerk", got, want, DS32_TOL["acc_jerk"])
+    assert ok, (case, err)
 
 
 def test_ds32_is_deterministic(ext):
@@ -307,7 +322,8 @@ def test_host_dropin_entry_points(orc):
         if exact:
             assert np.array_equal(got, np.stack(want))
         else:
-            assert rel_err("acc_jerk", got, np.stack(want)) <= DS32_TOL["acc_jerk"]
+            ok, err = within("acc_jerk", got, np.stack(want), DS32_TOL["acc_jerk"])
+            assert ok, err
     _native.lib.tg_set_host_precision(_native.PREC_FP64)
 
 
@@ -350,3 +366,21 @@ def test_sakura_softened_close_pair_is_bounded(ext):
     with pytest.warns(RuntimeWarning):
         out = run_kernel(ext, "sakura", "float64", P, P, (1.0 / 64, 1))
     assert np.all(np.isfinite(out))
+
+
+def test_headline_workload_force_error(ext):
+    """The benchmark's workload: Plummer N = 65536, Salpeter masses on
+    [0.1, 100] (total mass 1), pair softening 1e-6, seed 20261203.  Split
+    FP32 Acc and AccJerk against the FP64 kernels (bit-identical to the
+    reference C backend): the acceleration within 1e-6 for every particle,
+    the jerk within 1e-5."""
+    from tupan_gb300.ics import Salpeter, plummer_arrays
+    d = plummer_arrays(65536, 1e-3, imf=Salpeter(0.1, 100.0), seed=20261203)
+    for f in ("ax", "ay", "az", "jx", "jy", "jz"):
+        d[f] = np.zeros(65536)
+    P = PS(d)
+    for name in ("acc", "acc_jerk"):
+        want = run_kernel(ext, name, "float64", P, P, ())
+        got = run_kernel(ext, name, "ds32", P, P, ())
+        ok, err = within(name, got, want, DS32_TOL[name])
+        assert ok, (name, err)

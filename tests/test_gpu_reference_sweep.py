@@ -16,7 +16,7 @@ torch = pytest.importorskip("torch")
 
 pytestmark = pytest.mark.gpu
 
-from test_gpu_parity import DS32_TOL, GROUPS, KCLASS, PS, rel_err  # noqa: E402
+from test_gpu_parity import DS32_TOL, GROUPS, KCLASS, PS, rel_err, within  # noqa: E402
 
 N = 256
 PN = (7, 128.0)
@@ -83,4 +83,5 @@ def test_reference_prefix_sweep(env, name, sc):
             else:
                 assert np.array_equal(got, want), (name, p)
             if name != "sakura":
-                assert rel_err(name, gpu(ext, name, "ds32", I, J, sc), want) <= DS32_TOL[name], (name, p)
+                ok, err = within(name, gpu(ext, name, "ds32", I, J, sc), want, DS32_TOL[name])
+                assert ok, (name, p, err)

@@ -239,13 +239,15 @@ int tg_sync_status(void *stream) {
     int rc = current_ctx(&c);
     if (rc != TG_OK) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    unsigned h = 0;
+    unsigned h = 0, na = 0;
     cudaError_t e = cudaMemcpyAsync(&h, c->status, sizeof h, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e == cudaSuccess) e = cudaMemsetAsync(c->status, 0, sizeof(unsigned), s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    // and the bits tg_acc_jerk_noalloc keeps in its own scratch
+    if (e == cudaSuccess) e = tg::noalloc_take_status(s, &na);
     if (e != cudaSuccess) return fail(TG_ECUDA, "tg_sync_status", e);
-    return (int)h;
+    return (int)(h | na);
 }
 
 int tg_set_host_precision(int prec) {

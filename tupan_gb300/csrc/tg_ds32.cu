@@ -776,10 +776,16 @@ __device__ __forceinline__ void finish_itile(typename K::IS (&st)[K::IPT], long 
     }
     __threadfence();
     __syncthreads();
+    // contributors: the CTAs from the owner of the tile's first unit to the
+    // owner of its last that own at least one unit (a cost-weighted split
+    // may leave a CTA empty)
     const long long klo = bounds.owner(ta), khi = bounds.owner(tb - 1);
+    auto nonempty = [&](long long kk) { return bounds.start(kk) < bounds.start(kk + 1); };
+    int ncontrib = 0;
+    for (long long kk = klo; kk <= khi; ++kk) ncontrib += nonempty(kk) ? 1 : 0;
     if (tid == 0) {
         const int prev = atomicAdd(&ticket[t], 1);
-        *s_last = (prev == (int)(khi - klo));
+        *s_last = (prev == ncontrib - 1);
     }
     __syncthreads();
     if (!*s_last) return;
@@ -790,6 +796,10 @@ __device__ __forceinline__ void finish_itile(typename K::IS (&st)[K::IPT], long 
         const int sl = (t == bounds.start(kk) / nju) ? 0 : 1;
         return part + ((kk * 2 + sl) * IPT * K::NP) * DS_THREADS + tid;
     };
+    auto next = [&](long long kk) {   // first contributor after kk, or khi + 1
+        for (++kk; kk <= khi && !nonempty(kk); ++kk) {}
+        return kk;
+    };
     double acc[IPT][K::NP];
     {
         const double *s0 = slot_ptr(klo);
@@ -798,10 +808,11 @@ __device__ __forceinline__ void finish_itile(typename K::IS (&st)[K::IPT], long 
 #pragma unroll
             for (int w = 0; w < K::NP; ++w) acc[q][w] = __ldcg(s0 + (q * K::NP + w) * DS_THREADS);
     }
-    for (long long kk = klo + 1; kk <= khi; kk += 2) {
-        const bool two = kk + 1 <= khi;
+    for (long long kk = next(klo); kk <= khi;) {
+        const long long k2 = next(kk);
+        const bool two = k2 <= khi;
         const double *s0 = slot_ptr(kk);
-        const double *s1 = two ? slot_ptr(kk + 1) : s0;
+        const double *s1 = two ? slot_ptr(k2) : s0;
 #pragma unroll
         for (int q = 0; q < IPT; ++q) {
             double v0[K::NP], v1[K::NP];
@@ -813,6 +824,7 @@ __device__ __forceinline__ void finish_itile(typename K::IS (&st)[K::IPT], long 
             K::combine(acc[q], v0);
             if (two) K::combine(acc[q], v1);
         }
+        kk = two ? next(k2) : k2;
     }
 #pragma unroll
     for (int q = 0; q < IPT; ++q) store(q, acc[q]);
@@ -973,8 +985,8 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
 // The acceleration's FP32 lane sums are folded into Kahan sums every
 // 2 ORD_ACC_FOLD_PAIRS j, the jerk's every 64 j.  A per-i proxy of the sum
 // of term magnitudes (the sum of |folded lane sums|) travels with the
-// partials; particles whose proxy exceeds ORD_TAU |a| (strong cancellation)
-// are listed and their acceleration is recomputed in double-single
+// partials; particles whose proxy exceeds tau |a| (strong cancellation,
+// ord_tau) are listed and their acceleration is recomputed in double-single
 // arithmetic (ds32_refine_acc).
 // ===========================================================================
 constexpr int ORD_BLOCK = 64;                              // j per block
@@ -988,11 +1000,13 @@ constexpr int ORD_ACC_FOLD_PAIRS = TG_ORD_ACC_FOLD_PAIRS;  // records per accele
 #define TG_ORD_UNROLL 8    // records per unrolled body of the far and near forms
 #endif
 #ifndef TG_ORD_FAR_RCP
-#define TG_ORD_FAR_RCP 1   // far blocks take 1/s from MUFU.RCP (else y * y on the FMA pipe)
+#define TG_ORD_FAR_RCP 0   // far blocks take 1/s from MUFU.RCP (else y * y on the FMA pipe)
 #endif
 constexpr int ORD_UNROLL = TG_ORD_UNROLL;
-constexpr float ORD_THETA = 1.0f;
-constexpr float ORD_TAU = 20.0f;
+#ifndef TG_ORD_THETA
+#define TG_ORD_THETA 0.5f  // far: box distance >= TG_ORD_THETA x the block's half-extent
+#endif
+constexpr float ORD_THETA = TG_ORD_THETA;
 
 struct OrdInfo {
     float4 c;    // block centre (x, y, z), half-extent
@@ -1302,7 +1316,15 @@ struct DsOrdArgs {
     const unsigned char *form;    // [i-tile][64-j block]: ORD_FAR, ORD_NEAR or ORD_HEAVY
     const long long *start;       // CTA k owns units [start[k], start[k + 1])
     int *flag_count, *flag_list;
+    float tau;                    // recompute when proxy > tau |a|
 };
+
+// Recompute threshold: 20 at nj >= 65536, scaled with sqrt(nj) below (fewer
+// terms average out less of their rounding), at least 4.
+static float ord_tau(size_t nj) {
+    const double t = 20.0 * sqrt((double)nj / 65536.0);
+    return (float)(t > 20.0 ? 20.0 : (t < 4.0 ? 4.0 : t));
+}
 
 // Form of 64-j block `b` for an i-tile with float bounding box [ilo, ihi]:
 // heavy if it holds heavy j, far if the boxes are at least the block's
@@ -1340,34 +1362,20 @@ __global__ void ds32_ord_plan(const float4 *ibox, const OrdInfo *blk, long long 
     }
 }
 
-// CTA boundaries at equal cost: ucum = inclusive prefix sums of the unit
-// costs; CTA k starts at the unit holding cost position k * total / G, moved
-// up where needed so that every CTA owns at least one unit.  One CTA.
-constexpr int ORD_MAX_GRID = 2048;
-__global__ void ds32_ord_bounds(const int *ucum, long long U, long long G, long long *start) {
-    __shared__ long long s[ORD_MAX_GRID + 1];
+// CTA boundaries at equal cost, one thread per unit: with ucum the inclusive
+// prefix sums of the unit costs (total C), CTA k starts at the unit that
+// holds cost position floor(k C / G).  A unit costing more than C / G holds
+// several positions, and the CTAs between get no unit.
+__global__ void ds32_ord_bounds(const int *ucost, const int *ucum, long long U, long long G, long long *start) {
+    const long long u = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (u == 0) start[G] = U;
+    if (u >= U) return;
     const long long total = ucum[U - 1];
-    for (long long k = threadIdx.x; k < G; k += blockDim.x) {
-        const long long target = total * k / G;   // first unit with ucum > target
-        long long lo = 0, hi = U;
-        while (lo < hi) {
-            const long long mid = (lo + hi) >> 1;
-            if ((long long)ucum[mid] > target) hi = mid; else lo = mid + 1;
-        }
-        s[k] = k == 0 ? 0 : lo;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        start[0] = 0;
-        long long prev = 0;
-        for (long long k = 1; k < G; ++k) {
-            long long v = s[k] > prev + 1 ? s[k] : prev + 1;
-            if (v > U - (G - k)) v = U - (G - k);
-            start[k] = v;
-            prev = v;
-        }
-        start[G] = U;
-    }
+    const long long ce = ucum[u], cs = ce - ucost[u];
+    const long long klo = (cs * G + total - 1) / total;
+    long long khi = (ce * G + total - 1) / total - 1;
+    if (khi > G - 1) khi = G - 1;
+    for (long long k = klo; k <= khi; ++k) start[k] = u;
 }
 
 // One 64-j block of FORM against the thread's i-particles: acceleration
@@ -1525,7 +1533,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs o
                             const size_t i = (size_t)oa.pi[ii];
                             K::store(p, a.p, i);
                             const double am = sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
-                            if (!(p[K::PX] <= (double)ORD_TAU * am)) {
+                            if (!(p[K::PX] <= (double)oa.tau * am)) {
                                 const int f = atomicAdd(oa.flag_count, 1);
                                 oa.flag_list[f] = (int)i;
                             }
@@ -2091,7 +2099,7 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
     const bool same = same_sets(p, nfields);
     const OrdLayout L = ord_layout<K>(p.ni, p.nj, sms, same);
     const Geometry &g = L.g;
-    if (L.total() > ws_bytes || g.grid > ORD_MAX_GRID) return cudaErrorInvalidValue;
+    if (L.total() > ws_bytes) return cudaErrorInvalidValue;
     char *q = static_cast<char *>(ws);
     float *rec = reinterpret_cast<float *>(q); q += g.rec_bytes;
     double *part = reinterpret_cast<double *>(q); q += g.part_bytes;
@@ -2123,7 +2131,7 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
                                                   K::W_NEAR, K::W_HEAVY, form, ucost);
     e = inclusive_sum(ucost, ucum, (size_t)g.units, scan_ws, L.scan_bytes, s);
     if (e != cudaSuccess) return e;
-    ds32_ord_bounds<<<1, 1024, 0, s>>>(ucum, g.units, g.grid, start);
+    ds32_ord_bounds<<<(unsigned)((g.units + 255) / 256), 256, 0, s>>>(ucost, ucum, g.units, g.grid, start);
 
     DsOrdArgs a;
     a.d.p = p;
@@ -2141,6 +2149,7 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
     a.start = start;
     a.flag_count = flags;
     a.flag_list = flags + 64;
+    a.tau = ord_tau(p.nj);
     const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
     if (g.jsub == 2) ds32_ord<K, 2><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
     else ds32_ord<K, 1><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);

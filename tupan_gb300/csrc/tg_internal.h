@@ -114,5 +114,8 @@ void set_last_error(const char *msg);
 size_t ds32_workspace_bytes_capped(int kernel, size_t ni, size_t nj, int sms, long long max_grid);
 cudaError_t launch_ds32_capped(int kernel, const PairArgs &a, void *ws, size_t ws_bytes, int sms,
                                long long max_grid, cudaStream_t s);
+// Status bits tg_acc_jerk_noalloc left on the current device (read and
+// cleared; no allocation).
+cudaError_t noalloc_take_status(cudaStream_t s, unsigned *bits);
 
 }  // namespace tg

@@ -21,9 +21,13 @@
 // shares the one array and leaves its contents behind (the tickets are
 // cleared at the start of each call), so calls whose kernels overlap on the
 // GPU -- e.g. issued on two streams without ordering -- race and corrupt
-// each other's results.  Order them on one stream.  Device-side bounded-wait
-// timeouts are recorded only inside the array; this entry point reports
-// argument and launch errors.
+// each other's results.  Order them on one stream.
+//
+// Errors: arguments and launches are checked when the call is made (return
+// code, tg_last_error).  A device-side bounded wait that gives up sets
+// TG_ST_MBAR_TIMEOUT in a status word at the head of the array; the word is
+// sticky and tg_sync_status(stream) reports it together with the other
+// entry points' status bits, then clears it -- without allocating.
 #include <cstring>
 #include <mutex>
 
@@ -57,6 +61,28 @@ int na_fail(int code, const char *msg) {
 
 }  // namespace
 
+namespace tg {
+// Status bits that tg_acc_jerk_noalloc's kernels left in the scratch header
+// of the current device (0 if the entry point never ran there); clears them.
+// Ordered on `s`, then synchronised with it.
+cudaError_t noalloc_take_status(cudaStream_t s, unsigned *bits) {
+    *bits = 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEV) return e;
+    NoAllocDev &d = g_na[dev];
+    std::lock_guard<std::mutex> lk(d.mu);
+    if (!d.ready) return cudaSuccess;
+    unsigned h = 0;
+    e = cudaMemcpyAsync(&h, d.base, sizeof h, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.base, 0, sizeof h, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) *bits = h;
+    return e;
+}
+}  // namespace tg
+
 extern "C" int tg_acc_jerk_noalloc(size_t ni, const double *im, const double *irx, const double *iry,
                                    const double *irz, const double *ie2, const double *ivx,
                                    const double *ivy, const double *ivz, size_t nj, const double *jm,
@@ -64,6 +90,7 @@ extern "C" int tg_acc_jerk_noalloc(size_t ni, const double *im, const double *ir
                                    const double *je2, const double *jvx, const double *jvy,
                                    const double *jvz, double *iax, double *iay, double *iaz,
                                    double *ijx, double *ijy, double *ijz, void *stream) {
+    tg::set_last_error("");
     if (ni > NOALLOC_MAX_NI || nj > NOALLOC_MAX_NJ)
         return na_fail(TG_EINVAL, "tg_acc_jerk_noalloc: ni must be <= 1048576 and nj <= 131072 "
                                   "(fixed 24 MiB scratch)");
@@ -98,6 +125,10 @@ extern "C" int tg_acc_jerk_noalloc(size_t ni, const double *im, const double *ir
             e = cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
             if (e != cudaSuccess) return na_fail(TG_ECUDA, "tg_acc_jerk_noalloc: SM count query failed");
             d.base = static_cast<unsigned char *>(ptr);
+            // the status word starts at zero and then stays sticky until
+            // tg_sync_status reads it
+            if (cudaMemsetAsync(d.base, 0, NOALLOC_HEADER, static_cast<cudaStream_t>(stream)) != cudaSuccess)
+                return na_fail(TG_ECUDA, "tg_acc_jerk_noalloc: cudaMemsetAsync failed");
             d.ready = true;
         }
     }
@@ -114,8 +145,6 @@ extern "C" int tg_acc_jerk_noalloc(size_t ni, const double *im, const double *ir
     for (int k = 0; k < 6; ++k) a.out[k] = op[k];
     a.status = reinterpret_cast<unsigned *>(d.base);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (cudaMemsetAsync(d.base, 0, NOALLOC_HEADER, s) != cudaSuccess)
-        return na_fail(TG_ECUDA, "tg_acc_jerk_noalloc: cudaMemsetAsync failed");
     cudaError_t e = tg::launch_ds32_capped(tg::K_ACC_JERK, a, d.base + NOALLOC_HEADER,
                                            NOALLOC_BYTES - NOALLOC_HEADER, d.sms, NOALLOC_MAX_GRID, s);
     if (e != cudaSuccess) return na_fail(TG_ECUDA, "tg_acc_jerk_noalloc: kernel launch failed");
