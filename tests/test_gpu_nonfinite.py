@@ -2,9 +2,9 @@
 and an infinite velocity in another.  Every kernel returns and raises no
 status bit.  FP64 reproduces the CPU oracle (the reference algorithm)
 exactly: the same non-finite outputs and the same bits elsewhere.  Split
-FP32 excludes a pair only at r = 0 exactly, where the reference's `r2 > 0`
-test also excludes a pair whose distance is NaN, so there NaN reaches more
-outputs: it is non-finite at least wherever the reference is."""
+FP32 (for these small sets the double-single kernel of Acc and AccJerk, the
+unordered split-FP32 kernels of Phi and Tstep) is non-finite at least
+wherever the reference is."""
 import numpy as np
 import pytest
 

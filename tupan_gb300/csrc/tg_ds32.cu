@@ -1573,8 +1573,9 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs o
 // nch = clamp(G / F, 1, EXACT_MAX_CHUNKS) chunks; a CTA reduces a chunk in
 // a fixed-order tree, and with nch > 1 the last chunk of a particle to
 // finish (atomic ticket) adds the chunk sums in chunk order: the result is
-// deterministic.  Pairs at r = 0 are excluded as in the reference
-// (acc_kernel_common.h, acc_jerk_kernel_common.h: r2 > 0).
+// deterministic.  Pairs with r2 > 0 false get 1/r = 0 as in the reference
+// (acc_kernel_common.h, acc_jerk_kernel_common.h; smoothing.h), so a NaN
+// separation still reaches the sums as it does there.
 constexpr int EXACT_THREADS = 256;
 constexpr int EXACT_MAX_CHUNKS = 16;
 constexpr int EXACT_MAX_SPLIT = 512;   // particles that may be split (ticket and partial slots)
@@ -1610,9 +1611,10 @@ __global__ void __launch_bounds__(EXACT_THREADS) ds32_exact(PairArgs a, const fl
             d[1] = ds_add(xi[1], DS{-A.z, -A.w});
             d[2] = ds_add(xi[2], DS{-B.x, -B.y});
             const DS r2 = ds_add(ds_add(ds_mul(d[0], d[0]), ds_mul(d[1], d[1])), ds_mul(d[2], d[2]));
-            if (!(r2.hi > 0.f)) continue;
             const DS s2 = ds_add(r2, ds_add(ie2, DS{C.x, C.y}));
-            const DS y = ds_rsqrt(s2);
+            // excluded pairs (r2 > 0 false) get 1/r = 0, as in the reference,
+            // whose terms then still carry a NaN separation into the sums
+            const DS y = r2.hi > 0.f ? ds_rsqrt(s2) : DS{0.f, 0.f};
             const DS y2 = ds_mul(y, y);
             const DS mr3 = ds_mul(DS{B.z, B.w}, ds_mul(y2, y));
             for (int c = 0; c < 3; ++c) acc[c] = ds_add(acc[c], ds_neg(ds_mul(mr3, d[c])));
