@@ -155,6 +155,54 @@ __device__ __forceinline__ DS ds_rsqrt(DS s) {
 }
 __device__ __forceinline__ double ds_value(DS a) { return (double)a.hi + (double)a.lo; }
 
+// The same operations on two independent values per instruction (packed
+// f32x2): lane .x and lane .y are separate double-single numbers.
+struct DS2 {
+    float2 hi, lo;
+};
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2 &s, float2 &e) {
+    s = __fadd2_rn(a, b);
+    const float2 bb = __fadd2_rn(s, neg2(a));
+    e = __fadd2_rn(__fadd2_rn(a, neg2(__fadd2_rn(s, neg2(bb)))), __fadd2_rn(b, neg2(bb)));
+}
+__device__ __forceinline__ void fast_two_sum2(float2 a, float2 b, float2 &s, float2 &e) {
+    s = __fadd2_rn(a, b);
+    e = __fadd2_rn(b, neg2(__fadd2_rn(s, neg2(a))));
+}
+__device__ __forceinline__ DS2 ds2_add(DS2 a, DS2 b) {
+    float2 s, e;
+    two_sum2(a.hi, b.hi, s, e);
+    e = __fadd2_rn(e, __fadd2_rn(a.lo, b.lo));
+    DS2 r;
+    fast_two_sum2(s, e, r.hi, r.lo);
+    return r;
+}
+__device__ __forceinline__ DS2 ds2_neg(DS2 a) { return DS2{neg2(a.hi), neg2(a.lo)}; }
+__device__ __forceinline__ DS2 ds2_mul(DS2 a, DS2 b) {
+    const float2 p = __fmul2_rn(a.hi, b.hi);
+    float2 e = __ffma2_rn(a.hi, b.hi, neg2(p));
+    e = __ffma2_rn(a.hi, b.lo, e);
+    e = __ffma2_rn(a.lo, b.hi, e);
+    DS2 r;
+    fast_two_sum2(p, e, r.hi, r.lo);
+    return r;
+}
+__device__ __forceinline__ DS2 ds2_rsqrt(DS2 s) {
+    float2 y0;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y0.x) : "f"(s.hi.x));
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y0.y) : "f"(s.hi.y));
+    DS2 y2;
+    y2.hi = __fmul2_rn(y0, y0);
+    y2.lo = __ffma2_rn(y0, y0, neg2(y2.hi));
+    const DS2 q = ds2_mul(s, y2);
+    const DS2 r = ds2_add(DS2{make_float2(1.0f, 1.0f), make_float2(0.0f, 0.0f)}, ds2_neg(q));
+    const float2 corr = __fmul2_rn(__fmul2_rn(y0, r.hi), make_float2(0.5f, 0.5f));
+    DS2 y;
+    fast_two_sum2(y0, corr, y.hi, y.lo);
+    return y;
+}
+
 // ---------------------------------------------------------------------------
 // mbarrier / bulk-copy PTX (sm_90+ forms, valid on sm_103a).
 // ---------------------------------------------------------------------------

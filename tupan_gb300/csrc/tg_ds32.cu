@@ -1596,42 +1596,64 @@ __global__ void __launch_bounds__(EXACT_THREADS) ds32_exact(PairArgs a, const fl
         const long long f = w / nch, ch = w % nch;
         const size_t i = list ? (size_t)list[f] : (size_t)f;
         const size_t j0 = nj * ch / nch, j1 = nj * (ch + 1) / nch;
-        DS xi[3], vi[3];
-        for (int c = 0; c < 3; ++c) xi[c] = ds_from(a.I.f[F_RX + c][i]);
+        // two j per packed step: lane .x takes j, lane .y j + EXACT_THREADS
+        DS2 xi[3], vi[3];
+        for (int c = 0; c < 3; ++c) {
+            const DS x = ds_from(a.I.f[F_RX + c][i]);
+            xi[c] = DS2{f2(x.hi), f2(x.lo)};
+        }
         if (JERK)
-            for (int c = 0; c < 3; ++c) vi[c] = ds_from(a.I.f[F_VX + c][i]);
-        const DS ie2 = ds_from(a.I.f[F_E2][i]);
-        DS acc[NO];
-        for (int c = 0; c < NO; ++c) acc[c] = DS{0.f, 0.f};
-        for (size_t p = j0 + tid; p < j1; p += EXACT_THREADS) {
-            const float4 A = __ldg(jd + EXACT_JQ * p), B = __ldg(jd + EXACT_JQ * p + 1),
-                         C = __ldg(jd + EXACT_JQ * p + 2);
-            DS d[3];
-            d[0] = ds_add(xi[0], DS{-A.x, -A.y});
-            d[1] = ds_add(xi[1], DS{-A.z, -A.w});
-            d[2] = ds_add(xi[2], DS{-B.x, -B.y});
-            const DS r2 = ds_add(ds_add(ds_mul(d[0], d[0]), ds_mul(d[1], d[1])), ds_mul(d[2], d[2]));
-            const DS s2 = ds_add(r2, ds_add(ie2, DS{C.x, C.y}));
+            for (int c = 0; c < 3; ++c) {
+                const DS v = ds_from(a.I.f[F_VX + c][i]);
+                vi[c] = DS2{f2(v.hi), f2(v.lo)};
+            }
+        const DS ie = ds_from(a.I.f[F_E2][i]);
+        const DS2 ie2{f2(ie.hi), f2(ie.lo)};
+        DS2 acc2[NO];
+        for (int c = 0; c < NO; ++c) acc2[c] = DS2{f2(0.f), f2(0.f)};
+        for (size_t p = j0 + tid; p < j1; p += 2 * EXACT_THREADS) {
+            const size_t p1 = p + EXACT_THREADS;
+            const bool has1 = p1 < j1;
+            const float4 A0 = __ldg(jd + EXACT_JQ * p), B0 = __ldg(jd + EXACT_JQ * p + 1),
+                         C0 = __ldg(jd + EXACT_JQ * p + 2);
+            // a missing second j: massless, at the i-particle (adds 0)
+            const float4 A1 = has1 ? __ldg(jd + EXACT_JQ * p1) : make_float4(xi[0].hi.x, xi[0].lo.x, xi[1].hi.x, xi[1].lo.x);
+            const float4 B1 = has1 ? __ldg(jd + EXACT_JQ * p1 + 1) : make_float4(xi[2].hi.x, xi[2].lo.x, 0.f, 0.f);
+            const float4 C1 = has1 ? __ldg(jd + EXACT_JQ * p1 + 2) : make_float4(1.f, 0.f, 0.f, 0.f);
+            DS2 d[3];
+            d[0] = ds2_add(xi[0], DS2{make_float2(-A0.x, -A1.x), make_float2(-A0.y, -A1.y)});
+            d[1] = ds2_add(xi[1], DS2{make_float2(-A0.z, -A1.z), make_float2(-A0.w, -A1.w)});
+            d[2] = ds2_add(xi[2], DS2{make_float2(-B0.x, -B1.x), make_float2(-B0.y, -B1.y)});
+            const DS2 r2 = ds2_add(ds2_add(ds2_mul(d[0], d[0]), ds2_mul(d[1], d[1])), ds2_mul(d[2], d[2]));
+            const DS2 s2 = ds2_add(r2, ds2_add(ie2, DS2{make_float2(C0.x, C1.x), make_float2(C0.y, C1.y)}));
+            DS2 y = ds2_rsqrt(s2);
             // excluded pairs (r2 > 0 false) get 1/r = 0, as in the reference,
             // whose terms then still carry a NaN separation into the sums
-            const DS y = r2.hi > 0.f ? ds_rsqrt(s2) : DS{0.f, 0.f};
-            const DS y2 = ds_mul(y, y);
-            const DS mr3 = ds_mul(DS{B.z, B.w}, ds_mul(y2, y));
-            for (int c = 0; c < 3; ++c) acc[c] = ds_add(acc[c], ds_neg(ds_mul(mr3, d[c])));
+            if (!(r2.hi.x > 0.f)) { y.hi.x = 0.f; y.lo.x = 0.f; }
+            if (!(r2.hi.y > 0.f)) { y.hi.y = 0.f; y.lo.y = 0.f; }
+            const DS2 y2 = ds2_mul(y, y);
+            const DS2 mr3 = ds2_mul(DS2{make_float2(B0.z, B1.z), make_float2(B0.w, B1.w)}, ds2_mul(y2, y));
+            for (int c = 0; c < 3; ++c) acc2[c] = ds2_add(acc2[c], ds2_neg(ds2_mul(mr3, d[c])));
             if (JERK) {
-                const float4 D = __ldg(jd + EXACT_JQ * p + 3);
-                DS v[3];
-                v[0] = ds_add(vi[0], DS{-D.x, -D.y});
-                v[1] = ds_add(vi[1], DS{-D.z, -D.w});
-                v[2] = ds_add(vi[2], DS{-C.z, -C.w});
-                const DS rv = ds_add(ds_add(ds_mul(d[0], v[0]), ds_mul(d[1], v[1])), ds_mul(d[2], v[2]));
-                const DS al = ds_mul(DS{3.0f, 0.0f}, ds_mul(rv, y2));
+                const float4 D0 = __ldg(jd + EXACT_JQ * p + 3);
+                const float4 D1 = has1 ? __ldg(jd + EXACT_JQ * p1 + 3)
+                                       : make_float4(vi[0].hi.x, vi[0].lo.x, vi[1].hi.x, vi[1].lo.x);
+                const float vzh1 = has1 ? C1.z : vi[2].hi.x, vzl1 = has1 ? C1.w : vi[2].lo.x;
+                DS2 v[3];
+                v[0] = ds2_add(vi[0], DS2{make_float2(-D0.x, -D1.x), make_float2(-D0.y, -D1.y)});
+                v[1] = ds2_add(vi[1], DS2{make_float2(-D0.z, -D1.z), make_float2(-D0.w, -D1.w)});
+                v[2] = ds2_add(vi[2], DS2{make_float2(-C0.z, -vzh1), make_float2(-C0.w, -vzl1)});
+                const DS2 rv = ds2_add(ds2_add(ds2_mul(d[0], v[0]), ds2_mul(d[1], v[1])), ds2_mul(d[2], v[2]));
+                const DS2 al = ds2_mul(DS2{f2(3.0f), f2(0.0f)}, ds2_mul(rv, y2));
                 for (int c = 0; c < 3; ++c) {
-                    const DS t = ds_add(v[c], ds_neg(ds_mul(al, d[c])));
-                    acc[3 + c] = ds_add(acc[3 + c], ds_neg(ds_mul(mr3, t)));
+                    const DS2 t = ds2_add(v[c], ds2_neg(ds2_mul(al, d[c])));
+                    acc2[3 + c] = ds2_add(acc2[3 + c], ds2_neg(ds2_mul(mr3, t)));
                 }
             }
         }
+        DS acc[NO];
+        for (int c = 0; c < NO; ++c)
+            acc[c] = ds_add(DS{acc2[c].hi.x, acc2[c].lo.x}, DS{acc2[c].hi.y, acc2[c].lo.y});
         for (int c = 0; c < NO; ++c) red[c][tid] = ds_value(acc[c]);
         __syncthreads();
         for (int h = EXACT_THREADS / 2; h > 0; h >>= 1) {
