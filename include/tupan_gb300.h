@@ -63,6 +63,17 @@ int tg_sync_status(void *stream);
 /* Precision used by the drop-in host entry points (process-wide). */
 int tg_set_host_precision(int prec);
 int tg_get_host_precision(void);
+/* Timing of the pairwise kernel (no counterpart in the reference;
+ * process-wide, off by default).  While on, split-FP32 Acc and AccJerk calls
+ * that take the ordered path (2^24 pairs and more) record CUDA events on
+ * their stream around their pairwise kernel; tg_pair_kernel_time waits for
+ * the recorded launches of `kernel` (TG_KERNEL_ACC or TG_KERNEL_ACC_JERK)
+ * and returns their total milliseconds and count, then forgets them.
+ * tg_time_pair_kernel returns the previous setting. */
+#define TG_KERNEL_ACC 1
+#define TG_KERNEL_ACC_JERK 2
+int tg_time_pair_kernel(int on);
+int tg_pair_kernel_time(int kernel, double *ms, long long *launches);
 /* Sakura evaluation (no counterpart in the reference; process-wide): 1, the
  * default, solves the pairs that take the universal-variable Kepler solver
  * apart from the others (flags -1 and +1, ni * nj <= 2^30; uses the grow-only

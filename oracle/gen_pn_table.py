@@ -1,9 +1,9 @@
 """Generate oracle/pn_table.h: the post-Newtonian pair terms as monomial tables.
 
 TEST INFRASTRUCTURE (one-time generator for the oracle's data).  Run here,
-where the reference tree is mounted:
+with the reference tree's root in TUPAN_REF:
 
-    python oracle/gen_pn_table.py /root/reference/tupan/lib/src/pn_terms.h
+    python oracle/gen_pn_table.py $TUPAN_REF/tupan/lib/src/pn_terms.h
 
 It reads the reference's PN expressions (tupan/lib/src/pn_terms.h:126-567:
 p2p_pn2, p2p_pn4, p2p_pn5, p2p_pn6, p2p_pn7), expands each `a` and `b`
@@ -100,4 +100,6 @@ def main(path):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/tupan/lib/src/pn_terms.h")
+    if len(sys.argv) < 2:
+        sys.exit("usage: %s <reference root>/tupan/lib/src/pn_terms.h" % sys.argv[0])
+    main(sys.argv[1])

@@ -1,9 +1,14 @@
 # Builds the UNMODIFIED reference C backend from its own sources (read in
 # place, never copied) into oracle/_ref/, the way tupan/lib/cffi_backend.py
 # builds it (-O3 -std=c99, CONFIG_USE_DOUBLE for float64, libm).
-# Only usable where the reference tree is mounted; outputs are git-ignored.
-#   make -f oracle/ref.mk REF=/root/reference
-REF ?= /root/reference
+# REF is the root of a reference tree (its tupan/lib/src holds the C
+# sources): the installed copy baseline/_ref, or $TUPAN_REF.  Outputs are
+# git-ignored.
+#   make -f oracle/ref.mk REF=baseline/_ref
+REF ?= $(TUPAN_REF)
+ifeq ($(strip $(REF)),)
+$(error set REF=<reference root> or TUPAN_REF)
+endif
 SRC := $(REF)/tupan/lib/src
 HERE := $(dir $(lastword $(MAKEFILE_LIST)))
 OUT := $(HERE)_ref

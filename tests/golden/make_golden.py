@@ -1,9 +1,9 @@
 """Generate the golden fixtures in tests/golden/ from the reference C backend.
 
-Run where the reference tree is mounted:
+Run where a reference tree is available, its root in TUPAN_REF:
 
-    make -f oracle/ref.mk REF=/root/reference
-    python tests/golden/make_golden.py
+    make -f oracle/ref.mk REF=$TUPAN_REF
+    TUPAN_REF=<reference root> python tests/golden/make_golden.py
 
 The reference's own kernels (tupan/lib/src/*_kernel.c, compiled unmodified by
 oracle/ref.mk into oracle/_ref/libtupan_ref_f64.so) are called through
@@ -187,10 +187,11 @@ def integrator_ics(n=48, seed=7):
     return d
 
 
-def reference_trajectories(ref_root="/root/reference"):
+def reference_trajectories(ref_root=None):
     """Run the reference integrators (imported from the reference tree, with
     HOME redirected for its cffi build cache) on the same initial state."""
     import tempfile
+    ref_root = ref_root or os.environ["TUPAN_REF"]
     os.environ["HOME"] = tempfile.mkdtemp(prefix="tupan_home_")
     sys.path.insert(0, ref_root)
     from tupan.integrator import Integrator

@@ -91,6 +91,11 @@ def _load():
     lib.tg_acc_vjp.argtypes = [ctypes.c_size_t] + [_DP] * 12 + [ctypes.c_int, _DP]
     lib.tg_probe_fma_tflops.restype = ctypes.c_double
     lib.tg_probe_fma_tflops.argtypes = [ctypes.c_int, ctypes.c_int, _DP]
+    lib.tg_time_pair_kernel.restype = ctypes.c_int
+    lib.tg_time_pair_kernel.argtypes = [ctypes.c_int]
+    lib.tg_pair_kernel_time.restype = ctypes.c_int
+    lib.tg_pair_kernel_time.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                        ctypes.POINTER(ctypes.c_longlong)]
     lib.tg_set_sakura_split.restype = ctypes.c_int
     lib.tg_set_sakura_split.argtypes = [ctypes.c_int]
     lib.tg_check_bounded_wait.restype = ctypes.c_int
@@ -124,6 +129,18 @@ def call_device(name, ni, iptrs, nj, jptrs, scalars, optrs, prec, stream):
     fn = getattr(lib, "tg_" + name)
     rc = fn(ni, *iptrs, nj, *jptrs, *scalars, *optrs, int(prec), stream)
     return check(rc, "tg_" + name)
+
+
+KERNEL_ACC = 1
+KERNEL_ACC_JERK = 2
+
+
+def pair_kernel_time(kernel):
+    """(total ms, launches) of the ordered pairwise kernel of `kernel`
+    (KERNEL_ACC or KERNEL_ACC_JERK) recorded while tg_time_pair_kernel was on."""
+    ms, n = ctypes.c_double(), ctypes.c_longlong()
+    check(lib.tg_pair_kernel_time(kernel, ctypes.byref(ms), ctypes.byref(n)), "tg_pair_kernel_time")
+    return ms.value, n.value
 
 
 def sync_status(stream=None):

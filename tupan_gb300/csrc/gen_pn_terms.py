@@ -1,8 +1,8 @@
 """Generate tg_pn_terms.cuh: straight-line CUDA for the post-Newtonian pair terms.
 
-One-time generator, run where the reference tree is mounted:
+One-time generator, run with the reference tree's root in TUPAN_REF:
 
-    python tupan_gb300/csrc/gen_pn_terms.py /root/reference/tupan/lib/src/pn_terms.h
+    python tupan_gb300/csrc/gen_pn_terms.py $TUPAN_REF/tupan/lib/src/pn_terms.h
 
 The post-Newtonian two-body accelerations (1PN, 2PN, 2.5PN, 3PN and 3.5PN
 terms of the harmonic-coordinate equations of motion) are a fixed table of
@@ -165,4 +165,6 @@ def main(path):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/tupan/lib/src/pn_terms.h")
+    if len(sys.argv) < 2:
+        sys.exit("usage: %s <reference root>/tupan/lib/src/pn_terms.h" % sys.argv[0])
+    main(sys.argv[1])

@@ -259,6 +259,16 @@ int tg_get_host_precision(void) { return g_host_prec; }
 
 int tg_set_sakura_split(int on) { return g_sakura_split.exchange(on ? 1 : 0); }
 
+int tg_time_pair_kernel(int on) { return tg::prof_enable(on); }
+
+int tg_pair_kernel_time(int kernel, double *ms, long long *launches) {
+    if (!ms || !launches || (kernel != TG_KERNEL_ACC && kernel != TG_KERNEL_ACC_JERK))
+        return fail(TG_EINVAL, "tg_pair_kernel_time: kernel must be TG_KERNEL_ACC or TG_KERNEL_ACC_JERK");
+    cudaError_t e = tg::prof_read(kernel == TG_KERNEL_ACC ? tg::K_ACC : tg::K_ACC_JERK, ms, launches);
+    if (e != cudaSuccess) return fail(TG_ECUDA, "tg_pair_kernel_time", e);
+    return TG_OK;
+}
+
 int tg_phi(size_t ni, const double *im, const double *irx, const double *iry, const double *irz,
            const double *ie2, size_t nj, const double *jm, const double *jrx, const double *jry,
            const double *jrz, const double *je2, double *iphi, int prec, void *stream) {

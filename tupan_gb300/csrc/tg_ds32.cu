@@ -30,7 +30,9 @@
 // into Kahan-compensated accumulators.  The roofline is the FP32 pipe (FFMA2
 // issue).
 #include <atomic>
+#include <mutex>
 #include <type_traits>
+#include <vector>
 
 #include "tg_device.cuh"
 #include "tg_internal.h"
@@ -1571,7 +1573,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs o
 // and as the whole split-FP32 Acc and AccJerk of calls below 2^24 pairs.
 // With F particles and G CTAs each particle's j-range is cut into
 // nch = clamp(G / F, 1, EXACT_MAX_CHUNKS) chunks; a CTA reduces a chunk in
-// a fixed-order tree, and with nch > 1 the last chunk of a particle to
+// a fixed-order double-single tree, and with nch > 1 the last chunk of a particle to
 // finish (atomic ticket) adds the chunk sums in chunk order: the result is
 // deterministic.  Pairs with r2 > 0 false get 1/r = 0 as in the reference
 // (acc_kernel_common.h, acc_jerk_kernel_common.h; smoothing.h), so a NaN
@@ -1583,7 +1585,8 @@ template <bool JERK>
 __global__ void __launch_bounds__(EXACT_THREADS) ds32_exact(PairArgs a, const float4 *jd, const int *count,
                                                              const int *list, double *partial, int *ticket) {
     constexpr int NO = JERK ? 6 : 3;
-    __shared__ double red[NO][EXACT_THREADS];
+    __shared__ DS red[NO][EXACT_THREADS];
+    __shared__ DS s_i[7];   // the i-particle: x, y, z, e2, vx, vy, vz
     const long long F = list ? (long long)*count : (long long)a.ni;
     if (F == 0) return;
     const int G = gridDim.x, tid = threadIdx.x;
@@ -1596,19 +1599,18 @@ __global__ void __launch_bounds__(EXACT_THREADS) ds32_exact(PairArgs a, const fl
         const long long f = w / nch, ch = w % nch;
         const size_t i = list ? (size_t)list[f] : (size_t)f;
         const size_t j0 = nj * ch / nch, j1 = nj * (ch + 1) / nch;
+        // the i-particle's double-single values, converted once per CTA
+        if (tid < (JERK ? 7 : 4)) {
+            const int fld = tid < 3 ? F_RX + tid : (tid == 3 ? F_E2 : F_VX + tid - 4);
+            s_i[tid] = ds_from(a.I.f[fld][i]);
+        }
+        __syncthreads();
         // two j per packed step: lane .x takes j, lane .y j + EXACT_THREADS
         DS2 xi[3], vi[3];
-        for (int c = 0; c < 3; ++c) {
-            const DS x = ds_from(a.I.f[F_RX + c][i]);
-            xi[c] = DS2{f2(x.hi), f2(x.lo)};
-        }
+        for (int c = 0; c < 3; ++c) xi[c] = DS2{f2(s_i[c].hi), f2(s_i[c].lo)};
         if (JERK)
-            for (int c = 0; c < 3; ++c) {
-                const DS v = ds_from(a.I.f[F_VX + c][i]);
-                vi[c] = DS2{f2(v.hi), f2(v.lo)};
-            }
-        const DS ie = ds_from(a.I.f[F_E2][i]);
-        const DS2 ie2{f2(ie.hi), f2(ie.lo)};
+            for (int c = 0; c < 3; ++c) vi[c] = DS2{f2(s_i[4 + c].hi), f2(s_i[4 + c].lo)};
+        const DS2 ie2{f2(s_i[3].hi), f2(s_i[3].lo)};
         DS2 acc2[NO];
         for (int c = 0; c < NO; ++c) acc2[c] = DS2{f2(0.f), f2(0.f)};
         for (size_t p = j0 + tid; p < j1; p += 2 * EXACT_THREADS) {
@@ -1654,19 +1656,19 @@ __global__ void __launch_bounds__(EXACT_THREADS) ds32_exact(PairArgs a, const fl
         DS acc[NO];
         for (int c = 0; c < NO; ++c)
             acc[c] = ds_add(DS{acc2[c].hi.x, acc2[c].lo.x}, DS{acc2[c].hi.y, acc2[c].lo.y});
-        for (int c = 0; c < NO; ++c) red[c][tid] = ds_value(acc[c]);
+        for (int c = 0; c < NO; ++c) red[c][tid] = acc[c];
         __syncthreads();
         for (int h = EXACT_THREADS / 2; h > 0; h >>= 1) {
             if (tid < h)
-                for (int c = 0; c < NO; ++c) red[c][tid] += red[c][tid + h];
+                for (int c = 0; c < NO; ++c) red[c][tid] = ds_add(red[c][tid], red[c][tid + h]);
             __syncthreads();
         }
         if (nch == 1) {
             if (tid == 0)
-                for (int c = 0; c < NO; ++c) a.out[c][i] = red[c][0];
+                for (int c = 0; c < NO; ++c) a.out[c][i] = ds_value(red[c][0]);
         } else if (tid == 0) {
             double *mine = partial + ((size_t)f * EXACT_MAX_CHUNKS + ch) * NO;
-            for (int c = 0; c < NO; ++c) mine[c] = red[c][0];
+            for (int c = 0; c < NO; ++c) mine[c] = ds_value(red[c][0]);
             __threadfence();
             if (atomicAdd(ticket + f, 1) == (int)nch - 1) {
                 __threadfence();
@@ -2176,6 +2178,39 @@ static bool same_sets(const PairArgs &p, int nfields) {
     return true;
 }
 
+// Optional timing of the ordered pairwise kernel (tg_time_pair_kernel):
+// CUDA events recorded on the call's stream around its launch.
+static std::atomic<int> g_prof{0};
+static std::mutex g_prof_mu;
+struct ProfRec {
+    int kernel;
+    cudaEvent_t e0, e1;
+};
+static std::vector<ProfRec> g_prof_rec;
+
+int prof_enable(int on) { return g_prof.exchange(on ? 1 : 0); }
+
+cudaError_t prof_read(int kernel, double *ms, long long *launches) {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    *ms = 0.0;
+    *launches = 0;
+    cudaError_t err = cudaSuccess;
+    std::vector<ProfRec> keep;
+    for (const ProfRec &r : g_prof_rec) {
+        if (r.kernel != kernel) { keep.push_back(r); continue; }
+        float t = 0.f;
+        cudaError_t e = cudaEventSynchronize(r.e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, r.e0, r.e1);
+        if (e != cudaSuccess && err == cudaSuccess) err = e;
+        *ms += t;
+        *launches += 1;
+        cudaEventDestroy(r.e0);
+        cudaEventDestroy(r.e1);
+    }
+    g_prof_rec.swap(keep);
+    return err;
+}
+
 template <class K>
 static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_bytes, int sms, cudaStream_t s) {
     const bool same = same_sets(p, nfields);
@@ -2233,8 +2268,15 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
     a.flag_list = flags + 64;
     a.tau = ord_tau(p.nj);
     const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
+    ProfRec pr{K::NP == 7 ? K_ACC_JERK : K_ACC, nullptr, nullptr};
+    const bool prof = g_prof.load() && cudaEventCreate(&pr.e0) == cudaSuccess &&
+                      cudaEventCreate(&pr.e1) == cudaSuccess && cudaEventRecord(pr.e0, s) == cudaSuccess;
     if (g.jsub == 2) ds32_ord<K, 2><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
     else ds32_ord<K, 1><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
+    if (prof && cudaEventRecord(pr.e1, s) == cudaSuccess) {
+        std::lock_guard<std::mutex> lk(g_prof_mu);
+        g_prof_rec.push_back(pr);
+    }
     ds32_exact<false><<<(unsigned)(sms * 4), EXACT_THREADS, 0, s>>>(p, jd, flags, flags + 64, ref_part, ref_ticket);
     return cudaGetLastError();
 }

@@ -114,6 +114,10 @@ void set_last_error(const char *msg);
 size_t ds32_workspace_bytes_capped(int kernel, size_t ni, size_t nj, int sms, long long max_grid);
 cudaError_t launch_ds32_capped(int kernel, const PairArgs &a, void *ws, size_t ws_bytes, int sms,
                                long long max_grid, cudaStream_t s);
+// Timing of the ordered pairwise kernel (tg_time_pair_kernel).
+int prof_enable(int on);
+cudaError_t prof_read(int kernel, double *ms, long long *launches);
+
 // Status bits tg_acc_jerk_noalloc left on the current device (read and
 // cleared; no allocation).
 cudaError_t noalloc_take_status(cudaStream_t s, unsigned *bits);
