@@ -12,21 +12,29 @@ Printed JSON line (rank 0):
   e2e          the same metric through the drop-in host entry points
                acc_kernel / acc_jerk_kernel (libtupan.h signatures) with host
                buffers, host<->device copies inside the timed region
-  roofline     the AccJerk kernel: reference-counted 42 flop/interaction x
-               interactions / kernel time, against the FP32 FMA peak measured
-               on this GPU by tg_probe_fma_tflops
+  roofline     the AccJerk pairwise kernel (ds32_ord<AccJerkOrd>):
+               reference-counted 42 flop/interaction x interactions / that
+               kernel's own duration (CUDA events the library records around
+               it on the call's stream, tg_time_pair_kernel), against the FP32
+               FMA peak measured on this GPU by tg_probe_fma_tflops; call_frac
+               is the same over the whole call (spatial sort, record
+               preparation, plan, pairwise kernel, double-single recompute)
   fp64         the FP64 GPU kernels on the same workload (bit-identical to the
                reference C backend) and the split-FP32 speed-up over them
   force_error  per-particle |a_ds32 - a_fp64| / |a_fp64| (and jerk)
   other_kernels  split-FP32 Phi, SnapCrackle, Tstep and PNAcc on the same
                workload, FP64 Sakura on its first 4096 particles (device time)
-  cpu_baseline the CPU oracle port (same algorithm and operation order as the
-               reference C backend) on the host cores, bounded sample
+  energy       |dE/E| of a short shared-step SIA21 kdk leapfrog of the same
+               workload in split FP32 and in FP64, and their ratio
+  cpu_baseline the reference's own C backend (compiled unmodified from the
+               installed copy into oracle/_ref by __graft_entry__.build; kind
+               "reference"), else the CPU oracle port (same algorithm and
+               operation order; kind "port"), on all host cores, bounded sample
   clocks       nvidia-smi SM clock and throttle reasons during the timed region
 
-`--impl reference` times the reference algorithm on the host CPU (the oracle
-port; the reference tree itself is not present on the GPU machine) on a
-bounded sample of the same workload and prints the same metric.
+`--impl reference` times that same CPU implementation on a bounded sample of
+the same workload and prints the same metric; it imports nothing of the
+GPU library.
 """
 import argparse
 import ctypes
@@ -48,15 +56,16 @@ EPS = 1e-3
 SEED = 20261203
 FLOP_ACC = 20       # tupan/lib/src/acc_kernel_common.h:38
 FLOP_ACC_JERK = 42  # tupan/lib/src/acc_jerk_kernel_common.h:56
-# DRAM bytes (read + write) of one split-FP32 AccJerk launch on this workload,
-# from an ncu capture (profiles/ds32_acc_jerk_n65536.txt)
-TRAFFIC_ACC_JERK_N65536 = 6.88e6
+# DRAM bytes (read + write) of one AccJerk pairwise-kernel launch on this
+# workload, from an ncu capture (profiles/ds32_ord_acc_jerk_n65536.txt)
+TRAFFIC_ACC_JERK_N65536 = 7.22e6
 METRIC = "Gint/s Acc+AccJerk split-FP32 (N=65536 Plummer-Salpeter, eps2=1e-6)"
-# library kernels per step: Acc = prepare (records, softening flags,
-# zeroed tickets) + stream-K; AccJerk = prepare + coincidence check (insert,
-# lookup, mode) + the masked and unmasked stream-K forms (the one not
-# selected exits at entry)
-LAUNCHES_PER_STEP = 8
+# library kernels per ordered Acc or AccJerk call: spatial order (bounds,
+# keys, the radix sort's histogram, exclusive-sum and four one-sweep passes),
+# record preparation, i-tile boxes, plan, the prefix sum's two launches, CTA
+# bounds, the pairwise kernel and the double-single recompute
+LAUNCHES_PER_CALL = 17
+LAUNCHES_PER_STEP = 2 * LAUNCHES_PER_CALL
 SMALL_SIZES = (4096, 16384)
 P5 = ("mass", "rx", "ry", "rz", "eps2")
 P8 = P5 + ("vx", "vy", "vz")
@@ -72,6 +81,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=3.0,
                     help="target wall time of each CPU baseline sample")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--energy-steps", type=int, default=8,
+                    help="steps of the leapfrog whose |dE/E| is reported in both precisions")
     return ap.parse_args()
 
 
@@ -83,26 +94,78 @@ def workload(n, rank):
 def config(n):
     return {"workload": "plummer-salpeter", "n": n, "imf": "salpeter -2.35 [0.1,100], M=1",
             "eps2_pair": 2 * (EPS * EPS / 2), "units": "henon", "step": "acc + acc_jerk, i=j=all",
-            "interactions_per_step": 2 * n * n, "precision": "ds32 (hi/lo positions, Kahan-folded FP32)",
+            "interactions_per_step": 2 * n * n,
+            "precision": "ds32 (hi/lo or block-relative positions, Kahan-folded FP32 sums, "
+                         "double-single recompute of strongly cancelling particles)",
             "l2": "flushed between timed steps (256 MiB write)", "seed": SEED}
+
+
+def pn_flop(order):
+    """Flop per PNAcc interaction: the reference's 40 for the pair geometry
+    (pnacc_kernel_common.h:70, "40+???") plus the generated post-Newtonian
+    polynomial up to `order` (tupan_gb300/csrc/tg_pn_terms.cuh: powers, then
+    one block per order; fma = 2, every other +, -, * = 1)."""
+    import re
+    src = open(os.path.join(ROOT, "tupan_gb300", "csrc", "tg_pn_terms.cuh")).read()
+    body = src[src.index("pn_factors"):]
+    body = body[body.index("{") + 1:]
+    total, cur = 0, None
+    for line in body.splitlines():
+        m = re.search(r"if \(order >= (\d)ul\)", line)
+        if m:
+            cur = int(m.group(1))
+            continue
+        code = line.split("//")[0].strip()
+        if not code.endswith(";") or code.startswith(("return", "if")) or (cur is not None and cur > order):
+            continue
+        f = 2 * code.count("fma(")
+        t = re.sub(r"T\(-?[\d.]+\)", "K", code).replace("fma(", "(")
+        if "+=" in t or "-=" in t:
+            f += 1
+        t = t.replace("+=", "=").replace("-=", "=")
+        rhs = t.split("=", 1)[1] if "=" in t else ""
+        f += len(re.findall(r"[\*\+]|(?<=[\w\)])\s*-", rhs))
+        total += f
+    return 40 + total
 
 
 # ---------------------------------------------------------------------------
 # CPU baseline (oracle port of the reference algorithm)
 # ---------------------------------------------------------------------------
+def cpu_impl():
+    """The reference's own C backend when oracle/_ref holds its build, else
+    the oracle port: (calc(name, I, J, threads), kind)."""
+    from oracle import oracle as om
+    if om.reference_available():
+        ref = om.ReferenceLib()
+        from concurrent.futures import ThreadPoolExecutor
+
+        def calc(name, I, J, threads):
+            # the reference C is single-threaded: contiguous i-slices on a
+            # thread pool (ctypes releases the GIL during the call)
+            ni = len(I["mass"])
+            cuts = np.linspace(0, ni, threads + 1).astype(int)
+            with ThreadPoolExecutor(threads) as ex:
+                list(ex.map(lambda k: ref.calc(name, {f: v[cuts[k]:cuts[k + 1]] for f, v in I.items()}, J),
+                            [k for k in range(threads) if cuts[k + 1] > cuts[k]]))
+        return calc, "reference"
+    om.build()
+    orc = om.Oracle()
+    return (lambda name, I, J, threads: orc.calc(name, I, J, nthreads=threads)), "port"
+
+
 def cpu_sample(d, seconds, threads):
     """Time FP64 Acc + AccJerk of the first ni_s i-particles against all N.
 
     ni_s is calibrated so one sample takes about `seconds` of wall time."""
-    from oracle.oracle import Oracle
-    orc = Oracle()
+    calc, kind = cpu_impl()
     n = len(d["mass"])
 
     def run(ni):
         I = {k: v[:ni] for k, v in d.items()}
         t0 = time.perf_counter()
-        orc.calc("acc", I, d, nthreads=threads)
-        orc.calc("acc_jerk", I, d, nthreads=threads)
+        calc("acc", I, d, threads)
+        calc("acc_jerk", I, d, threads)
         return time.perf_counter() - t0
 
     ni = max(threads, 64)
@@ -113,7 +176,7 @@ def cpu_sample(d, seconds, threads):
     ni = int(min(n, max(threads, ni * seconds / max(t, 1e-6))))
     t = run(ni)
     return {"value": 2.0 * ni * n / t / 1e9, "unit": "Gint/s", "cores": threads,
-            "kind": "port", "seconds": t,
+            "kind": kind, "seconds": t,
             "sample": "FP64 acc + acc_jerk, %d i-particles x %d j-particles (%.3g interactions)"
                       % (ni, n, 2.0 * ni * n)}
 
@@ -121,8 +184,6 @@ def cpu_sample(d, seconds, threads):
 def reference_arm(args, rank, world):
     if rank != 0:
         return
-    from oracle import oracle as om
-    om.build()
     d = workload(args.particles, 0)
     threads = os.cpu_count() or 1
     for _ in range(max(args.warmup, 0)):
@@ -283,12 +344,26 @@ def other_kernels(dev, sp, T, outs, n, peak32):
         med = float(np.median(ms))
         rec = {"n": m, "precision": "ds32" if prec == _native.PREC_DS32 else "fp64", "ms": med,
                "gint_s": m * m / (med * 1e-3) / 1e9}
-        if name in FLOP_OTHER and peak32 > 0:
-            rec["frac"] = FLOP_OTHER[name] * m * m / (med * 1e-3) / 1e12 / peak32
+        flop = FLOP_OTHER.get(name) or (pn_flop(5) if name == "pnacc" else None)
+        if flop and peak32 > 0:
+            rec["flop_per_interaction"] = flop
+            rec["frac"] = flop * m * m / (med * 1e-3) / 1e12 / peak32
         res[name] = rec
     st = _native.sync_status(sp)
     res["status"] = st
     return res
+
+
+def energy_drift(n, steps):
+    """|dE/E| of a shared-step SIA21 kdk leapfrog (dt = 1/1024, Tstep each
+    step) of the benchmark workload, split FP32 against FP64; energies from
+    the FP64 Phi kernel (tupan_gb300.runs.precision_run)."""
+    from tupan_gb300.runs import precision_run
+    r = precision_run(n=n, steps=steps, dt=1.0 / 1024, seed=SEED, probe_every=0)
+    return {"steps": steps, "dt": 1.0 / 1024, "method": "sia21s.kdk",
+            "ds32": r["ds32"]["rel_energy_error"], "fp64": r["float64"]["rel_energy_error"],
+            "ratio_ds32_over_fp64": r["energy_drift_ratio_ds32_over_fp64"],
+            "ms_per_step_ds32": r["ds32"]["ms_per_step"], "ms_per_step_fp64": r["float64"]["ms_per_step"]}
 
 
 def ours(args, rank, world, dist):
@@ -325,6 +400,9 @@ def ours(args, rank, world, dist):
         w += 1
 
     ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    _native.pair_kernel_time(_native.KERNEL_ACC)        # drop earlier records
+    _native.pair_kernel_time(_native.KERNEL_ACC_JERK)
+    _native.lib.tg_time_pair_kernel(1)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -340,6 +418,9 @@ def ours(args, rank, world, dist):
     torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     wall = time.perf_counter() - wall0
+    _native.lib.tg_time_pair_kernel(0)
+    k_acc_ms, k_acc_n = _native.pair_kernel_time(_native.KERNEL_ACC)
+    k_aj_ms, k_aj_n = _native.pair_kernel_time(_native.KERNEL_ACC_JERK)
     if dist:
         dist.barrier()
     clk = clocks.stop()
@@ -363,22 +444,30 @@ def ours(args, rank, world, dist):
 
     peak32 = _native.lib.tg_probe_fma_tflops(0, 20000, sp)
     peak64 = _native.lib.tg_probe_fma_tflops(1, 2000, sp)
-    achieved = FLOP_ACC_JERK * n * n / (aj_ms * 1e-3) / 1e12
+    # the pairwise kernel's own average duration (events around its launch)
+    kaj_ms = k_aj_ms / k_aj_n if k_aj_n else aj_ms
+    kacc_ms = k_acc_ms / k_acc_n if k_acc_n else acc_ms
+    achieved = FLOP_ACC_JERK * n * n / (kaj_ms * 1e-3) / 1e12
+    call_achieved = FLOP_ACC_JERK * n * n / (aj_ms * 1e-3) / 1e12
     line = {"metric": METRIC, "value": value, "unit": "Gint/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "ds32", "data": "synthetic",
             "config": config(n), "gpu_launches": LAUNCHES_PER_STEP * args.steps,
-            "kernels": {"acc_ds32": {"ms": acc_ms, "gint_s": n * n / (acc_ms * 1e-3) / 1e9},
-                        "acc_jerk_ds32": {"ms": aj_ms, "gint_s": n * n / (aj_ms * 1e-3) / 1e9}},
-            "roofline": {"bound": "fp32", "kernel": "ds32_streamk<AccJerkDS>",
+            "kernels": {"acc_ds32": {"ms": acc_ms, "gint_s": n * n / (acc_ms * 1e-3) / 1e9,
+                                     "pair_kernel_ms": kacc_ms, "pair_kernel_launches": k_acc_n},
+                        "acc_jerk_ds32": {"ms": aj_ms, "gint_s": n * n / (aj_ms * 1e-3) / 1e9,
+                                          "pair_kernel_ms": kaj_ms, "pair_kernel_launches": k_aj_n}},
+            "roofline": {"bound": "fp32", "kernel": "ds32_ord<AccJerkOrd<2>>",
                          "achieved": achieved, "peak": peak32, "unit": "TFLOP/s",
                          "frac": achieved / peak32 if peak32 > 0 else None,
+                         "call_achieved": call_achieved,
+                         "call_frac": call_achieved / peak32 if peak32 > 0 else None,
                          "traffic": TRAFFIC_ACC_JERK_N65536 if n == N_DEFAULT else None,
                          "traffic_source": "ncu dram__bytes_read+write of one AccJerk launch at N=65536",
                          "flop_per_interaction": FLOP_ACC_JERK,
                          "peak_source": "measured: tg_probe_fma_tflops (FFMA2 chains, this GPU)",
                          "peak_fp64_tflops": peak64,
-                         "acc_frac": (FLOP_ACC * n * n / (acc_ms * 1e-3) / 1e12) / peak32 if peak32 > 0 else None},
+                         "acc_frac": (FLOP_ACC * n * n / (kacc_ms * 1e-3) / 1e12) / peak32 if peak32 > 0 else None},
             "clocks": clk, "wall_s": wall}
 
     if not args.no_fp64:
@@ -407,6 +496,7 @@ def ours(args, rank, world, dist):
     if rank == 0 and not args.no_fp64:
         line["sizes"] = small_sizes(dev, sp)
         line["other_kernels"] = other_kernels(dev, sp, T, outs, n, peak32)
+        line["energy"] = energy_drift(n, args.energy_steps)
 
     # ---- end to end through the drop-in host entry points ---------------
     pin = {k: torch.tensor(d[k], dtype=torch.float64).pin_memory() for k in P8}

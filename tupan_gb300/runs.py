@@ -59,7 +59,7 @@ def precision_run(n=65536, steps=128, dt=1.0 / 1024, seed=20261203, probe_every=
         for s in range(steps):
             integ.evolve_step((s + 1) * dt)
             integ.particle_system.set_tstep(integ.particle_system, dt)
-            if prec == "ds32" and (s + 1) % probe_every == 0:
+            if prec == "ds32" and probe_every and (s + 1) % probe_every == 0:
                 torch.cuda.synchronize()
                 t1 = time.perf_counter()
                 probes.append({"step": s + 1, "force_error": force_error(integ.particle_system)})
