@@ -1,10 +1,12 @@
 """The Acc adjoint (tg_acc_vjp) and the differentiable leapfrog.
 
 * VJP against PyTorch FP64 autograd through a naive O(N^2) restatement of
-  the softened acceleration: FP64 to 1e-10 relative, split FP32 to 1e-4.
+  the softened acceleration: FP64 to 1e-10 relative, split FP32 (the
+  double-single adjoint kernel) to 1e-9.
 * Gradient of a leapfrog trajectory loss with respect to initial positions,
   velocities and masses (adjoint, checkpointed) against FP64 central finite
-  differences of the same forward map: 1e-6 relative.
+  differences of the same forward map: 1e-6 relative, in FP64 and in split
+  FP32 (ordered Acc forward, double-single adjoint).
 """
 import numpy as np
 import pytest
@@ -40,7 +42,7 @@ def naive_acc(r, m, e2):
     return -(d * (m[None, :] * q3)[None]).sum(2)
 
 
-@pytest.mark.parametrize("prec,tol", [("float64", 1e-10), ("ds32", 1e-4)])
+@pytest.mark.parametrize("prec,tol", [("float64", 1e-10), ("ds32", 1e-9)])
 def test_vjp_matches_torch_autograd(ad, prec, tol):
     r, v, m, e2 = system(300, seed=1)
     g = torch.randn(3, 300, dtype=torch.float64, device="cuda")
@@ -121,6 +123,44 @@ def test_leapfrog_gradient_matches_finite_differences(ad):
                     am = dict(ap)
                     ap[which], am[which] = plus, minus
                     return float(loss(ap["r"], ap["v"], ap["m"]) - loss(am["r"], am["v"], am["m"])) / (2 * step)
+
+                fd = (4 * central(h) - central(2 * h)) / 3
+                g = float(grad[idx])
+                assert abs(fd - g) <= 1e-6 * abs(g) + 1e-9 * float(grad.abs().max()), (which, idx, fd, g)
+
+
+def test_ds32_leapfrog_gradient_matches_fp64_finite_differences(ad):
+    """The split-FP32 leapfrog (Acc on the ordered split-FP32 path at
+    N = 4096, the double-single adjoint) differentiated by the adjoint,
+    against Richardson-extrapolated FP64 central differences of the FP64
+    forward map: 1e-6 relative, on 12 coordinates of r0, v0 and m."""
+    n, steps, dt = 4096, 4, 1.0 / 256
+    r0, v0, m, e2 = system(n, seed=8, e2=1e-4)
+    target, _ = ad.leapfrog(r0 + 0.01, v0, m * 1.01, e2, dt, steps, "float64")
+
+    def loss(r, v, mm, prec):
+        rf, _ = ad.leapfrog(r, v, mm, e2, dt, steps, prec, checkpoint_every=2)
+        return ad.loss_to_target(rf, target)
+
+    r = r0.clone().requires_grad_(True)
+    v = v0.clone().requires_grad_(True)
+    mm = m.clone().requires_grad_(True)
+    loss(r, v, mm, "ds32").backward()
+    rng = np.random.default_rng(9)
+    with torch.no_grad():
+        for which, base, grad, h in (("r", r0, r.grad, 1e-4), ("v", v0, v.grad, 1e-4), ("m", m, mm.grad, 1e-7)):
+            for _ in range(4):
+                idx = tuple(int(rng.integers(0, s)) for s in base.shape)
+
+                def central(step):
+                    plus, minus = base.clone(), base.clone()
+                    plus[idx] += step
+                    minus[idx] -= step
+                    ap = {"r": r0, "v": v0, "m": m}
+                    am = dict(ap)
+                    ap[which], am[which] = plus, minus
+                    return float(loss(ap["r"], ap["v"], ap["m"], "float64")
+                                 - loss(am["r"], am["v"], am["m"], "float64")) / (2 * step)
 
                 fd = (4 * central(h) - central(2 * h)) / 3
                 g = float(grad[idx])

@@ -1201,16 +1201,17 @@ struct AccOrd {
 };
 
 // Double-single j-data of the exact kernel (ds32_exact), EXACT_JQ float4
-// per j: {xh, xl, yh, yl} {zh, zl, mh, ml} {e2h, e2l, vzh, vzl}
-// {vxh, vxl, vyh, vyl} (velocities only when `vel`, else zero).
+// per j: {xh, xl, yh, yl} {zh, zl, mh, ml} {e2h, e2l, uzh, uzl}
+// {uxh, uxl, uyh, uyl}, where u is the vector field `ufield` (F_VX: the
+// velocity, F_AX: the adjoint's upstream gradient) or zero (ufield < 0).
 constexpr int EXACT_JQ = 4;
-__device__ __forceinline__ void write_exact_record(float4 *r, const PSet &J, size_t j, bool vel) {
+__device__ __forceinline__ void write_exact_record(float4 *r, const PSet &J, size_t j, int ufield) {
     float xh[3], xl[3], mh, ml, eh, el, vh[3] = {0.f, 0.f, 0.f}, vl[3] = {0.f, 0.f, 0.f};
     for (int c = 0; c < 3; ++c) split_ds(J.f[F_RX + c][j], xh[c], xl[c]);
     split_ds(J.f[F_M][j], mh, ml);
     split_ds(J.f[F_E2][j], eh, el);
-    if (vel)
-        for (int c = 0; c < 3; ++c) split_ds(J.f[F_VX + c][j], vh[c], vl[c]);
+    if (ufield >= 0)
+        for (int c = 0; c < 3; ++c) split_ds(J.f[ufield + c][j], vh[c], vl[c]);
     r[0] = make_float4(xh[0], xl[0], xh[1], xl[1]);
     r[1] = make_float4(xh[2], xl[2], mh, ml);
     r[2] = make_float4(eh, el, vh[2], vl[2]);
@@ -1276,7 +1277,7 @@ __global__ void __launch_bounds__(DS_TILE) ds32_ord_prepare(PSet J, size_t nj, c
         else { h[c] = 0.f; l[c] = 0.f; }
     }
     K::write_record(rec + (p >> 1) * (size_t)(2 * K::JF), (int)(p & 1), h, l, J, j, valid);
-    if (valid) write_exact_record(jd + EXACT_JQ * p, J, j, false);
+    if (valid) write_exact_record(jd + EXACT_JQ * p, J, j, -1);
     if (tile_e2 != nullptr) {   // the tile's common float softening, or NaN
         const unsigned mine = valid ? __float_as_uint(__double2float_rn(J.f[F_E2][j])) : 0u;
         if (q == 0) s_first = mine;   // the tile's first j is always valid
@@ -1565,12 +1566,14 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs o
     }
 }
 
-// Acceleration (and with JERK the jerk) in double-single arithmetic, ~2^-43
-// per term, from the hi/lo floats of write_exact_record (no FP64 operation
-// in the pair loop), for the i-particles listed in `list` (count *count) or,
-// with list == nullptr, for all ni of them.  It serves twice: as the
-// recompute of the particles the ordered kernels flag (acceleration only),
-// and as the whole split-FP32 Acc and AccJerk of calls below 2^24 pairs.
+// Double-single arithmetic, ~2^-43 per term, from the hi/lo floats of
+// write_exact_record (no FP64 operation in the pair loop), for the
+// i-particles listed in `list` (count *count) or, with list == nullptr, for
+// all ni of them.  MODE: EX_ACC (acceleration), EX_ACC_JERK (and the jerk),
+// EX_VJP (the adjoint of Acc: r-bar and m-bar, the pair formulas of the FP64
+// AccVjp64).  It serves as the recompute of the particles the ordered kernels
+// flag (acceleration only), as the whole split-FP32 Acc and AccJerk of calls
+// below 2^24 pairs, and as the split-FP32 adjoint.
 // With F particles and G CTAs each particle's j-range is cut into
 // nch = clamp(G / F, 1, EXACT_MAX_CHUNKS) chunks; a CTA reduces a chunk in
 // a fixed-order double-single tree, and with nch > 1 the last chunk of a particle to
@@ -1581,12 +1584,14 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs o
 constexpr int EXACT_THREADS = 256;
 constexpr int EXACT_MAX_CHUNKS = 16;
 constexpr int EXACT_MAX_SPLIT = 512;   // particles that may be split (ticket and partial slots)
-template <bool JERK>
+enum : int { EX_ACC = 0, EX_ACC_JERK = 1, EX_VJP = 2 };
+template <int MODE>
 __global__ void __launch_bounds__(EXACT_THREADS) ds32_exact(PairArgs a, const float4 *jd, const int *count,
                                                              const int *list, double *partial, int *ticket) {
-    constexpr int NO = JERK ? 6 : 3;
+    constexpr bool JERK = MODE == EX_ACC_JERK, VJP = MODE == EX_VJP, UVEC = JERK || VJP;
+    constexpr int NO = JERK ? 6 : (VJP ? 4 : 3);
     __shared__ DS red[NO][EXACT_THREADS];
-    __shared__ DS s_i[7];   // the i-particle: x, y, z, e2, vx, vy, vz
+    __shared__ DS s_i[8];   // the i-particle: x, y, z, e2, u (v or g) x, y, z, m
     const long long F = list ? (long long)*count : (long long)a.ni;
     if (F == 0) return;
     const int G = gridDim.x, tid = threadIdx.x;
@@ -1600,16 +1605,18 @@ __global__ void __launch_bounds__(EXACT_THREADS) ds32_exact(PairArgs a, const fl
         const size_t i = list ? (size_t)list[f] : (size_t)f;
         const size_t j0 = nj * ch / nch, j1 = nj * (ch + 1) / nch;
         // the i-particle's double-single values, converted once per CTA
-        if (tid < (JERK ? 7 : 4)) {
-            const int fld = tid < 3 ? F_RX + tid : (tid == 3 ? F_E2 : F_VX + tid - 4);
-            s_i[tid] = ds_from(a.I.f[fld][i]);
+        if (tid < 8) {
+            const int ufld = VJP ? F_AX : F_VX;
+            const int fld = tid < 3 ? F_RX + tid : (tid == 3 ? F_E2 : (tid < 7 ? ufld + tid - 4 : F_M));
+            if (tid < 4 || UVEC) s_i[tid] = ds_from(a.I.f[fld][i]);
         }
         __syncthreads();
         // two j per packed step: lane .x takes j, lane .y j + EXACT_THREADS
-        DS2 xi[3], vi[3];
+        DS2 xi[3], vi[3], mi;
         for (int c = 0; c < 3; ++c) xi[c] = DS2{f2(s_i[c].hi), f2(s_i[c].lo)};
-        if (JERK)
+        if (UVEC)
             for (int c = 0; c < 3; ++c) vi[c] = DS2{f2(s_i[4 + c].hi), f2(s_i[4 + c].lo)};
+        if (VJP) mi = DS2{f2(s_i[7].hi), f2(s_i[7].lo)};
         const DS2 ie2{f2(s_i[3].hi), f2(s_i[3].lo)};
         DS2 acc2[NO];
         for (int c = 0; c < NO; ++c) acc2[c] = DS2{f2(0.f), f2(0.f)};
@@ -1634,7 +1641,28 @@ __global__ void __launch_bounds__(EXACT_THREADS) ds32_exact(PairArgs a, const fl
             if (!(r2.hi.x > 0.f)) { y.hi.x = 0.f; y.lo.x = 0.f; }
             if (!(r2.hi.y > 0.f)) { y.hi.y = 0.f; y.lo.y = 0.f; }
             const DS2 y2 = ds2_mul(y, y);
-            const DS2 mr3 = ds2_mul(DS2{make_float2(B0.z, B1.z), make_float2(B0.w, B1.w)}, ds2_mul(y2, y));
+            const DS2 mj{make_float2(B0.z, B1.z), make_float2(B0.w, B1.w)};
+            if (VJP) {
+                // w = m_i g_j - m_j g_i; r-bar += q3 w - 3 q3 q2 (r.w) r;
+                // m-bar += (g_j . r) q3  (q2 = y^2, q3 = y^3)
+                const float4 D0 = __ldg(jd + EXACT_JQ * p + 3);
+                const float4 D1 = has1 ? __ldg(jd + EXACT_JQ * p1 + 3) : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float gzh1 = has1 ? C1.z : 0.f, gzl1 = has1 ? C1.w : 0.f;
+                const DS2 gj[3] = {DS2{make_float2(D0.x, D1.x), make_float2(D0.y, D1.y)},
+                                   DS2{make_float2(D0.z, D1.z), make_float2(D0.w, D1.w)},
+                                   DS2{make_float2(C0.z, gzh1), make_float2(C0.w, gzl1)}};
+                const DS2 q3 = ds2_mul(y2, y);
+                DS2 w[3];
+                for (int c = 0; c < 3; ++c) w[c] = ds2_add(ds2_mul(mi, gj[c]), ds2_neg(ds2_mul(mj, vi[c])));
+                const DS2 rw = ds2_add(ds2_add(ds2_mul(d[0], w[0]), ds2_mul(d[1], w[1])), ds2_mul(d[2], w[2]));
+                const DS2 cc = ds2_mul(DS2{f2(3.0f), f2(0.0f)}, ds2_mul(ds2_mul(q3, y2), rw));
+                for (int c = 0; c < 3; ++c)
+                    acc2[c] = ds2_add(acc2[c], ds2_add(ds2_mul(q3, w[c]), ds2_neg(ds2_mul(cc, d[c]))));
+                const DS2 gr = ds2_add(ds2_add(ds2_mul(gj[0], d[0]), ds2_mul(gj[1], d[1])), ds2_mul(gj[2], d[2]));
+                acc2[3] = ds2_add(acc2[3], ds2_mul(gr, q3));
+                continue;
+            }
+            const DS2 mr3 = ds2_mul(mj, ds2_mul(y2, y));
             for (int c = 0; c < 3; ++c) acc2[c] = ds2_add(acc2[c], ds2_neg(ds2_mul(mr3, d[c])));
             if (JERK) {
                 const float4 D0 = __ldg(jd + EXACT_JQ * p + 3);
@@ -1684,9 +1712,9 @@ __global__ void __launch_bounds__(EXACT_THREADS) ds32_exact(PairArgs a, const fl
 }
 
 // j-data of ds32_exact in the caller's order, and zeroed chunk tickets.
-__global__ void ds32_exact_prepare(PSet J, size_t nj, bool vel, float4 *jd, int *ticket, int nticket) {
+__global__ void ds32_exact_prepare(PSet J, size_t nj, int ufield, float4 *jd, int *ticket, int nticket) {
     const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < nj) write_exact_record(jd + EXACT_JQ * j, J, j, vel);
+    if (j < nj) write_exact_record(jd + EXACT_JQ * j, J, j, ufield);
     if (j < (size_t)nticket) ticket[j] = 0;
 }
 
@@ -2153,7 +2181,7 @@ static size_t exact_ws_bytes(size_t nj) {
     return align_up(nj * EXACT_JQ * sizeof(float4), 256) +
            align_up((size_t)EXACT_MAX_SPLIT * (EXACT_MAX_CHUNKS * 6 * sizeof(double) + sizeof(int)), 256);
 }
-template <bool JERK>
+template <int MODE>
 static cudaError_t run_exact(const PairArgs &p, void *ws, size_t ws_bytes, int sms, cudaStream_t s) {
     if (exact_ws_bytes(p.nj) > ws_bytes) return cudaErrorInvalidValue;
     char *q = static_cast<char *>(ws);
@@ -2161,8 +2189,9 @@ static cudaError_t run_exact(const PairArgs &p, void *ws, size_t ws_bytes, int s
     double *part = reinterpret_cast<double *>(q);
     int *ticket = reinterpret_cast<int *>(part + (size_t)EXACT_MAX_SPLIT * EXACT_MAX_CHUNKS * 6);
     const size_t n = p.nj > (size_t)EXACT_MAX_SPLIT ? p.nj : (size_t)EXACT_MAX_SPLIT;
-    ds32_exact_prepare<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.J, p.nj, JERK, jd, ticket, EXACT_MAX_SPLIT);
-    ds32_exact<JERK><<<(unsigned)(sms * 4), EXACT_THREADS, 0, s>>>(p, jd, nullptr, nullptr, part, ticket);
+    const int ufield = MODE == EX_ACC_JERK ? F_VX : (MODE == EX_VJP ? F_AX : -1);
+    ds32_exact_prepare<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(p.J, p.nj, ufield, jd, ticket, EXACT_MAX_SPLIT);
+    ds32_exact<MODE><<<(unsigned)(sms * 4), EXACT_THREADS, 0, s>>>(p, jd, nullptr, nullptr, part, ticket);
     return cudaGetLastError();
 }
 
@@ -2277,7 +2306,7 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
         std::lock_guard<std::mutex> lk(g_prof_mu);
         g_prof_rec.push_back(pr);
     }
-    ds32_exact<false><<<(unsigned)(sms * 4), EXACT_THREADS, 0, s>>>(p, jd, flags, flags + 64, ref_part, ref_ticket);
+    ds32_exact<EX_ACC><<<(unsigned)(sms * 4), EXACT_THREADS, 0, s>>>(p, jd, flags, flags + 64, ref_part, ref_ticket);
     return cudaGetLastError();
 }
 
@@ -2392,7 +2421,7 @@ size_t ds32_workspace_bytes(int kernel, size_t ni, size_t nj, int sms) {
         case K_SNAP_CRACKLE: return ws_bytes_for<SnapCrackleDS<1, REF>>(ni, nj, sms);
         case K_TSTEP: return ws_pick<TstepDS<IPT2, REF>, TstepDS<1, REF>>(ni, nj, sms);
         case K_PNACC: return ws_bytes_for<PNAccDS<1, REF>>(ni, nj, sms);
-        case K_ACC_VJP: return ws_bytes_for<AccVjpDS<IPT2, REF>>(ni, nj, sms);
+        case K_ACC_VJP: return exact_ws_bytes(nj);
         default: return 0;
     }
 }
@@ -2402,14 +2431,14 @@ cudaError_t launch_ds32(int kernel, const PairArgs &a, void *ws, size_t ws_bytes
         case K_PHI: return run_pick<PhiDS<IPT2, REF>, PhiDS<1, REF>>(a, ws, ws_bytes, sms, s);
         case K_ACC:
             if (ord_applies(a.ni, a.nj)) return run_ord<AccOrd<2>>(a, 5, ws, ws_bytes, sms, s);
-            return run_exact<false>(a, ws, ws_bytes, sms, s);
+            return run_exact<EX_ACC>(a, ws, ws_bytes, sms, s);
         case K_ACC_JERK:
             if (ord_applies(a.ni, a.nj)) return run_ord<AccJerkOrd<2>>(a, 8, ws, ws_bytes, sms, s);
-            return run_exact<true>(a, ws, ws_bytes, sms, s);
+            return run_exact<EX_ACC_JERK>(a, ws, ws_bytes, sms, s);
         case K_SNAP_CRACKLE: return run_ds<SnapCrackleDS<1, REF>>(a, ws, ws_bytes, sms, s);
         case K_TSTEP: return run_pick<TstepDS<IPT2, REF>, TstepDS<1, REF>>(a, ws, ws_bytes, sms, s);
         case K_PNACC: return run_ds<PNAccDS<1, REF>>(a, ws, ws_bytes, sms, s);
-        case K_ACC_VJP: return run_ds<AccVjpDS<IPT2, REF>>(a, ws, ws_bytes, sms, s);
+        case K_ACC_VJP: return run_exact<EX_VJP>(a, ws, ws_bytes, sms, s);
         default: return cudaErrorInvalidValue;
     }
 }
