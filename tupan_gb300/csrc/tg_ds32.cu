@@ -1,5 +1,15 @@
 // tg_ds32.cu -- split-FP32 ("double-single") pairwise kernels.
 //
+// Three families:
+//   * the unordered stream-K kernels below (Phi, SnapCrackle, Tstep, PNAcc;
+//     Acc and AccJerk of the segmented ensembles and of the no-allocation
+//     entry point);
+//   * the ordered Acc and AccJerk (ds32_ord, calls of 2^24 pairs and more):
+//     spatially sorted sets, single-float separations on far blocks,
+//     cost-weighted stream-K, recompute of strongly cancelling particles;
+//   * the double-single kernel ds32_exact: Acc and AccJerk below 2^24 pairs,
+//     the Acc adjoint, and that recompute.
+//
 // Data layout in HBM (workspace, written by ds32_prepare once per call):
 //   the j-set as pair-interleaved float records.  Record p holds j = 2p and
 //   j = 2p+1; field f occupies floats [2f, 2f+1] of the record, so one
@@ -76,10 +86,6 @@ struct DsArgs {
     int *ticket;         // [NIT]
     const float *tile_e2;  // [NJT] common j softening per tile or NaN; may be null
     long long nit, njt;  // i-tiles, j-tiles
-    // When set, the kernel runs only if *mode == run_mode (the unmasked and
-    // masked forms of a kernel are both launched; a pre-pass picks one).
-    const int *mode;
-    int run_mode;
 };
 
 __device__ __forceinline__ float fzero_norm(float x) { return x + 0.0f; }  // -0 -> +0
@@ -129,13 +135,11 @@ __global__ void ds32_pack(PSet J, size_t nj, size_t npairs, PackSpec ps, float *
 // Fused per-call preparation, one CTA of DS_TILE threads per j-tile, one j
 // per thread: the tile's records (as ds32_pack), its softening flag
 // (tile_e2[t]: the common float e2 of its valid particles or NaN; skipped if
-// tile_e2 is null), and, grid-stride, the zeroed stream-K tickets, the
-// cleared coincidence table (-1) and flags.  Every thread issues its loads
-// at once, so the launch costs about one memory round trip.
+// tile_e2 is null), and, grid-stride, the zeroed stream-K tickets.  Every
+// thread issues its loads at once, so the launch costs about one memory
+// round trip.
 struct PrepArgs {
     int *ticket; long long nticket;
-    int *table; size_t ntable;
-    int *flags; int nflags;
 };
 __global__ void __launch_bounds__(DS_TILE) ds32_prepare(PSet J, size_t nj, PackSpec ps, float *rec, float *tile_e2,
                                                         PrepArgs z) {
@@ -175,8 +179,6 @@ __global__ void __launch_bounds__(DS_TILE) ds32_prepare(PSet J, size_t nj, PackS
     }
     const size_t g = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
     for (size_t x = g; x < (size_t)z.nticket; x += stride) z.ticket[x] = 0;
-    for (size_t x = g; x < z.ntable; x += stride) z.table[x] = -1;
-    for (size_t x = g; x < (size_t)z.nflags; x += stride) z.flags[x] = 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -315,19 +317,13 @@ struct PhiDS {
     static PackSpec pack() { return PackSpec{8, 2, {F_M, F_E2}}; }
 };
 
-// NOMASK: the pair r = 0 needs no mask because the call has been checked to
-// have every pair softening above 1e-20 and no two distinct coincident
-// particles (ds32_nomask_check): a self pair then has dr = dv = +0 and adds
-// exactly nothing, as the mask would make it.
-template <int IPT_, bool REFINE, bool NOMASK = false>
+// The unordered split-FP32 AccJerk (ensembles and the no-allocation entry
+// point).  Compensated sums stay in registers (shared-memory sums measured
+// 0.3% slower); eight records per unrolled block (0.8% faster than four).
+template <int IPT_, bool REFINE>
 struct AccJerkDS {
     static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 6;
-    using NomaskTwin = typename std::conditional<NOMASK, void, AccJerkDS<IPT_, REFINE, true>>::type;
-    // The hoisted-softening form pays only without the mask (masked:
-    // 4.67 vs 4.57 ms, unmasked: 4.28 vs 4.37 ms at N = 65536, measured).
-    // Compensated sums stay in registers (shared-memory sums measured 0.3%
-    // slower); eight records per unrolled block (0.8% faster than four).
-    static constexpr bool UE2 = NOMASK;
+    static constexpr bool UE2 = false;
     static constexpr int UNROLL = 8;
     struct IS { IPos q; float2 u, v, w, e; float2 a[6]; Comp c[6]; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {
@@ -355,10 +351,7 @@ struct AccJerkDS {
             const float2 e2 = UE ? E : add2(s.e, lo2(q5));
             const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
             float2 y, y2;
-            if (NOMASK) {
-                y = make_float2(rsqrt_hw(ss.x), rsqrt_hw(ss.y));
-                y2 = make_float2(rcp_hw(ss.x), rcp_hw(ss.y));
-            } else if (REFINE) {
+            if (REFINE) {
                 y = inv_r<true>(ss, dx, dy, dz);
                 y2 = mul2(y, y);
             } else {
@@ -582,55 +575,6 @@ struct PNAccDS {
     static PackSpec pack() { return PackSpec{12, 6, {F_VX, F_VY, F_VZ, F_M, F_E2, -2}}; }
 };
 
-// Vector-Jacobian product of Acc (see AccVjp64 in tg_fp64.cu for the
-// formulas); the upstream gradient g travels in the acceleration slots.
-template <int IPT_, bool REFINE>
-struct AccVjpDS {
-    static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 4;
-    static constexpr bool UE2 = false;
-    struct IS { IPos q; float2 e, m, g[3]; float2 o[4]; Comp c[4]; };
-    __device__ static void load(IS &s, const PairArgs &a, size_t i) {
-        load_pos(a, i, s.q);
-        s.e = f2(__double2float_rn(a.I.f[F_E2][i]));
-        s.m = f2(__double2float_rn(a.I.f[F_M][i]));
-        for (int k = 0; k < 3; ++k) s.g[k] = f2(__double2float_rn(a.I.f[F_AX + k][i]));
-        for (int k = 0; k < 4; ++k) { s.o[k] = f2(0.f); s.c[k] = Comp{0.f, 0.f}; }
-    }
-    // record: {xh,yh} {zh,xl} {yl,zl} {m,e2} {gx,gy} {gz,pad}
-    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R) {
-        const float4 q0 = R[0], q1 = R[1], q2 = R[2], q3 = R[3], q4 = R[4], q5 = R[5];
-#pragma unroll
-        for (int u = 0; u < IPT; ++u) {
-            IS &s = S[u];
-            float2 r[3];
-            pair_dr(s.q, lo2(q0), hi2(q0), lo2(q1), hi2(q1), lo2(q2), hi2(q2), r[0], r[1], r[2]);
-            const float2 e2 = add2(s.e, hi2(q3));
-            const float2 ss = fma2(r[0], r[0], fma2(r[1], r[1], fma2(r[2], r[2], e2)));
-            float2 y, y2;
-            inv_r_r2(ss, r[0], r[1], r[2], y, y2);
-            const float2 y3 = mul2(y, y2);
-            const float2 mj = lo2(q3);
-            const float2 gj[3] = {lo2(q4), hi2(q4), lo2(q5)};
-            float2 w[3];
-            for (int k = 0; k < 3; ++k) w[k] = fnma2(mj, s.g[k], mul2(s.m, gj[k]));
-            const float2 rw = fma2(r[0], w[0], fma2(r[1], w[1], mul2(r[2], w[2])));
-            const float2 c = mul2(mul2(mul2(y3, y2), f2(3.0f)), rw);
-            for (int k = 0; k < 3; ++k) s.o[k] = fnma2(c, r[k], fma2(y3, w[k], s.o[k]));
-            const float2 gr = fma2(gj[0], r[0], fma2(gj[1], r[1], mul2(gj[2], r[2])));
-            s.o[3] = fma2(gr, y3, s.o[3]);
-        }
-    }
-    __device__ static void fold(IS &s) {
-        for (int k = 0; k < 4; ++k) { comp_add(s.c[k], __fadd_rn(s.o[k].x, s.o[k].y)); s.o[k] = f2(0.f); }
-    }
-    __device__ static void partials(const IS &s, double *p) { for (int k = 0; k < 4; ++k) p[k] = comp_value(s.c[k]); }
-    __device__ static void combine(double *acc, const double *p) { for (int k = 0; k < 4; ++k) acc[k] += p[k]; }
-    __device__ static void store(const double *p, const PairArgs &a, size_t i) {
-        for (int k = 0; k < 4; ++k) a.out[k][i] = p[k];
-    }
-    static PackSpec pack() { return PackSpec{12, 6, {F_M, F_E2, F_AX, F_AY, F_AZ, -2}}; }
-};
-
 // One packed step of kernel K over a j-record; UE selects the uniform-
 // softening form for kernels that have it (E = the tile's common ie2 + je2).
 template <class K, bool UE>
@@ -638,12 +582,6 @@ __device__ __forceinline__ void kstep(typename K::IS (&st)[K::IPT], const float4
     if constexpr (K::UE2) K::template step<UE>(st, R, E);
     else K::step(st, R);
 }
-
-// Kernels with an unmasked twin (the masked form sets NOMASK_TWIN to it).
-template <class K, class = void>
-struct nomask_twin { using type = void; };
-template <class K>
-struct nomask_twin<K, std::void_t<typename K::NomaskTwin>> { using type = typename K::NomaskTwin; };
 
 // j-records per unrolled block: K::UNROLL if the kernel sets it, else
 // TG_DS32_UNROLL.
@@ -653,62 +591,6 @@ template <class K>
 struct kunroll<K, decltype(void(K::UNROLL))> : std::integral_constant<int, K::UNROLL> {};
 
 
-
-// ---------------------------------------------------------------------------
-// Pre-pass for the unmasked forms: *bad becomes nonzero if some particle has
-// float softening <= 6e-21 (a pair sum could fall below 1e-20) or a
-// non-finite position, or if two distinct particles of I x J coincide.
-// Coincidences are found with an open-addressing hash table of j indices
-// keyed on the positions (-0 folded to +0); "distinct" compares addresses, so
-// a particle that is in both sets (I and J overlapping arrays) is itself.
-// Probing is bounded by the table size.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ unsigned long long mix64(unsigned long long h) {
-    h ^= h >> 33; h *= 0xff51afd7ed558ccdULL;
-    h ^= h >> 33; h *= 0xc4ceb9fe1a85ec53ULL;
-    h ^= h >> 33;
-    return h;
-}
-__device__ __forceinline__ unsigned long long pos_key(double x, double y, double z) {
-    unsigned long long h = mix64((unsigned long long)__double_as_longlong(x + 0.0));
-    h = mix64(h ^ (unsigned long long)__double_as_longlong(y + 0.0));
-    return mix64(h ^ (unsigned long long)__double_as_longlong(z + 0.0));
-}
-__device__ __forceinline__ bool check_particle(const PSet &S, size_t k) {
-    const double x = S.f[F_RX][k], y = S.f[F_RY][k], z = S.f[F_RZ][k];
-    const bool finite = isfinite(x) && isfinite(y) && isfinite(z);
-    return finite && __double2float_rn(S.f[F_E2][k]) > 6e-21f;
-}
-__device__ __forceinline__ bool same_pos(const PSet &A, size_t a, const PSet &B, size_t b) {
-    return A.f[F_RX][a] == B.f[F_RX][b] && A.f[F_RY][a] == B.f[F_RY][b] && A.f[F_RZ][a] == B.f[F_RZ][b];
-}
-__global__ void ds32_nomask_insert(PSet J, size_t nj, int *table, unsigned long long tmask, int *bad) {
-    const size_t j = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= nj) return;
-    if (!check_particle(J, j)) { atomicOr(bad, 1); return; }
-    unsigned long long slot = pos_key(J.f[F_RX][j], J.f[F_RY][j], J.f[F_RZ][j]) & tmask;
-    for (unsigned long long probe = 0; probe <= tmask; ++probe) {
-        const int prev = atomicCAS(table + slot, -1, (int)j);
-        if (prev == -1) return;
-        if (same_pos(J, j, J, (size_t)prev)) { atomicOr(bad, 2); return; }   // coincident j's
-        slot = (slot + 1) & tmask;
-    }
-    atomicOr(bad, 4);   // table full: cannot happen at load factor 1/2
-}
-__global__ void ds32_nomask_lookup(PSet I, size_t ni, PSet J, const int *table, unsigned long long tmask, int *bad) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ni) return;
-    if (!check_particle(I, i)) { atomicOr(bad, 1); return; }
-    unsigned long long slot = pos_key(I.f[F_RX][i], I.f[F_RY][i], I.f[F_RZ][i]) & tmask;
-    for (unsigned long long probe = 0; probe <= tmask; ++probe) {
-        const int j = table[slot];
-        if (j < 0) return;
-        if (same_pos(I, i, J, (size_t)j) && (I.f[F_RX] + i) != (J.f[F_RX] + j)) { atomicOr(bad, 2); return; }
-        slot = (slot + 1) & tmask;
-    }
-}
-// mode = 1 (unmasked) if the check passed, else 0 (masked)
-__global__ void ds32_nomask_mode(const int *bad, int *mode) { *mode = (*bad == 0) ? 1 : 0; }
 
 // ---------------------------------------------------------------------------
 // Stream-K geometry helpers.
@@ -850,7 +732,6 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
     const long long k = blockIdx.x;
     const long long u0 = unit_start(k, U, G), u1 = unit_start(k + 1, U, G);
     if (u0 >= u1) return;
-    if (a.mode && *a.mode != a.run_mode) return;
     const int tid = threadIdx.x;
 
     if (tid == 0) {
@@ -1955,7 +1836,6 @@ struct Geometry {
     long long nit, njt, units, grid;
     int jsub;
     size_t rec_bytes, part_bytes, ticket_bytes, tile_bytes;
-    size_t nomask_len, nomask_bytes;   // coincidence-check table (ints) for the unmasked twin
 };
 
 // Resident CTAs per SM of kernel K (computed once; concurrent first calls
@@ -2031,29 +1911,19 @@ static Geometry geometry(size_t ni, size_t nj, int sms) {
     g.part_bytes = align_up((size_t)g.grid * 2 * K::IPT * K::NP * DS_THREADS * sizeof(double), 256);
     g.ticket_bytes = align_up((size_t)g.nit * sizeof(int), 256);
     g.tile_bytes = K::UE2 ? align_up((size_t)g.njt * sizeof(float), 256) : 0;
-    g.nomask_len = 0;
-    // the pre-pass costs ~50 us (hash insert + lookup): worth it from 2^30 pairs
-    if (!std::is_void<typename nomask_twin<K>::type>::value && (double)ni * (double)nj >= 1073741824.0 &&
-        nj <= ((size_t)1 << 26)) {
-        size_t t = 1;
-        while (t < 2 * nj) t *= 2;
-        g.nomask_len = t;
-    }
-    g.nomask_bytes = g.nomask_len ? align_up(g.nomask_len * sizeof(int), 256) + 256 : 0;
     return g;
 }
 
 template <class K>
 static size_t ws_bytes_for(size_t ni, size_t nj, int sms) {
     const Geometry g = geometry<K>(ni, nj, sms);
-    return g.rec_bytes + g.part_bytes + g.ticket_bytes + g.tile_bytes + g.nomask_bytes;
+    return g.rec_bytes + g.part_bytes + g.ticket_bytes + g.tile_bytes;
 }
 
 template <class K>
 static cudaError_t run_ds(const PairArgs &p, void *ws, size_t ws_bytes, int sms, cudaStream_t s) {
     const Geometry g = geometry<K>(p.ni, p.nj, sms);
-    if (g.rec_bytes + g.part_bytes + g.ticket_bytes + g.tile_bytes + g.nomask_bytes > ws_bytes)
-        return cudaErrorInvalidValue;
+    if (g.rec_bytes + g.part_bytes + g.ticket_bytes + g.tile_bytes > ws_bytes) return cudaErrorInvalidValue;
     char *base = static_cast<char *>(ws);
     DsArgs a;
     a.p = p;
@@ -2064,39 +1934,10 @@ static cudaError_t run_ds(const PairArgs &p, void *ws, size_t ws_bytes, int sms,
     a.tile_e2 = K::UE2 ? tile_e2 : nullptr;
     a.nit = g.nit;
     a.njt = g.njt;
-    a.mode = nullptr;
-    a.run_mode = 0;
-
     const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
-    using Twin = typename nomask_twin<K>::type;
-    char *nb = base + g.rec_bytes + g.part_bytes + g.ticket_bytes + g.tile_bytes;
-    int *table = reinterpret_cast<int *>(nb);
-    int *flags = g.nomask_len ? reinterpret_cast<int *>(nb + g.nomask_bytes - 256) : nullptr;   // bad, mode
-    PrepArgs z{a.ticket, g.nit, table, g.nomask_len, flags, g.nomask_len ? 2 : 0};
+    PrepArgs z{a.ticket, g.nit};
     ds32_prepare<<<(unsigned)g.njt, DS_TILE, 0, s>>>(p.J, p.nj, K::pack(), reinterpret_cast<float *>(base),
                                                  K::UE2 ? tile_e2 : nullptr, z);
-    if constexpr (!std::is_void<Twin>::value) {
-        if (g.nomask_len) {
-            // pre-pass, then both forms; each runs only if the mode matches
-            const unsigned long long tmask = g.nomask_len - 1;
-            ds32_nomask_insert<<<(unsigned)((p.nj + 255) / 256), 256, 0, s>>>(p.J, p.nj, table, tmask, flags);
-            ds32_nomask_lookup<<<(unsigned)((p.ni + 255) / 256), 256, 0, s>>>(p.I, p.ni, p.J, table, tmask, flags);
-            ds32_nomask_mode<<<1, 1, 0, s>>>(flags, flags + 1);
-            a.mode = flags + 1;
-            DsArgs b = a;
-            b.run_mode = 1;
-            a.run_mode = 0;
-            ctas_per_sm<Twin>();   // raises the twin's shared-memory limit (once)
-            if (g.jsub == 2) {
-                ds32_streamk<K, 2><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
-                ds32_streamk<Twin, 2><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(b);
-            } else {
-                ds32_streamk<K, 1><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
-                ds32_streamk<Twin, 1><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(b);
-            }
-            return cudaGetLastError();
-        }
-    }
     if (g.jsub == 2) ds32_streamk<K, 2><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
     else ds32_streamk<K, 1><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
     return cudaGetLastError();
@@ -2127,8 +1968,6 @@ static cudaError_t run_ds_capped(const PairArgs &p, void *ws, size_t ws_bytes, i
     a.tile_e2 = nullptr;   // general path only: the scratch layout stays fixed
     a.nit = g.nit;
     a.njt = g.njt;
-    a.mode = nullptr;
-    a.run_mode = 0;
 
     const size_t npairs = (size_t)g.njt * DS_PAIRS;
     const PackSpec spec = K::pack();
@@ -2287,8 +2126,6 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
     a.d.tile_e2 = tile_e2;
     a.d.nit = g.nit;
     a.d.njt = g.njt;
-    a.d.mode = nullptr;
-    a.d.run_mode = 0;
     a.pi = o.pi;
     a.blk = blk;
     a.form = form;
