@@ -852,8 +852,8 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
 // ===========================================================================
 // Ordered split-FP32 Acc and AccJerk (single-set calls of >= 2^24 pairs).
 //
-// Per call, tg_order.cu sorts the j-set (light particles in Morton order,
-// then the heavy ones, mass > max(m) / 32) and the i-set (Morton order), and
+// Per call, tg_order.cu sorts the j-set (light particles in Hilbert order,
+// then the heavy ones, mass > max(m) / 32) and the i-set (Hilbert order), and
 // ds32_ord_prepare writes the j-records in that order with positions
 // relative to the centre c_b of their 64-j block.  The pairwise kernel then
 // decides per 64-j block, from the block's and the i-tile's bounding boxes:

@@ -93,7 +93,7 @@ cudaError_t launch_fp64_seg(int kernel, const PairArgs &a, long long C, long lon
 
 // Spatial ordering of the particle sets for the ordered split-FP32 Acc and
 // AccJerk (tg_order.cu).  pj: sorted j position -> j index (light particles
-// in Morton order, then the heavy ones); pi: the same for the i-set (pj
+// in Hilbert order, then the heavy ones); pi: the same for the i-set (pj
 // itself when `same`); *nlight: number of light j (device).
 struct OrderOut {
     const int *pi, *pj;
