@@ -1455,14 +1455,15 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs o
 // AccVjp64).  It serves as the recompute of the particles the ordered kernels
 // flag (acceleration only), as the whole split-FP32 Acc and AccJerk of calls
 // below 2^24 pairs, and as the split-FP32 adjoint.
-// With F particles and G CTAs each particle's j-range is cut into
-// nch = clamp(G / F, 1, EXACT_MAX_CHUNKS) chunks; a CTA reduces a chunk in
-// a fixed-order double-single tree, and with nch > 1 the last chunk of a particle to
-// finish (atomic ticket) adds the chunk sums in chunk order: the result is
-// deterministic.  Pairs with r2 > 0 false get 1/r = 0 as in the reference
+// One warp per work item: with F particles and GW warps in the grid each
+// particle's j-range is cut into nch = clamp(GW / F, 1, EXACT_MAX_CHUNKS)
+// chunks; a warp reduces its chunk by a double-single butterfly, and with
+// nch > 1 the last chunk of a particle to finish (atomic ticket) adds the
+// chunk sums in chunk order: the result is deterministic.  Pairs with r2 > 0 false get 1/r = 0 as in the reference
 // (acc_kernel_common.h, acc_jerk_kernel_common.h; smoothing.h), so a NaN
 // separation still reaches the sums as it does there.
-constexpr int EXACT_THREADS = 256;
+constexpr int EXACT_THREADS = 256;                 // 8 warps per CTA
+constexpr int EXACT_WARPS = EXACT_THREADS / 32;
 constexpr int EXACT_MAX_CHUNKS = 16;
 constexpr int EXACT_MAX_SPLIT = 512;   // particles that may be split (ticket and partial slots)
 enum : int { EX_ACC = 0, EX_ACC_JERK = 1, EX_VJP = 2 };
@@ -1471,28 +1472,31 @@ __global__ void __launch_bounds__(EXACT_THREADS) ds32_exact(PairArgs a, const fl
                                                              const int *list, double *partial, int *ticket) {
     constexpr bool JERK = MODE == EX_ACC_JERK, VJP = MODE == EX_VJP, UVEC = JERK || VJP;
     constexpr int NO = JERK ? 6 : (VJP ? 4 : 3);
-    __shared__ DS red[NO][EXACT_THREADS];
-    __shared__ DS s_i[8];   // the i-particle: x, y, z, e2, u (v or g) x, y, z, m
     const long long F = list ? (long long)*count : (long long)a.ni;
     if (F == 0) return;
-    const int G = gridDim.x, tid = threadIdx.x;
-    long long nch = G / F;
+    const int lane = threadIdx.x & 31;
+    const long long GW = (long long)gridDim.x * EXACT_WARPS;
+    long long nch = GW / F;
     nch = nch < 1 ? 1 : (nch > EXACT_MAX_CHUNKS ? EXACT_MAX_CHUNKS : nch);
     if (F > EXACT_MAX_SPLIT) nch = 1;
     const long long W = F * nch;
     const size_t nj = a.nj;
-    for (long long w = blockIdx.x; w < W; w += G) {
+    for (long long w = (long long)blockIdx.x * EXACT_WARPS + (threadIdx.x >> 5); w < W; w += GW) {
         const long long f = w / nch, ch = w % nch;
         const size_t i = list ? (size_t)list[f] : (size_t)f;
         const size_t j0 = nj * ch / nch, j1 = nj * (ch + 1) / nch;
-        // the i-particle's double-single values, converted once per CTA
-        if (tid < 8) {
+        // the i-particle's double-single values: lane q converts field q
+        // (x, y, z, e2, u (v or g) x, y, z, m), then every lane takes them
+        DS own{0.f, 0.f};
+        if (lane < 8) {
             const int ufld = VJP ? F_AX : F_VX;
-            const int fld = tid < 3 ? F_RX + tid : (tid == 3 ? F_E2 : (tid < 7 ? ufld + tid - 4 : F_M));
-            if (tid < 4 || UVEC) s_i[tid] = ds_from(a.I.f[fld][i]);
+            const int fld = lane < 3 ? F_RX + lane : (lane == 3 ? F_E2 : (lane < 7 ? ufld + lane - 4 : F_M));
+            if (lane < 4 || UVEC) own = ds_from(a.I.f[fld][i]);
         }
-        __syncthreads();
-        // two j per packed step: lane .x takes j, lane .y j + EXACT_THREADS
+        DS s_i[8];
+        for (int q = 0; q < 8; ++q)
+            s_i[q] = DS{__shfl_sync(0xffffffffu, own.hi, q), __shfl_sync(0xffffffffu, own.lo, q)};
+        // two j per packed step: lane .x takes j, lane .y j + 32
         DS2 xi[3], vi[3], mi;
         for (int c = 0; c < 3; ++c) xi[c] = DS2{f2(s_i[c].hi), f2(s_i[c].lo)};
         if (UVEC)
@@ -1501,8 +1505,8 @@ __global__ void __launch_bounds__(EXACT_THREADS) ds32_exact(PairArgs a, const fl
         const DS2 ie2{f2(s_i[3].hi), f2(s_i[3].lo)};
         DS2 acc2[NO];
         for (int c = 0; c < NO; ++c) acc2[c] = DS2{f2(0.f), f2(0.f)};
-        for (size_t p = j0 + tid; p < j1; p += 2 * EXACT_THREADS) {
-            const size_t p1 = p + EXACT_THREADS;
+        for (size_t p = j0 + lane; p < j1; p += 64) {
+            const size_t p1 = p + 32;
             const bool has1 = p1 < j1;
             const float4 A0 = __ldg(jd + EXACT_JQ * p), B0 = __ldg(jd + EXACT_JQ * p + 1),
                          C0 = __ldg(jd + EXACT_JQ * p + 2);
@@ -1565,19 +1569,18 @@ __global__ void __launch_bounds__(EXACT_THREADS) ds32_exact(PairArgs a, const fl
         DS acc[NO];
         for (int c = 0; c < NO; ++c)
             acc[c] = ds_add(DS{acc2[c].hi.x, acc2[c].lo.x}, DS{acc2[c].hi.y, acc2[c].lo.y});
-        for (int c = 0; c < NO; ++c) red[c][tid] = acc[c];
-        __syncthreads();
-        for (int h = EXACT_THREADS / 2; h > 0; h >>= 1) {
-            if (tid < h)
-                for (int c = 0; c < NO; ++c) red[c][tid] = ds_add(red[c][tid], red[c][tid + h]);
-            __syncthreads();
-        }
+        // butterfly over the warp (ds_add is commutative: every lane ends
+        // with the same, deterministic value)
+        for (int o = 16; o > 0; o >>= 1)
+            for (int c = 0; c < NO; ++c)
+                acc[c] = ds_add(acc[c], DS{__shfl_xor_sync(0xffffffffu, acc[c].hi, o),
+                                           __shfl_xor_sync(0xffffffffu, acc[c].lo, o)});
         if (nch == 1) {
-            if (tid == 0)
-                for (int c = 0; c < NO; ++c) a.out[c][i] = ds_value(red[c][0]);
-        } else if (tid == 0) {
+            if (lane == 0)
+                for (int c = 0; c < NO; ++c) a.out[c][i] = ds_value(acc[c]);
+        } else if (lane == 0) {
             double *mine = partial + ((size_t)f * EXACT_MAX_CHUNKS + ch) * NO;
-            for (int c = 0; c < NO; ++c) mine[c] = ds_value(red[c][0]);
+            for (int c = 0; c < NO; ++c) mine[c] = ds_value(acc[c]);
             __threadfence();
             if (atomicAdd(ticket + f, 1) == (int)nch - 1) {
                 __threadfence();
@@ -1588,7 +1591,7 @@ __global__ void __launch_bounds__(EXACT_THREADS) ds32_exact(PairArgs a, const fl
                 for (int c = 0; c < NO; ++c) a.out[c][i] = v[c];
             }
         }
-        __syncthreads();
+        __syncwarp();
     }
 }
 
