@@ -58,7 +58,7 @@ FLOP_ACC = 20       # tupan/lib/src/acc_kernel_common.h:38
 FLOP_ACC_JERK = 42  # tupan/lib/src/acc_jerk_kernel_common.h:56
 # DRAM bytes (read + write) of one AccJerk pairwise-kernel launch on this
 # workload, from an ncu capture (profiles/ds32_ord_acc_jerk_n65536.txt)
-TRAFFIC_ACC_JERK_N65536 = 7.22e6
+TRAFFIC_ACC_JERK_N65536 = 7.35e6
 METRIC = "Gint/s Acc+AccJerk split-FP32 (N=65536 Plummer-Salpeter, eps2=1e-6)"
 # library kernels per ordered Acc or AccJerk call: spatial order (bounds,
 # keys, the radix sort's histogram, exclusive-sum and four one-sweep passes),

@@ -293,6 +293,50 @@ int tg_hermite_correct(int order, size_t n, double tau, const double *const *rv0
                        const double *const *deriv0, const double *const *deriv1, double *const *rv1,
                        void *stream);
 
+/* One step of the hierarchical SIA integrators (methods sia<NM>h.kdk and
+ * sia<NM>h.dkd; SIA.recurse, tupan/integrator/sia.py:1092-1123, with split,
+ * join, sf_kick and FewBody, sia.py:24-57, 175-230, fewbody.py:13-57),
+ * driven from native code: per time-step level one Tstep call, one stable
+ * slow/fast partition whose size is read back (the call waits for the
+ * stream there), the scheme's kicks, drifts and cross kicks, and Kepler
+ * pair solutions for two-particle subsets.  No counterpart in the
+ * reference's C library (its recursion is Python).
+ *   op_kind/op_coef: the scheme's symmetric operator sequence (nops <= 64;
+ *     kind 0 opens and closes it): for kdk kind 0 is a kick and kind 1 a
+ *     drift, for dkd the reverse; in the slow/fast bridge kind 0 advances
+ *     the slow part and recurses on the fast part, kind 1 is the cross kick.
+ *   prec_acc/prec_tstep: TG_PREC_* of the Acc and Tstep calls.
+ *   real: rows_real rows of n float64 values, ld_real apart; ints: rows_int
+ *     rows of n int64 values, ld_int apart; row_of[TG_SIA_ROW_*] gives each
+ *     attribute's row (NSTEP in ints, the others in real).  Every row is
+ *     permuted with the particles: on return the blocks hold the set after
+ *     the step in the reference's order (slow before fast at every level).
+ *   *t_curr: the integrator's current time, advanced as the reference's
+ *     recursion advances it.
+ * FP64 results are bit-identical to the same recursion over the Python
+ * extension calls.  Level buffers are library-owned and grow on demand;
+ * calls must not overlap in time. */
+#define TG_SIA_ROW_MASS 0
+#define TG_SIA_ROW_EPS2 1
+#define TG_SIA_ROW_RX 2
+#define TG_SIA_ROW_RY 3
+#define TG_SIA_ROW_RZ 4
+#define TG_SIA_ROW_VX 5
+#define TG_SIA_ROW_VY 6
+#define TG_SIA_ROW_VZ 7
+#define TG_SIA_ROW_TIME 8
+#define TG_SIA_ROW_TSTEP 9
+#define TG_SIA_ROW_TSTEPIJ 10
+#define TG_SIA_ROW_AX 11
+#define TG_SIA_ROW_AY 12
+#define TG_SIA_ROW_AZ 13
+#define TG_SIA_ROW_NSTEP 14
+#define TG_SIA_NROWS 15
+int tg_sia_h_step(int nops, const int *op_kind, const double *op_coef, int kdk, double eta, double tau,
+                  int prec_acc, int prec_tstep, size_t n, double *real, size_t ld_real, int rows_real,
+                  long long *ints, size_t ld_int, int rows_int, const int *row_of, double *t_curr,
+                  void *stream);
+
 /* No counterpart in the reference.  Split-FP32 AccJerk (the unordered
  * stream-K kernels that tg_acc_jerk with TG_PREC_DS32 runs for calls below
  * 2^24 pairs) for callers that cannot let a library allocate GPU memory --

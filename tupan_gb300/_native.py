@@ -106,6 +106,11 @@ def _load():
     lib.tg_sum.argtypes = [ctypes.c_size_t, _DP, _DP, _DP]
     lib.tg_kepler_solver.restype = ctypes.c_int
     lib.tg_kepler_solver.argtypes = [ctypes.c_size_t] + [_DP] * 8 + [ctypes.c_double] + [_DP] * 6 + [_DP]
+    lib.tg_sia_h_step.restype = ctypes.c_int
+    lib.tg_sia_h_step.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double),
+                                  ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_size_t, _DP, ctypes.c_size_t, ctypes.c_int, _DP, ctypes.c_size_t,
+                                  ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double), _DP]
     lib.kepler_solver_kernel.restype = None
     lib.kepler_solver_kernel.argtypes = [_DP] * 8 + [ctypes.c_double] + [_DP] * 6
     return lib

@@ -17,7 +17,7 @@ OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libtupan_gb300.so")
 SOURCES = ("tg_api.cu", "tg_fp64.cu", "tg_ds32.cu", "tg_order.cu", "tg_probe.cu", "tg_noalloc.cu",
-           "tg_integrate.cu")
+           "tg_integrate.cu", "tg_sia.cu")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -26,7 +26,17 @@ of the particle set (order preserved) and joining concatenates slow then
 fast, as the reference does, so the particle order after an h. step is the
 reference's.  Post-Newtonian SIA (sia.py:88-160) is not provided: the
 reference's PN bridge calls particle methods that do not exist.
+
+The h. modes run the recursion natively (tg_sia_h_step): on a small
+cluster a step is about a thousand levels of a few particles each, and a
+level driven from Python costs more than its arithmetic.  The native step
+makes the same kernel calls in the same order with the same arguments, so
+its FP64 trajectories equal this module's recursion bit for bit;
+`SIA.native_h = False` selects the Python recursion below.
 """
+import ctypes
+import warnings
+
 import torch
 
 from .. import _native
@@ -171,9 +181,17 @@ class Scheme(object):
         return slow, fast
 
 
+# attribute rows tg_sia_h_step reads and permutes, in TG_SIA_ROW_* order
+# (the last one, nstep, is in the int64 block)
+NATIVE_ROWS = ("mass", "eps2", "rx", "ry", "rz", "vx", "vy", "vz", "time", "tstep", "tstepij",
+               "ax", "ay", "az", "nstep")
+KEPLER_CAP = 2   # TG_ST_KEPLER_CAP
+
+
 class SIA(Base):
     PROVIDED_METHODS = tuple("%s%s.%s" % (s, m, f) for s in sorted(COEFS)
                              for m in ("s", "a", "h") for f in ("dkd", "kdk"))
+    native_h = True
 
     def __init__(self, eta, time, ps, method, **kwargs):
         if kwargs.get("pn_order", 0):
@@ -186,7 +204,11 @@ class SIA(Base):
         mode = method[5]
         self.update_tstep = mode in "ah"
         self.shared_tstep = mode in "sa"
-        self.evolve = self.scheme.kdk if method.endswith("kdk") else self.scheme.dkd
+        self.kdk = method.endswith("kdk")
+        self.evolve = self.scheme.kdk if self.kdk else self.scheme.dkd
+        nops = len(self.scheme.ops)
+        self._op_kind = (ctypes.c_int * nops)(*[op for op, _ in self.scheme.ops])
+        self._op_coef = (ctypes.c_double * nops)(*[c for _, c in self.scheme.ops])
 
     def recurse(self, ps, tau, evolve, bridge):
         """sia.py:1092-1123"""
@@ -214,4 +236,37 @@ class SIA(Base):
         return join(slow, fast)
 
     def do_step(self, ps, tau):
+        if self.native_h and self.update_tstep and not self.shared_tstep:
+            return self.native_step(ps, tau)
         return self.recurse(ps, tau, self.evolve, self.scheme.bridge)
+
+    def native_step(self, ps, tau):
+        """One h. step by tg_sia_h_step: the particles of `ps` are advanced
+        and reordered in place (slow before fast at every level, the order
+        recurse() returns), and t_curr advances as recurse() advances it.
+        Kepler pairs that reach their retry bound are reported once per
+        step."""
+        if not ps.n:
+            return ps
+        for name in ("tstepij", "ax", "ay", "az"):
+            if name not in ps._layout:
+                ps.register_auxiliary_attribute(name, "real")
+        real, ints = ps._real, ps._int
+        if real.stride(1) != 1 or ints.stride(1) != 1:
+            raise ValueError("particle blocks must have contiguous rows")
+        rows = (ctypes.c_int * len(NATIVE_ROWS))(*[ps._layout[k][1] for k in NATIVE_ROWS])
+        t = ctypes.c_double(self.t_curr)
+        stream = _stream()
+        prec = extensions.PRECISIONS
+        _native.check(_native.lib.tg_sia_h_step(
+            len(self._op_kind), self._op_kind, self._op_coef, int(self.kdk), float(self.eta), float(tau),
+            prec[extensions.acc.kernel.prec], prec[extensions.tstep.kernel.prec], ps.n,
+            real.data_ptr(), real.stride(0), len(ps._rnames), ints.data_ptr(), ints.stride(0), len(ps._inames),
+            rows, ctypes.byref(t), stream), "tg_sia_h_step")
+        self.t_curr = t.value
+        ps.t_curr = self.t_curr
+        st = _native.sync_status(stream)
+        if st & KEPLER_CAP:
+            warnings.warn("kepler_solver: retry bound reached for some pairs (status %d); "
+                          "the last iterate was kept" % st, RuntimeWarning)
+        return ps

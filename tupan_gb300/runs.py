@@ -6,6 +6,7 @@ configurations, each reporting a JSON summary.
     python -m tupan_gb300.runs binaries       # 2048 + 64 binaries, PN + Sakura
     python -m tupan_gb300.runs ensemble       # 512 clusters, Hermite-6, CUDA graph
     python -m tupan_gb300.runs kernels --n N  # per-kernel device time, ds32 and FP64
+    python -m tupan_gb300.runs integrators    # ms per step of the integrators, N=256
 
 All inputs are seeded synthetic Plummer spheres (tupan_gb300.ics).
 """
@@ -346,9 +347,45 @@ def kernels_run(n=65536, reps=5, kernels="phi,acc,acc_jerk,snap_crackle,tstep,pn
     return out
 
 
+def integrators_run(n=256, steps=8, methods="sia21h.dkd,sia21h.kdk,sia44h.kdk,sia21s.kdk,"
+                    "ahermite4,hermite6,sakura,nreg", eta=1.0 / 64, seed=1):
+    """Wall-clock ms per step (base step eta, one step per evolve_step call)
+    of the GPU integrators in FP64 on a Plummer sphere of n equal-mass
+    particles without softening (the reference's SIA/Sakura setting): one
+    untimed step, then `steps` timed steps, synchronised on both sides.
+    Hierarchical SIA methods are timed with the native recursion
+    (tg_sia_h_step) and with the Python one; `levels` counts the time-step
+    levels of one step (Tstep calls)."""
+    from .integrator import sia
+    extensions.set_precision("float64")
+    d = plummer_arrays(n, 0.0, seed=seed)
+    d["eps2"] = np.zeros(n)
+    out = {"config": {"n": n, "eta": eta, "steps": steps, "eps2": 0.0, "seed": seed,
+                      "ics": "plummer, equal masses, henon units", "precision": "float64"},
+           "ms_per_step": {}}
+    for method in methods.split(","):
+        variants = [("", True)]
+        if method[5:6] == "h":
+            variants = [("", True), (" python", False)]
+        for tag, native in variants:
+            ps = ParticleSystem.from_arrays(**d)
+            integ = Integrator(eta, 0.0, ps, method=method)
+            if isinstance(integ.integrator, sia.SIA):
+                integ.integrator.native_h = native
+            integ.evolve_step(eta)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for k in range(steps):
+                integ.evolve_step((k + 2) * eta)
+            torch.cuda.synchronize()
+            out["ms_per_step"][method + tag] = (time.perf_counter() - t0) / steps * 1e3
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("which", choices=["precision", "adjoint", "binaries", "ensemble", "kernels"])
+    ap.add_argument("which", choices=["precision", "adjoint", "binaries", "ensemble", "kernels",
+                                            "integrators"])
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--reps", type=int, default=None, help="kernels: timed calls per kernel")
@@ -364,7 +401,7 @@ def main():
         if getattr(args, k) is not None:
             kw[k] = getattr(args, k)
     fn = {"precision": precision_run, "adjoint": adjoint_run, "binaries": binaries_run,
-          "ensemble": ensemble_run, "kernels": kernels_run}[args.which]
+          "ensemble": ensemble_run, "kernels": kernels_run, "integrators": integrators_run}[args.which]
     print(json.dumps(fn(**kw), default=float))
 
 
