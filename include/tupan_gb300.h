@@ -38,6 +38,8 @@ extern "C" {
 /* precision selectors */
 #define TG_PREC_FP64 0 /* IEEE double, per-pair operations in the reference's order */
 #define TG_PREC_DS32 1 /* split FP32: hi/lo positions, compensated FP32 sums */
+#define TG_PREC_DS32X 2 /* double-single (float-float) arithmetic on the FP32 pipes, ~1e-12:
+                           Acc, AccJerk and tg_acc_vjp only (other kernels: TG_EINVAL) */
 
 /* return codes */
 #define TG_OK 0

@@ -7,6 +7,10 @@
   velocities and masses (adjoint, checkpointed) against FP64 central finite
   differences of the same forward map: 1e-6 relative, in FP64 and in split
   FP32 (ordered Acc forward, double-single adjoint).
+* TG_PREC_DS32X (double-single forces and adjoint): the forward within 1e-10
+  of FP64 at N = 65536 (ordered-path size), the VJP within 1e-9 of autograd,
+  the leapfrog gradient within 1e-8 of the FP64 adjoint; other kernels
+  refuse it.
 """
 import numpy as np
 import pytest
@@ -42,7 +46,7 @@ def naive_acc(r, m, e2):
     return -(d * (m[None, :] * q3)[None]).sum(2)
 
 
-@pytest.mark.parametrize("prec,tol", [("float64", 1e-10), ("ds32", 1e-9)])
+@pytest.mark.parametrize("prec,tol", [("float64", 1e-10), ("ds32", 1e-9), ("ds32x", 1e-9)])
 def test_vjp_matches_torch_autograd(ad, prec, tol):
     r, v, m, e2 = system(300, seed=1)
     g = torch.randn(3, 300, dtype=torch.float64, device="cuda")
@@ -165,3 +169,38 @@ def test_ds32_leapfrog_gradient_matches_fp64_finite_differences(ad):
                 fd = (4 * central(h) - central(2 * h)) / 3
                 g = float(grad[idx])
                 assert abs(fd - g) <= 1e-6 * abs(g) + 1e-9 * float(grad.abs().max()), (which, idx, fd, g)
+
+
+def test_ds32x_forward_at_ordered_size(ad):
+    """N = 65536 takes the ordered path in ds32; ds32x runs the double-single
+    kernel for every particle: per-particle error against FP64 <= 1e-10."""
+    r, v, m, e2 = system(65536, seed=10, e2=1e-6)
+    a64 = ad.acc_forward(r, m, e2, ad.PREC["float64"])
+    ax = ad.acc_forward(r, m, e2, ad.PREC["ds32x"])
+    err = ((ax - a64).norm(dim=0) / a64.norm(dim=0)).max()
+    assert float(err) <= 1e-10, float(err)
+
+
+def test_ds32x_leapfrog_gradient_matches_fp64_adjoint(ad):
+    n, steps, dt = 4096, 8, 1.0 / 256
+    r0, v0, m, e2 = system(n, seed=11, e2=1e-4)
+    target, _ = ad.leapfrog(r0 + 0.01, v0, m * 1.01, e2, dt, steps, "float64")
+    grads = {}
+    for prec in ("float64", "ds32x"):
+        r = r0.clone().requires_grad_(True)
+        v = v0.clone().requires_grad_(True)
+        mm = m.clone().requires_grad_(True)
+        rf, _ = ad.leapfrog(r, v, mm, e2, dt, steps, prec, checkpoint_every=4)
+        ad.loss_to_target(rf, target).backward()
+        grads[prec] = (r.grad, v.grad, mm.grad)
+    for gx, g64 in zip(grads["ds32x"], grads["float64"]):
+        assert float((gx - g64).norm() / g64.norm()) <= 1e-8
+
+
+def test_ds32x_refused_by_other_kernels(ad):
+    from tupan_gb300 import _native
+    r, v, m, e2 = system(64, seed=12)
+    out = torch.empty(64, dtype=torch.float64, device="cuda")
+    p = [m.data_ptr(), r[0].data_ptr(), r[1].data_ptr(), r[2].data_ptr(), e2.data_ptr()]
+    with pytest.raises(_native.TupanGB300Error, match="DS32X"):
+        _native.call_device("phi", 64, p, 64, p, (), [out.data_ptr()], _native.PREC_DS32X, _native.current_stream())

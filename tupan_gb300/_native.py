@@ -12,6 +12,7 @@ LIB_PATH = os.environ.get("TUPAN_GB300_LIB") or os.path.join(HERE, "_lib", "libt
 
 PREC_FP64 = 0
 PREC_DS32 = 1
+PREC_DS32X = 2   # double-single arithmetic: Acc, AccJerk, the Acc adjoint
 
 OK = 0
 EINVAL = -1

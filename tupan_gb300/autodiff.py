@@ -18,7 +18,8 @@ from torch.utils.checkpoint import checkpoint
 
 from . import _native
 
-PREC = {"float64": _native.PREC_FP64, "ds32": _native.PREC_DS32, "float32": _native.PREC_DS32}
+PREC = {"float64": _native.PREC_FP64, "ds32": _native.PREC_DS32, "float32": _native.PREC_DS32,
+        "ds32x": _native.PREC_DS32X}
 
 
 def _stream():

@@ -87,7 +87,10 @@ constexpr size_t MAX_N = (size_t)1 << 31;
 
 int run(int kernel, tg::PairArgs &a, int prec, void *stream) {
     g_err.clear();
-    if (prec != TG_PREC_FP64 && prec != TG_PREC_DS32) return fail(TG_EINVAL, "unknown precision");
+    if (prec != TG_PREC_FP64 && prec != TG_PREC_DS32 && prec != TG_PREC_DS32X)
+        return fail(TG_EINVAL, "unknown precision");
+    if (prec == TG_PREC_DS32X && !tg::ds32x_supported(kernel))
+        return fail(TG_EINVAL, "TG_PREC_DS32X is available for Acc, AccJerk and tg_acc_vjp only");
     if (a.ni > MAX_N || a.nj > MAX_N) return fail(TG_EINVAL, "ni or nj above 2^31");
     const int nf = tg::kernel_fields(kernel), no = tg::kernel_outputs(kernel);
     if (a.ni > 0) {
@@ -114,6 +117,11 @@ int run(int kernel, tg::PairArgs &a, int prec, void *stream) {
         e = tg::launch_sakura_split(a, c->ws, c->ws_bytes, c->sms, s);
     } else if (prec == TG_PREC_FP64 || !tg::ds32_supported(kernel) || a.nj == 0) {
         e = tg::launch_fp64(kernel, a, c->sms, s);
+    } else if (prec == TG_PREC_DS32X) {
+        std::lock_guard<std::mutex> lk(c->mu);
+        rc = ensure_ws(*c, tg::ds32x_workspace_bytes(kernel, a.nj), s);
+        if (rc != TG_OK) return rc;
+        e = tg::launch_ds32x(kernel, a, c->ws, c->ws_bytes, c->sms, s);
     } else {
         std::lock_guard<std::mutex> lk(c->mu);
         const size_t need = tg::ds32_workspace_bytes(kernel, a.ni, a.nj, c->sms);

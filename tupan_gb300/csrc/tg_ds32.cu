@@ -857,16 +857,19 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
 // ds32_ord_prepare writes the j-records in that order with positions
 // relative to the centre c_b of their 64-j block.  The pairwise kernel then
 // decides per 64-j block, from the block's and the i-tile's bounding boxes:
-//   * far (box distance >= the block's half-extent): dx = fl(xi - c_b) - x'h,
-//     one subtraction per component; its error is at most
-//     eps (|xi - c_b| + |xj - c_b|) <= 3 eps |dx|;
+//   * far (box distance >= ORD_THETA x the block's half-extent):
+//     dx = fl(xi - c_b) - x'h, one subtraction per component; its error is
+//     at most eps (|xi - c_b| + |xj - c_b|) <= (1 + 2 / ORD_THETA) eps |dx|
+//     = 5 eps |dx|;
 //   * near: the hi/lo difference (xi - c_b) - (xj - c_b), as accurate as
 //     the global hi/lo form;
 //   * heavy (the block holds heavy j): the near form with a Newton-refined
 //     1/sqrt and the compensated sums folded after every record, so the
 //     large terms of massive particles never sit in an FP32 lane sum.
 // The acceleration's FP32 lane sums are folded into Kahan sums every
-// 2 ORD_ACC_FOLD_PAIRS j, the jerk's every 64 j.  A per-i proxy of the sum
+// 2 ORD_ACC_FOLD_PAIRS j (far blocks of Acc: every 2 K::FAR_FOLD_PAIRS j,
+// 32; far terms are of one size within a block, and the longer fold left
+// the errors unchanged while saving 2% of Acc), the jerk's every 64 j.  A per-i proxy of the sum
 // of term magnitudes (the sum of |folded lane sums|) travels with the
 // partials; particles whose proxy exceeds tau |a| (strong cancellation,
 // ord_tau) are listed and their acceleration is recomputed in double-single
@@ -920,6 +923,7 @@ struct AccJerkOrd {
     static constexpr bool ORDERED = true;
     static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 7, PX = 6;
     static constexpr int W_FAR = 4, W_NEAR = 5, W_HEAVY = 9;   // relative cost of a 64-j block
+    static constexpr int FAR_FOLD_PAIRS = ORD_ACC_FOLD_PAIRS;  // (32-j far folds were 1% slower here)
     static constexpr bool UE2 = true;
     struct IS { float2 dh[3], dl[3]; float2 u, v, w, e; float2 a[3], j[3]; Comp ca[3], cj[3]; float px; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {
@@ -1016,6 +1020,7 @@ struct AccOrd {
     static constexpr bool ORDERED = true;
     static constexpr int IPT = IPT_, JF = 8, NQ = 4, NP = 4, PX = 3;
     static constexpr int W_FAR = 2, W_NEAR = 3, W_HEAVY = 6;   // relative cost of a 64-j block
+    static constexpr int FAR_FOLD_PAIRS = 16;                  // far blocks fold every 32 j
     static constexpr bool UE2 = true;
     struct IS { float2 dh[3], dl[3]; float2 e; float2 a[3]; Comp ca[3]; float px; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {
@@ -1272,8 +1277,8 @@ __global__ void ds32_ord_bounds(const int *ucost, const int *ucum, long long U, 
 }
 
 // One 64-j block of FORM against the thread's i-particles: acceleration
-// folds every ORD_ACC_FOLD_PAIRS records, jerk fold at the end (heavy
-// blocks: both after every record).
+// folds every ORD_ACC_FOLD_PAIRS records (far blocks: K::FAR_FOLD_PAIRS),
+// jerk fold at the end (heavy blocks: both after every record).
 template <class K, int FORM, bool UE>
 __device__ __forceinline__ void ord_block(typename K::IS (&st)[K::IPT], const float4 *R, float2 E) {
     if constexpr (FORM == ORD_HEAVY) {
@@ -1285,9 +1290,11 @@ __device__ __forceinline__ void ord_block(typename K::IS (&st)[K::IPT], const fl
         }
     } else {
 #pragma unroll 1
-        for (int r0 = 0; r0 < ORD_BLOCK_PAIRS; r0 += ORD_ACC_FOLD_PAIRS) {
+        constexpr int FOLD = FORM == ORD_FAR ? K::FAR_FOLD_PAIRS : ORD_ACC_FOLD_PAIRS;
+        static_assert(ORD_BLOCK_PAIRS % FOLD == 0, "folds must tile a block");
+        for (int r0 = 0; r0 < ORD_BLOCK_PAIRS; r0 += FOLD) {
 #pragma unroll ORD_UNROLL
-            for (int r = 0; r < ORD_ACC_FOLD_PAIRS; ++r) K::template step<FORM, UE>(st, R + (r0 + r) * K::NQ, E);
+            for (int r = 0; r < FOLD; ++r) K::template step<FORM, UE>(st, R + (r0 + r) * K::NQ, E);
 #pragma unroll
             for (int q = 0; q < K::IPT; ++q) K::fold_acc(st[q]);
         }
@@ -2278,6 +2285,20 @@ cudaError_t launch_ds32(int kernel, const PairArgs &a, void *ws, size_t ws_bytes
         case K_SNAP_CRACKLE: return run_ds<SnapCrackleDS<1, REF>>(a, ws, ws_bytes, sms, s);
         case K_TSTEP: return run_pick<TstepDS<IPT2, REF>, TstepDS<1, REF>>(a, ws, ws_bytes, sms, s);
         case K_PNACC: return run_ds<PNAccDS<1, REF>>(a, ws, ws_bytes, sms, s);
+        case K_ACC_VJP: return run_exact<EX_VJP>(a, ws, ws_bytes, sms, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+bool ds32x_supported(int kernel) { return kernel == K_ACC || kernel == K_ACC_JERK || kernel == K_ACC_VJP; }
+
+size_t ds32x_workspace_bytes(int kernel, size_t nj) { return ds32x_supported(kernel) ? exact_ws_bytes(nj) : 0; }
+
+// TG_PREC_DS32X: the double-single kernel for every particle, whatever the size
+cudaError_t launch_ds32x(int kernel, const PairArgs &a, void *ws, size_t ws_bytes, int sms, cudaStream_t s) {
+    switch (kernel) {
+        case K_ACC: return run_exact<EX_ACC>(a, ws, ws_bytes, sms, s);
+        case K_ACC_JERK: return run_exact<EX_ACC_JERK>(a, ws, ws_bytes, sms, s);
         case K_ACC_VJP: return run_exact<EX_VJP>(a, ws, ws_bytes, sms, s);
         default: return cudaErrorInvalidValue;
     }

@@ -72,6 +72,10 @@ size_t ds32_workspace_bytes(int kernel, size_t ni, size_t nj, int sms);
 cudaError_t launch_ds32(int kernel, const PairArgs &a, void *ws, size_t ws_bytes, int sms,
                         cudaStream_t s);
 bool ds32_supported(int kernel);
+// TG_PREC_DS32X (double-single for every particle): Acc, AccJerk, AccVjp
+bool ds32x_supported(int kernel);
+size_t ds32x_workspace_bytes(int kernel, size_t nj);
+cudaError_t launch_ds32x(int kernel, const PairArgs &a, void *ws, size_t ws_bytes, int sms, cudaStream_t s);
 
 // Segmented (ensemble) geometry for one kernel's i-tile size: C clusters,
 // U units, NIT i-tiles, NJT j-tiles in total; `dev` holds the device tables

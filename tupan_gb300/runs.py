@@ -49,7 +49,7 @@ def precision_run(n=65536, steps=128, dt=1.0 / 1024, seed=20261203, probe_every=
     d = plummer_arrays(n, 1e-3, imf=Salpeter(0.1, 100.0), seed=seed)
     out = {"config": {"n": n, "imf": "salpeter [0.1,100]", "eps2_pair": 1e-6, "method": "sia21s.kdk",
                       "dt": dt, "steps": steps, "tstep_eta": dt}}
-    for prec in ("ds32", "float64"):
+    for prec in ("ds32", "ds32x", "float64"):
         extensions.set_precision(prec)
         ps = ParticleSystem.from_arrays(**d)
         e0 = energy(ps)
@@ -87,7 +87,10 @@ def precision_run(n=65536, steps=128, dt=1.0 / 1024, seed=20261203, probe_every=
 
 def adjoint_run(n=16384, steps=64, dt=1.0 / 256, seed=16384, checkpoint_every=8, ncoords=32):
     """Gradients of a trajectory loss by the Acc adjoint, checked by FP64
-    central finite differences."""
+    central finite differences.  Three arithmetics for the forward and the
+    adjoint: ds32 (the split-FP32 forces, <= 1e-6 per particle, with the
+    double-single adjoint), ds32x (double-single forces and adjoint, ~1e-12)
+    and float64."""
     d = plummer_arrays(n, 0.01, seed=seed)
     dev = torch.device("cuda", torch.cuda.current_device())
     r0 = torch.tensor(np.stack([d["rx"], d["ry"], d["rz"]]), dtype=torch.float64, device=dev)
@@ -106,7 +109,7 @@ def adjoint_run(n=16384, steps=64, dt=1.0 / 256, seed=16384, checkpoint_every=8,
     out = {"config": {"n": n, "steps": steps, "dt": dt, "eps2_pair": 1e-4, "checkpoint_every": checkpoint_every,
                       "target": "same ICs, masses x lognormal(sigma=0.01), not renormalised, FP64 run"}}
     grads = {}
-    for prec in ("ds32", "float64"):
+    for prec in ("ds32", "ds32x", "float64"):
         # untimed one-step pass: first use of the torch and library kernels
         # (loading them on a fresh machine takes seconds)
         rw = r0.clone().requires_grad_(True)
@@ -124,9 +127,10 @@ def adjoint_run(n=16384, steps=64, dt=1.0 / 256, seed=16384, checkpoint_every=8,
         grads[prec] = (r.grad, v.grad, m.grad)
         out[prec] = {"loss": float(L.detach()), "seconds_forward_backward": time.perf_counter() - t0,
                      "peak_mem_mb": torch.cuda.max_memory_allocated() / 2 ** 20}
-    rel = [float((a - b).norm() / b.norm()) for a, b in zip(grads["ds32"], grads["float64"])]
-    out["ds32_vs_fp64_adjoint_rel_norm"] = {"r": rel[0], "v": rel[1], "m": rel[2]}
-    worst64, worst32, within, checks = 0.0, 0.0, 0, []
+    for prec in ("ds32", "ds32x"):
+        rel = [float((a - b).norm() / b.norm()) for a, b in zip(grads[prec], grads["float64"])]
+        out[prec + "_vs_fp64_adjoint_rel_norm"] = {"r": rel[0], "v": rel[1], "m": rel[2]}
+    worst64, worst32, worst32x, within, within32x, checks = 0.0, 0.0, 0.0, 0, 0, []
     with torch.no_grad():
         for q in range(ncoords):
             which = ("r", "v", "m")[q % 3]
@@ -156,21 +160,25 @@ def adjoint_run(n=16384, steps=64, dt=1.0 / 256, seed=16384, checkpoint_every=8,
             kb, kn = min(pairs, key=lambda p: abs(R[p[0]] - R[p[1]]))
             fd, spread = R[kb], abs(R[kb] - R[kn])
             k = "rvm".index(which)
-            g64, g32 = float(grads["float64"][k][idx]), float(grads["ds32"][k][idx])
+            g64, g32, g32x = (float(grads[p][k][idx]) for p in ("float64", "ds32", "ds32x"))
             den = max(abs(fd), 1e-300)
-            e64, e32 = abs(g64 - fd) / den, abs(g32 - fd) / den
-            worst64, worst32 = max(worst64, e64), max(worst32, e32)
+            e64, e32, e32x = abs(g64 - fd) / den, abs(g32 - fd) / den, abs(g32x - fd) / den
+            worst64, worst32, worst32x = max(worst64, e64), max(worst32, e32), max(worst32x, e32x)
             within += abs(g64 - fd) <= max(1e-6 * abs(fd), 2.0 * spread)
+            within32x += abs(g32x - fd) <= max(1e-6 * abs(fd), 2.0 * spread)
             checks.append({"coord": which + str(idx), "fd": fd, "h": scale * 10.0 ** -kb,
                            "fd_spread_rel": spread / den, "adjoint_fp64": g64, "adjoint_ds32": g32,
-                           "rel_error_fp64": e64})
+                           "adjoint_ds32x": g32x, "rel_error_fp64": e64, "rel_error_ds32x": e32x})
     out["finite_difference"] = {
         "coordinates": ncoords,
         "method": "central differences at h = scale x 10^-k (k = %s), Richardson ratio 10, "
                   "most self-consistent step kept" % ",".join(map(str, FD_LADDER)),
         "max_rel_error_fp64_adjoint": worst64, "max_rel_error_ds32_adjoint": worst32,
+        "max_rel_error_ds32x_adjoint": worst32x,
         "median_rel_error_fp64_adjoint": float(np.median([c["rel_error_fp64"] for c in checks])),
+        "median_rel_error_ds32x_adjoint": float(np.median([c["rel_error_ds32x"] for c in checks])),
         "fp64_within_max(1e-6, 2 x fd spread)": "%d of %d" % (within, ncoords),
+        "ds32x_within_max(1e-6, 2 x fd spread)": "%d of %d" % (within32x, ncoords),
         "samples": sorted(checks, key=lambda c: -c["rel_error_fp64"])[:6]}
     return out
 
