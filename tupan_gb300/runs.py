@@ -49,7 +49,7 @@ def precision_run(n=65536, steps=128, dt=1.0 / 1024, seed=20261203, probe_every=
     d = plummer_arrays(n, 1e-3, imf=Salpeter(0.1, 100.0), seed=seed)
     out = {"config": {"n": n, "imf": "salpeter [0.1,100]", "eps2_pair": 1e-6, "method": "sia21s.kdk",
                       "dt": dt, "steps": steps, "tstep_eta": dt}}
-    for prec in ("ds32", "ds32x", "float64"):
+    for prec in ("ds32", "float64"):
         extensions.set_precision(prec)
         ps = ParticleSystem.from_arrays(**d)
         e0 = energy(ps)
