@@ -949,11 +949,20 @@ struct AccJerkOrd {
         r[16 + lane] = l[0]; r[18 + lane] = l[1]; r[20 + lane] = l[2];
         r[22 + lane] = 0.f;
     }
+    struct Rec { float4 q[NQ]; };
+    // the floats of one record that FORM reads (far: positions' hi parts,
+    // mass, velocities, softening)
     template <int FORM, bool UE>
-    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R, float2 E) {
-        const float4 q0 = R[0], q1 = R[1], q2 = R[2], q3 = R[3];
-        float4 q4 = q0, q5 = q0;
-        if (FORM != ORD_FAR) { q4 = R[4]; q5 = R[5]; }
+    __device__ __forceinline__ static Rec load_rec(const float4 *R) {
+        Rec c;
+        c.q[0] = R[0]; c.q[1] = R[1]; c.q[2] = R[2]; c.q[3] = R[3];
+        c.q[4] = c.q[0]; c.q[5] = c.q[0];
+        if (FORM != ORD_FAR) { c.q[4] = R[4]; c.q[5] = R[5]; }
+        return c;
+    }
+    template <int FORM, bool UE>
+    __device__ __forceinline__ static void step(IS (&S)[IPT], const Rec &c, float2 E) {
+        const float4 q0 = c.q[0], q1 = c.q[1], q2 = c.q[2], q3 = c.q[3], q4 = c.q[4], q5 = c.q[5];
 #pragma unroll
         for (int u = 0; u < IPT; ++u) {
             IS &s = S[u];
@@ -1036,12 +1045,19 @@ struct AccOrd {
         r[8 + lane] = l[0]; r[10 + lane] = l[1]; r[12 + lane] = l[2];
         r[14 + lane] = valid ? __double2float_rn(J.f[F_E2][j]) : 1.f;
     }
+    struct Rec { float4 q[NQ]; };
     template <int FORM, bool UE>
-    __device__ __forceinline__ static void step(IS (&S)[IPT], const float4 *R, float2 E) {
-        const float4 q0 = R[0], q1 = R[1];
-        float4 q2 = q0, q3 = q1;
-        if (FORM != ORD_FAR || !UE) q3 = R[3];
-        if (FORM != ORD_FAR) q2 = R[2];
+    __device__ __forceinline__ static Rec load_rec(const float4 *R) {
+        Rec c;
+        c.q[0] = R[0]; c.q[1] = R[1];
+        c.q[2] = c.q[0]; c.q[3] = c.q[1];
+        if (FORM != ORD_FAR || !UE) c.q[3] = R[3];
+        if (FORM != ORD_FAR) c.q[2] = R[2];
+        return c;
+    }
+    template <int FORM, bool UE>
+    __device__ __forceinline__ static void step(IS (&S)[IPT], const Rec &c, float2 E) {
+        const float4 q0 = c.q[0], q1 = c.q[1], q2 = c.q[2], q3 = c.q[3];
 #pragma unroll
         for (int u = 0; u < IPT; ++u) {
             IS &s = S[u];
@@ -1284,7 +1300,7 @@ __device__ __forceinline__ void ord_block(typename K::IS (&st)[K::IPT], const fl
     if constexpr (FORM == ORD_HEAVY) {
 #pragma unroll 1
         for (int r = 0; r < ORD_BLOCK_PAIRS; ++r) {
-            K::template step<FORM, UE>(st, R + r * K::NQ, E);
+            K::template step<FORM, UE>(st, K::template load_rec<FORM, UE>(R + r * K::NQ), E);
 #pragma unroll
             for (int q = 0; q < K::IPT; ++q) { K::fold_acc(st[q]); K::fold_jerk(st[q]); }
         }
@@ -1294,7 +1310,8 @@ __device__ __forceinline__ void ord_block(typename K::IS (&st)[K::IPT], const fl
         static_assert(ORD_BLOCK_PAIRS % FOLD == 0, "folds must tile a block");
         for (int r0 = 0; r0 < ORD_BLOCK_PAIRS; r0 += FOLD) {
 #pragma unroll ORD_UNROLL
-            for (int r = 0; r < FOLD; ++r) K::template step<FORM, UE>(st, R + (r0 + r) * K::NQ, E);
+            for (int r = 0; r < FOLD; ++r)
+                K::template step<FORM, UE>(st, K::template load_rec<FORM, UE>(R + (r0 + r) * K::NQ), E);
 #pragma unroll
             for (int q = 0; q < K::IPT; ++q) K::fold_acc(st[q]);
         }
@@ -1472,7 +1489,10 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs o
 constexpr int EXACT_THREADS = 256;                 // 8 warps per CTA
 constexpr int EXACT_WARPS = EXACT_THREADS / 32;
 constexpr int EXACT_MAX_CHUNKS = 16;
-constexpr int EXACT_MAX_SPLIT = 512;   // particles that may be split (ticket and partial slots)
+#ifndef TG_EXACT_MAX_SPLIT
+#define TG_EXACT_MAX_SPLIT 4096
+#endif
+constexpr int EXACT_MAX_SPLIT = TG_EXACT_MAX_SPLIT;   // particles that may be split (ticket and partial slots)
 enum : int { EX_ACC = 0, EX_ACC_JERK = 1, EX_VJP = 2 };
 template <int MODE>
 __global__ void __launch_bounds__(EXACT_THREADS) ds32_exact(PairArgs a, const float4 *jd, const int *count,
@@ -1839,6 +1859,11 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
 // ---------------------------------------------------------------------------
 // Host side.
 // ---------------------------------------------------------------------------
+#ifndef TG_ORD_UNITS_PER_CTA
+#define TG_ORD_UNITS_PER_CTA 8   // ordered kernel: j-tiles are split until units >= this x CTA slots
+#endif
+constexpr long long ORD_UNITS_PER_CTA = TG_ORD_UNITS_PER_CTA;
+constexpr long long ORD_MAX_CONTRIB = 24;   // mean CTAs per i-tile the j-split may reach
 #ifndef TG_DS32_MAX_JSUB
 #define TG_DS32_MAX_JSUB 2   // parts a j-tile may be split into (1 or 2; 2 measured best at N = 4096)
 #endif
@@ -1883,6 +1908,8 @@ static int ctas_per_sm_ord() {
         const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
         cudaFuncSetAttribute(ds32_ord<K, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(ds32_ord<K, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(ds32_ord<K, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(ds32_ord<K, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int n = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ds32_ord<K, 1>, DS_THREADS, smem) != cudaSuccess || n < 1)
             n = 1;
@@ -1910,7 +1937,20 @@ static Geometry geometry(size_t ni, size_t nj, int sms) {
     // a CTA's time is its whole-unit count, ceil(U / slots) units of size
     // 1 / jsub (N = 16384, AccJerk: 4 whole units per CTA, or 7 halves).
     g.jsub = 1;
-    if (TG_DS32_MAX_JSUB >= 2) {
+    if constexpr (is_ordered<K>::value) {
+        // cost-weighted CTA ranges end on unit boundaries: split j-tiles
+        // (up to 8 parts of 64 j) until there are ORD_UNITS_PER_CTA units
+        // per CTA slot, so small calls fill the GPU and a CTA's share is
+        // within about 1 / ORD_UNITS_PER_CTA of the mean -- but not so far
+        // that an i-tile's partial sums come from more than ORD_MAX_CONTRIB
+        // CTAs on average (its last CTA adds them all; N = 4096: 0.18 ms
+        // with 8 parts, 0.16 ms with 2)
+        while (g.jsub < 8 && g.nit * g.njt * g.jsub < ORD_UNITS_PER_CTA * slots) {
+            const long long u2 = g.nit * g.njt * g.jsub * 2, grid2 = u2 < slots ? u2 : slots;
+            if (grid2 > ORD_MAX_CONTRIB * g.nit) break;
+            g.jsub *= 2;
+        }
+    } else if (TG_DS32_MAX_JSUB >= 2) {
         const long long u = g.nit * g.njt;
         const double t1 = (double)((u + slots - 1) / slots), t2 = 0.5 * (double)((2 * u + slots - 1) / slots);
         if (u < 2 * slots || t2 <= 0.9 * t1) g.jsub = 2;
@@ -2147,8 +2187,12 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
     ProfRec pr{K::NP == 7 ? K_ACC_JERK : K_ACC, nullptr, nullptr};
     const bool prof = g_prof.load() && cudaEventCreate(&pr.e0) == cudaSuccess &&
                       cudaEventCreate(&pr.e1) == cudaSuccess && cudaEventRecord(pr.e0, s) == cudaSuccess;
-    if (g.jsub == 2) ds32_ord<K, 2><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
-    else ds32_ord<K, 1><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a);
+    switch (g.jsub) {
+        case 8: ds32_ord<K, 8><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a); break;
+        case 4: ds32_ord<K, 4><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a); break;
+        case 2: ds32_ord<K, 2><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a); break;
+        default: ds32_ord<K, 1><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a); break;
+    }
     if (prof && cudaEventRecord(pr.e1, s) == cudaSuccess) {
         std::lock_guard<std::mutex> lk(g_prof_mu);
         g_prof_rec.push_back(pr);
