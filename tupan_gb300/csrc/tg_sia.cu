@@ -373,6 +373,11 @@ extern "C" int tg_sia_h_step(int nops, const int *op_kind, const double *op_coef
         tg::set_last_error("tg_sia_h_step: bad scheme or null pointer");
         return TG_EINVAL;
     }
+    for (int q = 0; q < nops; ++q)
+        if (op_kind[q] != 0 && op_kind[q] != 1) {
+            tg::set_last_error("tg_sia_h_step: operator kinds are 0 or 1");
+            return TG_EINVAL;
+        }
     if (n == 0) return TG_OK;
     if (!real || !ints || rows_real < 1 || rows_int < 1 || ld_real < n || ld_int < n) {
         tg::set_last_error("tg_sia_h_step: bad particle blocks");
@@ -388,9 +393,10 @@ extern "C" int tg_sia_h_step(int nops, const int *op_kind, const double *op_coef
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) return TG_ENODEV;
     if (g_pool.device != dev) {
-        // buffers of another device are not usable here (the old ones leak
-        // only if a process alternates devices, which the library does not
-        // support for one particle set)
+        // level buffers of another device are not usable here: release them
+        // (with unified addressing cudaFree finds their device)
+        for (Level &L : g_pool.levels)
+            if (L.p) cudaFree(L.p);
         g_pool.levels.clear();
         g_pool.device = dev;
     }
@@ -402,10 +408,6 @@ extern "C" int tg_sia_h_step(int nops, const int *op_kind, const double *op_coef
     Engine e;
     e.nops = nops;
     for (int q = 0; q < nops; ++q) {
-        if (op_kind[q] != 0 && op_kind[q] != 1) {
-            tg::set_last_error("tg_sia_h_step: operator kinds are 0 or 1");
-            return TG_EINVAL;
-        }
         e.kind[q] = op_kind[q];
         e.coef[q] = op_coef[q];
     }
