@@ -382,10 +382,12 @@ def integrators_run(n=256, steps=8, methods="sia21h.dkd,sia21h.kdk,sia44h.kdk,si
                 integ.integrator.native_h = native
             integ.evolve_step(eta)
             torch.cuda.synchronize()
+            torch.cuda.nvtx.range_push(method + tag.replace(" ", "_"))   # ncu --nvtx-include <name>/
             t0 = time.perf_counter()
             for k in range(steps):
                 integ.evolve_step((k + 2) * eta)
             torch.cuda.synchronize()
+            torch.cuda.nvtx.range_pop()
             out["ms_per_step"][method + tag] = (time.perf_counter() - t0) / steps * 1e3
     return out
 
@@ -398,14 +400,15 @@ def main():
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--reps", type=int, default=None, help="kernels: timed calls per kernel")
     ap.add_argument("--kernels", default=None, help="kernels: comma-separated kernel names")
-    ap.add_argument("--precisions", default=None, help="kernels: comma-separated, ds32/float64")
+    ap.add_argument("--precisions", default=None, help="kernels: comma-separated, ds32/ds32x/float64")
+    ap.add_argument("--methods", default=None, help="integrators: comma-separated method names")
     args = ap.parse_args()
     kw = {}
     if args.steps:
         kw["steps"] = args.steps
     if args.n:
         kw["n"] = args.n
-    for k in ("reps", "kernels", "precisions"):
+    for k in ("reps", "kernels", "precisions", "methods"):
         if getattr(args, k) is not None:
             kw[k] = getattr(args, k)
     fn = {"precision": precision_run, "adjoint": adjoint_run, "binaries": binaries_run,
