@@ -421,6 +421,10 @@ def ours(args, rank, world, dist):
     _native.lib.tg_time_pair_kernel(0)
     k_acc_ms, k_acc_n = _native.pair_kernel_time(_native.KERNEL_ACC)
     k_aj_ms, k_aj_n = _native.pair_kernel_time(_native.KERNEL_ACC_JERK)
+    if n >= 4096 and (k_acc_n != args.steps or k_aj_n != args.steps):
+        # every timed call at these sizes takes the ordered path
+        raise RuntimeError("pairwise-kernel events: %d Acc and %d AccJerk launches recorded for %d steps"
+                           % (k_acc_n, k_aj_n, args.steps))
     if dist:
         dist.barrier()
     clk = clocks.stop()

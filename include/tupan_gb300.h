@@ -76,6 +76,16 @@ int tg_get_host_precision(void);
 #define TG_KERNEL_ACC_JERK 2
 int tg_time_pair_kernel(int on);
 int tg_pair_kernel_time(int kernel, double *ms, long long *launches);
+/* Accuracy control of split-FP32 Acc and AccJerk calls of 2^24 pairs and
+ * more (no counterpart in the reference; process-wide).  Such a call
+ * recomputes in double-single arithmetic every particle whose sum of term
+ * magnitudes exceeds tau times its |a| (jerk: 2.5 tau times |j|), tau
+ * scaled down with sqrt(nj / 65536) below 65536 j-particles.  The default,
+ * 20, holds every particle of a Plummer-Salpeter sphere within 1e-6 of
+ * FP64; 10 does so on flattened, multi-cluster and six-decade-mass-range
+ * sets as well, at +20% time.  Returns the previous tau, or -1 (unchanged)
+ * unless 1 <= tau <= 1e6. */
+double tg_set_recompute_threshold(double tau);
 /* Sakura evaluation (no counterpart in the reference; process-wide): 1, the
  * default, solves the pairs that take the universal-variable Kepler solver
  * apart from the others (flags -1 and +1, ni * nj <= 2^30; uses the grow-only

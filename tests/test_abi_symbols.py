@@ -101,3 +101,13 @@ def test_sia_h_step_validates_its_arguments_before_any_cuda_call(lib):
     odd = (ctypes.c_int * 3)(0, 2, 0)
     assert call(k=odd) == -1 and b"kinds" in lib.tg_last_error()
     assert call(n=0, k=odd) == -1                          # the scheme is checked even for an empty set
+
+
+def test_recompute_threshold_setting_without_gpu(lib):
+    f = lib.tg_set_recompute_threshold
+    f.restype = ctypes.c_double
+    f.argtypes = [ctypes.c_double]
+    prev = f(12.5)
+    assert prev == 20.0                      # the default
+    assert f(0.5) == -1.0 and f(float("nan")) == -1.0 and f(2e6) == -1.0
+    assert f(prev) == 12.5                   # restored

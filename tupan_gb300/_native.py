@@ -92,6 +92,8 @@ def _load():
     lib.tg_acc_vjp.argtypes = [ctypes.c_size_t] + [_DP] * 12 + [ctypes.c_int, _DP]
     lib.tg_probe_fma_tflops.restype = ctypes.c_double
     lib.tg_probe_fma_tflops.argtypes = [ctypes.c_int, ctypes.c_int, _DP]
+    lib.tg_set_recompute_threshold.restype = ctypes.c_double
+    lib.tg_set_recompute_threshold.argtypes = [ctypes.c_double]
     lib.tg_time_pair_kernel.restype = ctypes.c_int
     lib.tg_time_pair_kernel.argtypes = [ctypes.c_int]
     lib.tg_pair_kernel_time.restype = ctypes.c_int
@@ -147,6 +149,15 @@ def pair_kernel_time(kernel):
     ms, n = ctypes.c_double(), ctypes.c_longlong()
     check(lib.tg_pair_kernel_time(kernel, ctypes.byref(ms), ctypes.byref(n)), "tg_pair_kernel_time")
     return ms.value, n.value
+
+
+def set_recompute_threshold(tau):
+    """Split-FP32 Acc/AccJerk accuracy control (tg_set_recompute_threshold):
+    returns the previous threshold; raises on a value outside [1, 1e6]."""
+    prev = lib.tg_set_recompute_threshold(float(tau))
+    if prev < 0:
+        raise ValueError("recompute threshold must lie in [1, 1e6], got %r" % (tau,))
+    return prev
 
 
 def sync_status(stream=None):

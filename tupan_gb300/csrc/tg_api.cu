@@ -269,6 +269,8 @@ int tg_set_sakura_split(int on) { return g_sakura_split.exchange(on ? 1 : 0); }
 
 int tg_time_pair_kernel(int on) { return tg::prof_enable(on); }
 
+double tg_set_recompute_threshold(double tau) { return tg::set_recompute_threshold(tau); }
+
 int tg_pair_kernel_time(int kernel, double *ms, long long *launches) {
     if (!ms || !launches || (kernel != TG_KERNEL_ACC && kernel != TG_KERNEL_ACC_JERK))
         return fail(TG_EINVAL, "tg_pair_kernel_time: kernel must be TG_KERNEL_ACC or TG_KERNEL_ACC_JERK");

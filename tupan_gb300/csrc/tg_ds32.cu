@@ -921,11 +921,11 @@ enum : int { ORD_FAR = 0, ORD_NEAR = 1, ORD_HEAVY = 2 };
 template <int IPT_>
 struct AccJerkOrd {
     static constexpr bool ORDERED = true;
-    static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 7, PX = 6;
+    static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 8, PX = 6, PJ = 7;   // PJ: jerk proxy
     static constexpr int W_FAR = 4, W_NEAR = 5, W_HEAVY = 9;   // relative cost of a 64-j block
     static constexpr int FAR_FOLD_PAIRS = ORD_ACC_FOLD_PAIRS;  // (32-j far folds were 1% slower here)
     static constexpr bool UE2 = true;
-    struct IS { float2 dh[3], dl[3]; float2 u, v, w, e; float2 a[3], j[3]; Comp ca[3], cj[3]; float px; };
+    struct IS { float2 dh[3], dl[3]; float2 u, v, w, e; float2 a[3], j[3]; Comp ca[3], cj[3]; float px, pj; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {
         s.u = f2(__double2float_rn(a.I.f[F_VX][i]));
         s.v = f2(__double2float_rn(a.I.f[F_VY][i]));
@@ -936,6 +936,7 @@ struct AccJerkOrd {
             s.ca[k] = Comp{0.f, 0.f}; s.cj[k] = Comp{0.f, 0.f};
         }
         s.px = 0.f;
+        s.pj = 0.f;
     }
     // record: {x'h,y'h} {z'h,m} {vx,vy} {vz,e2} {x'l,y'l} {z'l,pad}
     __device__ static void write_record(float *r, int lane, const float h[3], const float l[3], const PSet &J,
@@ -1012,11 +1013,17 @@ struct AccJerkOrd {
         }
     }
     __device__ static void fold_jerk(IS &s) {
-        for (int k = 0; k < 3; ++k) { comp_add(s.cj[k], __fadd_rn(s.j[k].x, s.j[k].y)); s.j[k] = f2(0.f); }
+        for (int k = 0; k < 3; ++k) {
+            const float x = __fadd_rn(s.j[k].x, s.j[k].y);
+            comp_add(s.cj[k], x);
+            s.pj = __fadd_rn(s.pj, fabsf(x));
+            s.j[k] = f2(0.f);
+        }
     }
     __device__ static void partials(const IS &s, double *p) {
         for (int k = 0; k < 3; ++k) { p[k] = comp_value(s.ca[k]); p[3 + k] = comp_value(s.cj[k]); }
         p[6] = (double)s.px;
+        p[7] = (double)s.pj;
     }
     __device__ static void combine(double *acc, const double *p) { for (int k = 0; k < NP; ++k) acc[k] += p[k]; }
     __device__ static void store(const double *p, const PairArgs &a, size_t i) {
@@ -1027,7 +1034,7 @@ struct AccJerkOrd {
 template <int IPT_>
 struct AccOrd {
     static constexpr bool ORDERED = true;
-    static constexpr int IPT = IPT_, JF = 8, NQ = 4, NP = 4, PX = 3;
+    static constexpr int IPT = IPT_, JF = 8, NQ = 4, NP = 4, PX = 3, PJ = -1;
     static constexpr int W_FAR = 2, W_NEAR = 3, W_HEAVY = 6;   // relative cost of a 64-j block
     static constexpr int FAR_FOLD_PAIRS = 16;                  // far blocks fold every 32 j
     static constexpr bool UE2 = true;
@@ -1179,7 +1186,7 @@ __global__ void __launch_bounds__(DS_TILE) ds32_ord_prepare(PSet J, size_t nj, c
         else { h[c] = 0.f; l[c] = 0.f; }
     }
     K::write_record(rec + (p >> 1) * (size_t)(2 * K::JF), (int)(p & 1), h, l, J, j, valid);
-    if (valid) write_exact_record(jd + EXACT_JQ * p, J, j, -1);
+    if (valid) write_exact_record(jd + EXACT_JQ * p, J, j, K::PJ >= 0 ? F_VX : -1);
     if (tile_e2 != nullptr) {   // the tile's common float softening, or NaN
         const unsigned mine = valid ? __float_as_uint(__double2float_rn(J.f[F_E2][j])) : 0u;
         if (q == 0) s_first = mine;   // the tile's first j is always valid
@@ -1231,13 +1238,24 @@ struct DsOrdArgs {
     const long long *start;       // CTA k owns units [start[k], start[k + 1])
     int *flag_count, *flag_list;
     float tau;                    // recompute when proxy > tau |a|
+    float tau_jerk;               // or jerk proxy > tau_jerk |j| (AccJerk)
 };
 
-// Recompute threshold: 20 at nj >= 65536, scaled with sqrt(nj) below (fewer
-// terms average out less of their rounding), at least 4.
+// Recompute threshold tau (process-wide, tg_set_recompute_threshold; 20 by
+// default) at nj >= 65536, scaled with sqrt(nj) below (fewer terms average
+// out less of their rounding), at least 4 (and at most tau).  The jerk's
+// threshold is ORD_TAU_JERK_FACTOR times the acceleration's: its bound
+// (1e-5) is ten times looser, its proxy coarser (folds every 64 j).
+constexpr float ORD_TAU_JERK_FACTOR = 2.5f;
+std::atomic<float> g_ord_tau{20.0f};
 static float ord_tau(size_t nj) {
-    const double t = 20.0 * sqrt((double)nj / 65536.0);
-    return (float)(t > 20.0 ? 20.0 : (t < 4.0 ? 4.0 : t));
+    const double tau = g_ord_tau.load(), t = tau * sqrt((double)nj / 65536.0);
+    return (float)(t > tau ? tau : (t < 4.0 ? (tau < 4.0 ? tau : 4.0) : t));
+}
+
+double set_recompute_threshold(double tau) {
+    if (!(tau >= 1.0 && tau <= 1e6)) return -1.0;
+    return (double)g_ord_tau.exchange((float)tau);
 }
 
 // Form of 64-j block `b` for an i-tile with float bounding box [ilo, ihi]:
@@ -1450,7 +1468,12 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs o
                             const size_t i = (size_t)oa.pi[ii];
                             K::store(p, a.p, i);
                             const double am = sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
-                            if (!(p[K::PX] <= (double)oa.tau * am)) {
+                            bool redo = !(p[K::PX] <= (double)oa.tau * am);
+                            if constexpr (K::PJ >= 0) {
+                                const double jm = sqrt(p[3] * p[3] + p[4] * p[4] + p[5] * p[5]);
+                                redo = redo || !(p[K::PJ] <= (double)oa.tau_jerk * jm);
+                            }
+                            if (redo) {
                                 const int f = atomicAdd(oa.flag_count, 1);
                                 oa.flag_list[f] = (int)i;
                             }
@@ -2183,8 +2206,9 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
     a.flag_count = flags;
     a.flag_list = flags + 64;
     a.tau = ord_tau(p.nj);
+    a.tau_jerk = ORD_TAU_JERK_FACTOR * a.tau;
     const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
-    ProfRec pr{K::NP == 7 ? K_ACC_JERK : K_ACC, nullptr, nullptr};
+    ProfRec pr{K::PJ >= 0 ? K_ACC_JERK : K_ACC, nullptr, nullptr};   // AccJerkOrd has a jerk proxy
     const bool prof = g_prof.load() && cudaEventCreate(&pr.e0) == cudaSuccess &&
                       cudaEventCreate(&pr.e1) == cudaSuccess && cudaEventRecord(pr.e0, s) == cudaSuccess;
     switch (g.jsub) {
@@ -2197,7 +2221,10 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
         std::lock_guard<std::mutex> lk(g_prof_mu);
         g_prof_rec.push_back(pr);
     }
-    ds32_exact<EX_ACC><<<(unsigned)(sms * 4), EXACT_THREADS, 0, s>>>(p, jd, flags, flags + 64, ref_part, ref_ticket);
+    // flagged AccJerk particles get both vectors recomputed (a second list
+    // for the acceleration-only ones measured no faster)
+    ds32_exact<K::PJ >= 0 ? EX_ACC_JERK : EX_ACC><<<(unsigned)(sms * 4), EXACT_THREADS, 0, s>>>(p, jd, flags, flags + 64,
+                                                                                        ref_part, ref_ticket);
     return cudaGetLastError();
 }
 

@@ -119,6 +119,10 @@ size_t ds32_workspace_bytes_capped(int kernel, size_t ni, size_t nj, int sms, lo
 cudaError_t launch_ds32_capped(int kernel, const PairArgs &a, void *ws, size_t ws_bytes, int sms,
                                long long max_grid, cudaStream_t s);
 // Timing of the ordered pairwise kernel (tg_time_pair_kernel).
+// Ordered split-FP32 Acc/AccJerk: a particle whose sum of term magnitudes
+// (proxy) exceeds tau |a| is recomputed in double-single; returns the
+// previous tau, or -1 (unchanged) unless 1 <= tau <= 1e6.
+double set_recompute_threshold(double tau);
 int prof_enable(int on);
 cudaError_t prof_read(int kernel, double *ms, long long *launches);
 
