@@ -65,3 +65,21 @@ def test_nonfinite_inputs_follow_the_reference(mods, name, prec):
         assert np.array_equal(got[ok], want[ok])
     else:
         assert not np.isfinite(got[~np.isfinite(want)]).any(), name
+
+
+@pytest.mark.parametrize("name", ["acc", "acc_jerk"])
+def test_nonfinite_inputs_on_the_ordered_path(mods, name):
+    """4096 particles take the ordered split-FP32 path (Hilbert sort, block
+    records, recompute): a NaN position and an infinite velocity still give
+    non-finite results wherever the FP64 kernels (the reference's
+    arithmetic) do, and no status bit."""
+    native, ext, _ = mods
+    d = particles(4096, seed=22)
+    d["rx"][100] = np.nan
+    d["vy"][3000] = np.inf
+    native.sync_status()
+    got = np.stack([o.cpu().numpy() for o in getattr(ext, KCLASS[name])("CUDA", "ds32").calc(PS(d), PS(d))])
+    want = np.stack([o.cpu().numpy() for o in getattr(ext, KCLASS[name])("CUDA", "float64").calc(PS(d), PS(d))])
+    torch.cuda.synchronize()
+    assert native.sync_status() == 0
+    assert not np.isfinite(got[~np.isfinite(want)]).any(), name
