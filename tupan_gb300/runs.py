@@ -257,10 +257,13 @@ def binaries_run(nbg=2048, nbin=64, t_end=1.0 / 16, dt=1.0 / 1024, clight=1e4, p
                                          "max": float(max(s / a for s, a in zip(sep, semis)))}}
 
 
-def ensemble_run(nclusters=512, steps=16, dt=1.0 / 1024, base_seed=512):
+def ensemble_run(nclusters=512, steps=16, dt=1.0 / 1024, base_seed=512, compare_fp64=True):
     """512 Plummer clusters (N log-uniform in [64, 8192]), 6th-order Hermite
     with a shared step, every force evaluation one segmented launch, one
-    step captured in a CUDA graph and replayed."""
+    step captured in a CUDA graph and replayed.  With compare_fp64 the same
+    steps are taken with the FP64 kernels (eagerly) and the per-cluster
+    energy errors of the two are compared: the split-FP32 AccJerk and
+    SnapCrackle bounds against what they do to the integrator."""
     from .ensemble import Ensemble, random_ensemble
     cl = random_ensemble(nclusters, base_seed=base_seed)
     ens = Ensemble(cl, prec="ds32")
@@ -292,14 +295,34 @@ def ensemble_run(nclusters=512, steps=16, dt=1.0 / 1024, base_seed=512):
     e1 = ens.energy()
     de = np.abs((e1 - e0) / e0)
     total_steps = steps + 3
-    return {"config": {"clusters": nclusters, "n_range": [64, 8192], "total_particles": int(ens.ps.n),
-                       "sum_n2": ens.interactions, "eps2_pair": 1e-4, "method": "hermite6 shared step",
-                       "dt": dt, "steps": total_steps, "precision": "ds32"},
-            "acc_jerk": {"ms": aj_ms, "gint_s": ens.interactions / (aj_ms * 1e-3) / 1e9},
-            "snap_crackle": {"ms": sc_ms, "gint_s": ens.interactions / (sc_ms * 1e-3) / 1e9},
-            "ms_per_step_eager": eager_ms, "ms_per_step_graph": graph_ms,
-            "gint_s_per_step_graph": 3 * 2 * ens.interactions / (graph_ms * 1e-3) / 1e9,
-            "energy_error": {"median": float(np.median(de)), "max": float(de.max())}}
+    out = {"config": {"clusters": nclusters, "n_range": [64, 8192], "total_particles": int(ens.ps.n),
+                      "sum_n2": ens.interactions, "eps2_pair": 1e-4, "method": "hermite6 shared step",
+                      "dt": dt, "steps": total_steps, "precision": "ds32"},
+           "acc_jerk": {"ms": aj_ms, "gint_s": ens.interactions / (aj_ms * 1e-3) / 1e9},
+           "snap_crackle": {"ms": sc_ms, "gint_s": ens.interactions / (sc_ms * 1e-3) / 1e9},
+           "ms_per_step_eager": eager_ms, "ms_per_step_graph": graph_ms,
+           "gint_s_per_step_graph": 3 * 2 * ens.interactions / (graph_ms * 1e-3) / 1e9,
+           "energy_error": {"median": float(np.median(de)), "max": float(de.max())}}
+    if compare_fp64:
+        ref = Ensemble(cl, prec="float64")
+        f0 = ref.energy()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(total_steps):
+            ref.hermite_step(dt)
+        torch.cuda.synchronize()
+        f1 = ref.energy()
+        df = np.abs((f1 - f0) / f0)
+        out["fp64"] = {"ms_per_step_eager": 1e3 * (time.perf_counter() - t0) / total_steps,
+                       "energy_error": {"median": float(np.median(df)), "max": float(df.max())}}
+        # per cluster: the split-FP32 run's energy error beside the FP64 run's
+        ratio = de / np.maximum(df, 1e-300)
+        out["ds32_over_fp64_energy_error"] = {"median": float(np.median(ratio)),
+                                              "p90": float(np.percentile(ratio, 90)),
+                                              "max": float(ratio.max())}
+        diff = np.abs((e1 - f1) / f1)
+        out["energy_ds32_vs_fp64_at_end"] = {"median": float(np.median(diff)), "max": float(diff.max())}
+    return out
 
 
 KERNEL_SCALARS = {"tstep": (1.0 / 1024,), "sakura": (1.0 / 1024, 1)}
@@ -413,7 +436,12 @@ def main():
             kw[k] = getattr(args, k)
     fn = {"precision": precision_run, "adjoint": adjoint_run, "binaries": binaries_run,
           "ensemble": ensemble_run, "kernels": kernels_run, "integrators": integrators_run}[args.which]
-    print(json.dumps(fn(**kw), default=float))
+    from .clocks import Clocks
+    clocks = Clocks(torch.cuda.current_device())
+    clocks.start()
+    out = fn(**kw)
+    out["clocks"] = clocks.stop()   # SM clock and throttle reasons over the whole run
+    print(json.dumps(out, default=float))
 
 
 if __name__ == "__main__":
