@@ -187,10 +187,13 @@ def adjoint_run(n=16384, steps=64, dt=1.0 / 256, seed=16384, checkpoint_every=8,
 FD_LADDER = (3, 4, 5, 6)
 
 
-def binaries_run(nbg=2048, nbin=64, t_end=1.0 / 16, dt=1.0 / 1024, clight=1e4, pn_order=5, seed=2176):
+def binaries_run(nbg=2048, nbin=64, t_end=1.0 / 16, dt=1.0 / 1024, clight=1e4, pn_order=5, seed=2176,
+                 compare_fp64=True):
     """Plummer background plus hard binaries: Sakura Kepler-drift steps (FP64)
     with a post-Newtonian kick (split FP32 PNAcc) split around them
-    (kick tau/2, Sakura step tau, kick tau/2)."""
+    (kick tau/2, Sakura step tau, kick tau/2).  With compare_fp64 the same
+    run with the FP64 PNAcc gives what the split-FP32 PN bound does to the
+    binaries: the spread of their final separations and of all positions."""
     from .integrator.sakura import sakura_step
     d = plummer_arrays(nbg, 0.0, seed=seed)
     rng = np.random.default_rng(seed + 1)
@@ -220,33 +223,51 @@ def binaries_run(nbg=2048, nbin=64, t_end=1.0 / 16, dt=1.0 / 1024, clight=1e4, p
     extensions.set_precision("float64")
     extensions.clight.pn_order = pn_order
     extensions.clight.clight = clight
-    pn = extensions.PNAcc("CUDA", "ds32")
-    ps = ParticleSystem.from_arrays(**arrays)
-    e0 = energy(ps)
-
-    def pn_kick(ps, tau):
-        pn.calc(ps, ps)
-        ps.vx += ps.pnax * tau
-        ps.vy += ps.pnay * tau
-        ps.vz += ps.pnaz * tau
-
     steps = int(round(t_end / dt))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        pn_kick(ps, dt / 2)
-        ps = sakura_step(ps, dt)
-        pn_kick(ps, dt / 2)
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
+
+    def run(prec):
+        pn = extensions.PNAcc("CUDA", prec)
+        ps = ParticleSystem.from_arrays(**arrays)
+
+        def pn_kick(ps, tau):
+            pn.calc(ps, ps)
+            ps.vx += ps.pnax * tau
+            ps.vy += ps.pnay * tau
+            ps.vz += ps.pnaz * tau
+
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            pn_kick(ps, dt / 2)
+            ps = sakura_step(ps, dt)
+            pn_kick(ps, dt / 2)
+        torch.cuda.synchronize()
+        return ps, time.perf_counter() - t0
+
+    def separations(ps):
+        sep = []
+        for k, h in enumerate(host):
+            j = nbg + k
+            dx = [float(getattr(ps, "r" + ax)[h] - getattr(ps, "r" + ax)[j]) for ax in "xyz"]
+            sep.append(math.sqrt(sum(x * x for x in dx)))
+        return np.array(sep)
+
+    e0 = energy(ParticleSystem.from_arrays(**arrays))
+    ps, wall = run("ds32")
     status = _native.sync_status(torch.cuda.current_stream().cuda_stream)
     e1 = energy(ps)
-    # binary separations after the run
-    sep = []
-    for k, h in enumerate(host):
-        j = nbg + k
-        dx = [float(getattr(ps, "r" + ax)[h] - getattr(ps, "r" + ax)[j]) for ax in "xyz"]
-        sep.append(math.sqrt(sum(x * x for x in dx)))
+    sep = separations(ps)
+    extra = {}
+    if compare_fp64:
+        ps64, wall64 = run("float64")
+        status |= _native.sync_status(torch.cuda.current_stream().cuda_stream)
+        sep64 = separations(ps64)
+        dr = max(float((getattr(ps, "r" + ax) - getattr(ps64, "r" + ax)).abs().max()) for ax in "xyz")
+        extra = {"fp64_pnacc": {"ms_per_step": 1e3 * wall64 / steps,
+                                "rel_energy_error_newtonian": abs((energy(ps64) - e0) / e0)},
+                 "ds32_vs_fp64": {"max_separation_difference_over_a":
+                                      float(np.max(np.abs(sep - sep64) / np.array(semis))),
+                                  "max_position_difference": dr}}
     return {"config": {"background": nbg, "binaries": nbin, "n": n, "a_range": [1e-4, 1e-3],
                        "e": "0.9*sqrt(u)", "eps2": 0.0, "pn_order": pn_order, "clight": clight,
                        "dt": dt, "t_end": t_end, "scheme": "PN kick dt/2, sakura_step dt, PN kick dt/2",
@@ -254,7 +275,8 @@ def binaries_run(nbg=2048, nbin=64, t_end=1.0 / 16, dt=1.0 / 1024, clight=1e4, p
             "steps": steps, "ms_per_step": 1e3 * wall / steps, "kepler_status": status,
             "rel_energy_error_newtonian": abs((e1 - e0) / e0),
             "binary_separation_over_a": {"min": float(min(s / a for s, a in zip(sep, semis))),
-                                         "max": float(max(s / a for s, a in zip(sep, semis)))}}
+                                         "max": float(max(s / a for s, a in zip(sep, semis)))},
+            **extra}
 
 
 def ensemble_run(nclusters=512, steps=16, dt=1.0 / 1024, base_seed=512, compare_fp64=True):
