@@ -922,6 +922,7 @@ template <int IPT_>
 struct AccJerkOrd {
     static constexpr bool ORDERED = true;
     static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 8, PX = 6, PJ = 7;   // PJ: jerk proxy
+    static constexpr int KERNEL = K_ACC_JERK;
     static constexpr int W_FAR = 4, W_NEAR = 5, W_HEAVY = 9;   // relative cost of a 64-j block
     static constexpr int FAR_FOLD_PAIRS = ORD_ACC_FOLD_PAIRS;  // (32-j far folds were 1% slower here)
     static constexpr bool UE2 = true;
@@ -1035,6 +1036,7 @@ template <int IPT_>
 struct AccOrd {
     static constexpr bool ORDERED = true;
     static constexpr int IPT = IPT_, JF = 8, NQ = 4, NP = 4, PX = 3, PJ = -1;
+    static constexpr int KERNEL = K_ACC;
     static constexpr int W_FAR = 2, W_NEAR = 3, W_HEAVY = 6;   // relative cost of a 64-j block
     static constexpr int FAR_FOLD_PAIRS = 16;                  // far blocks fold every 32 j
     static constexpr bool UE2 = true;
@@ -1107,6 +1109,73 @@ struct AccOrd {
     __device__ static void store(const double *p, const PairArgs &a, size_t i) {
         for (int k = 0; k < 3; ++k) a.out[k][i] = p[k];
     }
+};
+
+// Ordered split-FP32 Phi (phi_kernel_common.h:7-31): phi_i = -sum_j m_j / r,
+// r masked to 0 where r2 > 0 fails.  Every term has the same sign, so the
+// sums cannot cancel: no proxy and no recompute.  Far blocks need neither
+// the lo words nor the mask (no pair there has r = 0); near and heavy blocks
+// keep the mask even with a uniform softening, because a self pair's
+// -m / sqrt(e2) is not zero.
+template <int IPT_>
+struct PhiOrd {
+    static constexpr bool ORDERED = true;
+    static constexpr int IPT = IPT_, JF = 8, NQ = 4, NP = 1, PX = -1, PJ = -1;
+    static constexpr int KERNEL = K_PHI;
+    static constexpr int W_FAR = 2, W_NEAR = 3, W_HEAVY = 6;   // relative cost of a 64-j block
+    static constexpr int FAR_FOLD_PAIRS = 16;                  // far blocks fold every 32 j
+    static constexpr bool UE2 = true;
+    struct IS { float2 dh[3], dl[3]; float2 e; float2 p; Comp cp; };
+    __device__ static void load(IS &s, const PairArgs &a, size_t i) {
+        s.e = f2(__double2float_rn(a.I.f[F_E2][i]));
+        s.p = f2(0.f);
+        s.cp = Comp{0.f, 0.f};
+    }
+    // record: {x'h,y'h} {z'h,m} {x'l,y'l} {z'l,e2}
+    __device__ static void write_record(float *r, int lane, const float h[3], const float l[3], const PSet &J,
+                                        size_t j, bool valid) {
+        AccOrd<IPT_>::write_record(r, lane, h, l, J, j, valid);
+    }
+    struct Rec { float4 q[NQ]; };
+    template <int FORM, bool UE>
+    __device__ __forceinline__ static Rec load_rec(const float4 *R) {
+        Rec c;
+        c.q[0] = R[0]; c.q[1] = R[1];
+        c.q[2] = c.q[0]; c.q[3] = c.q[1];
+        if (FORM != ORD_FAR || !UE) c.q[3] = R[3];
+        if (FORM != ORD_FAR) c.q[2] = R[2];
+        return c;
+    }
+    template <int FORM, bool UE>
+    __device__ __forceinline__ static void step(IS (&S)[IPT], const Rec &c, float2 E) {
+        const float4 q0 = c.q[0], q1 = c.q[1], q2 = c.q[2], q3 = c.q[3];
+#pragma unroll
+        for (int u = 0; u < IPT; ++u) {
+            IS &s = S[u];
+            float2 dx, dy, dz;
+            if (FORM == ORD_FAR) {
+                dx = sub2(s.dh[0], lo2(q0)); dy = sub2(s.dh[1], hi2(q0)); dz = sub2(s.dh[2], lo2(q1));
+            } else {
+                dx = add2(sub2(s.dh[0], lo2(q0)), sub2(s.dl[0], lo2(q2)));
+                dy = add2(sub2(s.dh[1], hi2(q0)), sub2(s.dl[1], hi2(q2)));
+                dz = add2(sub2(s.dh[2], lo2(q1)), sub2(s.dl[2], lo2(q3)));
+            }
+            const float2 e2 = UE ? E : add2(s.e, hi2(q3));
+            const float2 ss = fma2(dx, dx, fma2(dy, dy, fma2(dz, dz, e2)));
+            float2 y;
+            if (FORM == ORD_FAR) y = make_float2(rsqrt_hw(ss.x), rsqrt_hw(ss.y));
+            else y = inv_r<FORM == ORD_HEAVY>(ss, dx, dy, dz);
+            s.p = fnma2(hi2(q1), y, s.p);
+        }
+    }
+    __device__ static void fold_acc(IS &s) {
+        comp_add(s.cp, __fadd_rn(s.p.x, s.p.y));
+        s.p = f2(0.f);
+    }
+    __device__ static void fold_jerk(IS &) {}
+    __device__ static void partials(const IS &s, double *p) { p[0] = comp_value(s.cp); }
+    __device__ static void combine(double *acc, const double *p) { acc[0] += p[0]; }
+    __device__ static void store(const double *p, const PairArgs &a, size_t i) { a.out[0][i] = p[0]; }
 };
 
 // Double-single j-data of the exact kernel (ds32_exact), EXACT_JQ float4
@@ -1186,7 +1255,7 @@ __global__ void __launch_bounds__(DS_TILE) ds32_ord_prepare(PSet J, size_t nj, c
         else { h[c] = 0.f; l[c] = 0.f; }
     }
     K::write_record(rec + (p >> 1) * (size_t)(2 * K::JF), (int)(p & 1), h, l, J, j, valid);
-    if (valid) write_exact_record(jd + EXACT_JQ * p, J, j, K::PJ >= 0 ? F_VX : -1);
+    if (K::PX >= 0 && valid) write_exact_record(jd + EXACT_JQ * p, J, j, K::PJ >= 0 ? F_VX : -1);
     if (tile_e2 != nullptr) {   // the tile's common float softening, or NaN
         const unsigned mine = valid ? __float_as_uint(__double2float_rn(J.f[F_E2][j])) : 0u;
         if (q == 0) s_first = mine;   // the tile's first j is always valid
@@ -1420,7 +1489,12 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs o
         const float4 *R = ring + s * TILE_Q;
         const long long jp = u % nju, jt = jp / JSUB;
         const float ue = __fadd_rn(ie2, __ldg(a.tile_e2 + jt));
-        const bool UEok = ue > 1e-20f;   // NaN (not uniform) takes the per-pair softening
+        // ue is NaN unless both tiles' softenings are uniform.  Far blocks
+        // take the uniform value whenever there is one (zero included: no
+        // pair there has r = 0); near blocks only above 1e-20, where a pair
+        // at r = 0 adds exactly nothing without the mask
+        const bool uniform = ue == ue;
+        const bool UEok = ue > 1e-20f;
         const float2 E = f2(ue);
 #pragma unroll 1
         for (int bl = 0; bl < PART_BLOCKS; ++bl) {
@@ -1437,7 +1511,7 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs o
                         const int x = q * DS_THREADS + tid;
                         st[q].dh[c] = f2(rel_single(s_xi[c][x], s_xi[3 + c][x], cc[c]));
                     }
-                if (UEok) ord_block<K, ORD_FAR, true>(st, Rb, E);
+                if (uniform) ord_block<K, ORD_FAR, true>(st, Rb, E);
                 else ord_block<K, ORD_FAR, false>(st, Rb, E);
             } else {
 #pragma unroll
@@ -1467,15 +1541,17 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_ord(DsOrdArgs o
                             if (ii >= ni) return;
                             const size_t i = (size_t)oa.pi[ii];
                             K::store(p, a.p, i);
-                            const double am = sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
-                            bool redo = !(p[K::PX] <= (double)oa.tau * am);
-                            if constexpr (K::PJ >= 0) {
-                                const double jm = sqrt(p[3] * p[3] + p[4] * p[4] + p[5] * p[5]);
-                                redo = redo || !(p[K::PJ] <= (double)oa.tau_jerk * jm);
-                            }
-                            if (redo) {
-                                const int f = atomicAdd(oa.flag_count, 1);
-                                oa.flag_list[f] = (int)i;
+                            if constexpr (K::PX >= 0) {
+                                const double am = sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+                                bool redo = !(p[K::PX] <= (double)oa.tau * am);
+                                if constexpr (K::PJ >= 0) {
+                                    const double jm = sqrt(p[3] * p[3] + p[4] * p[4] + p[5] * p[5]);
+                                    redo = redo || !(p[K::PJ] <= (double)oa.tau_jerk * jm);
+                                }
+                                if (redo) {
+                                    const int f = atomicAdd(oa.flag_count, 1);
+                                    oa.flag_list[f] = (int)i;
+                                }
                             }
                         });
         if (tn >= 0) {
@@ -1882,6 +1958,9 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk_seg(DsS
 // ---------------------------------------------------------------------------
 // Host side.
 // ---------------------------------------------------------------------------
+#ifndef TG_ORD_PHI
+#define TG_ORD_PHI 1   // Phi calls of 2^24 pairs and more take the ordered kernel
+#endif
 #ifndef TG_ORD_UNITS_PER_CTA
 #define TG_ORD_UNITS_PER_CTA 8   // ordered kernel: j-tiles are split until units >= this x CTA slots
 #endif
@@ -2107,9 +2186,16 @@ static cudaError_t run_exact(const PairArgs &p, void *ws, size_t ws_bytes, int s
     return cudaGetLastError();
 }
 
-// The ordered path serves calls of at least 2^24 pairs.
+// The ordered path serves Acc and AccJerk calls of at least 2^24 pairs.
 static bool ord_applies(size_t ni, size_t nj) {
     return ni >= 512 && nj >= 512 && (double)ni * (double)nj >= 16777216.0 && nj < ((size_t)1 << 30);
+}
+// Phi has no cancellation to guard against (every term has one sign), so it
+// takes the ordered kernel for speed alone: from 2^31 pairs, where its
+// cheaper far blocks outweigh the ordering's fixed cost (N = 65536: 1.63 ms
+// against 2.02 ms unordered; N = 16384: 0.25 against 0.17 ms).
+static bool phi_ord_applies(size_t ni, size_t nj) {
+    return TG_ORD_PHI && ord_applies(ni, nj) && (double)ni * (double)nj >= 2147483648.0;
 }
 
 static bool same_sets(const PairArgs &p, int nfields) {
@@ -2208,8 +2294,9 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
     a.tau = ord_tau(p.nj);
     a.tau_jerk = ORD_TAU_JERK_FACTOR * a.tau;
     const size_t smem = (size_t)DS_STAGES * DS_PAIRS * K::NQ * sizeof(float4);
-    ProfRec pr{K::PJ >= 0 ? K_ACC_JERK : K_ACC, nullptr, nullptr};   // AccJerkOrd has a jerk proxy
-    const bool prof = g_prof.load() && cudaEventCreate(&pr.e0) == cudaSuccess &&
+    ProfRec pr{K::KERNEL, nullptr, nullptr};
+    const bool prof = (K::KERNEL == K_ACC || K::KERNEL == K_ACC_JERK) && g_prof.load() &&
+                      cudaEventCreate(&pr.e0) == cudaSuccess &&
                       cudaEventCreate(&pr.e1) == cudaSuccess && cudaEventRecord(pr.e0, s) == cudaSuccess;
     switch (g.jsub) {
         case 8: ds32_ord<K, 8><<<(unsigned)g.grid, DS_THREADS, smem, s>>>(a); break;
@@ -2222,9 +2309,10 @@ static cudaError_t run_ord(const PairArgs &p, int nfields, void *ws, size_t ws_b
         g_prof_rec.push_back(pr);
     }
     // flagged AccJerk particles get both vectors recomputed (a second list
-    // for the acceleration-only ones measured no faster)
-    ds32_exact<K::PJ >= 0 ? EX_ACC_JERK : EX_ACC><<<(unsigned)(sms * 4), EXACT_THREADS, 0, s>>>(p, jd, flags, flags + 64,
-                                                                                        ref_part, ref_ticket);
+    // for the acceleration-only ones measured no faster); Phi has no recompute
+    if constexpr (K::PX >= 0)
+        ds32_exact<K::PJ >= 0 ? EX_ACC_JERK : EX_ACC><<<(unsigned)(sms * 4), EXACT_THREADS, 0, s>>>(
+            p, jd, flags, flags + 64, ref_part, ref_ticket);
     return cudaGetLastError();
 }
 
@@ -2329,7 +2417,9 @@ bool ds32_supported(int kernel) { return kernel != K_SAKURA && kernel >= 0 && ke
 
 size_t ds32_workspace_bytes(int kernel, size_t ni, size_t nj, int sms) {
     switch (kernel) {
-        case K_PHI: return ws_pick<PhiDS<IPT2, REF>, PhiDS<1, REF>>(ni, nj, sms);
+        case K_PHI:
+            if (phi_ord_applies(ni, nj)) return ord_layout<PhiOrd<2>>(ni, nj, sms, false).total();
+            return ws_pick<PhiDS<IPT2, REF>, PhiDS<1, REF>>(ni, nj, sms);
         case K_ACC:
             if (ord_applies(ni, nj)) return ord_layout<AccOrd<2>>(ni, nj, sms, false).total();
             return exact_ws_bytes(nj);
@@ -2346,7 +2436,9 @@ size_t ds32_workspace_bytes(int kernel, size_t ni, size_t nj, int sms) {
 
 cudaError_t launch_ds32(int kernel, const PairArgs &a, void *ws, size_t ws_bytes, int sms, cudaStream_t s) {
     switch (kernel) {
-        case K_PHI: return run_pick<PhiDS<IPT2, REF>, PhiDS<1, REF>>(a, ws, ws_bytes, sms, s);
+        case K_PHI:
+            if (phi_ord_applies(a.ni, a.nj)) return run_ord<PhiOrd<2>>(a, 5, ws, ws_bytes, sms, s);
+            return run_pick<PhiDS<IPT2, REF>, PhiDS<1, REF>>(a, ws, ws_bytes, sms, s);
         case K_ACC:
             if (ord_applies(a.ni, a.nj)) return run_ord<AccOrd<2>>(a, 5, ws, ws_bytes, sms, s);
             return run_exact<EX_ACC>(a, ws, ws_bytes, sms, s);
