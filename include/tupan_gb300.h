@@ -82,8 +82,8 @@ int tg_pair_kernel_time(int kernel, double *ms, long long *launches);
  * magnitudes exceeds tau times its |a| (jerk: 2.5 tau times |j|), tau
  * scaled down with sqrt(nj / 65536) below 65536 j-particles.  The default,
  * 20, holds every particle of a Plummer-Salpeter sphere within 1e-6 of
- * FP64; 10 does so on flattened, multi-cluster and six-decade-mass-range
- * sets as well, at +20% time.  Returns the previous tau, or -1 (unchanged)
+ * FP64; 10 does so on multi-cluster and six-decade-mass-range sets as
+ * well, at +20% time; a flat disk of equal masses needs 5 (4x the time).   Returns the previous tau, or -1 (unchanged)
  * unless 1 <= tau <= 1e6. */
 double tg_set_recompute_threshold(double tau);
 /* Sakura evaluation (no counterpart in the reference; process-wide): 1, the

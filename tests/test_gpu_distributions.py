@@ -6,10 +6,13 @@ acceleration within 1e-6, jerk within 1e-5.
 * a central massive particle (5% of the mass), coincident particles (pairs
   at one position, softened), zero softening, a uniform cube: with the
   default recompute threshold;
-* two clusters 100 length units apart, a flat disk, masses spread over six
-  decades: with tg_set_recompute_threshold(10) (the default, 20, leaves
-  these at 1.0-1.4e-6 in the acceleration at N = 65536);
-* both at N = 16384 and 65536.
+* two clusters 100 length units apart and masses spread over six decades:
+  with tg_set_recompute_threshold(10) (the default, 20, leaves these at
+  1.2-1.4e-6 in the acceleration at N = 65536);
+* a flat disk of equal masses (every particle's forces cancel in the
+  plane): with tg_set_recompute_threshold(5) (20 leaves it at 2.5e-6, 10
+  at 1.4e-6);
+* all at N = 16384 and 65536.
 """
 import numpy as np
 import pytest
@@ -99,10 +102,10 @@ def test_default_threshold(mods, case, n):
 
 
 @pytest.mark.parametrize("n", [16384, 65536])
-@pytest.mark.parametrize("case", ["two_clusters", "disk", "mass_range"])
-def test_threshold_ten(mods, case, n):
+@pytest.mark.parametrize("case,tau", [("two_clusters", 10.0), ("mass_range", 10.0), ("disk", 5.0)])
+def test_lower_threshold(mods, case, tau, n):
     native = mods[0]
-    prev = native.set_recompute_threshold(10.0)
+    prev = native.set_recompute_threshold(tau)
     try:
         check(mods, case, n)
     finally:

@@ -924,7 +924,7 @@ struct AccJerkOrd {
     static constexpr int IPT = IPT_, JF = 12, NQ = 6, NP = 8, PX = 6, PJ = 7;   // PJ: jerk proxy
     static constexpr int KERNEL = K_ACC_JERK;
     static constexpr int W_FAR = 4, W_NEAR = 5, W_HEAVY = 9;   // relative cost of a 64-j block
-    static constexpr int FAR_FOLD_PAIRS = ORD_ACC_FOLD_PAIRS;  // (32-j far folds were 1% slower here)
+    static constexpr int FAR_FOLD_PAIRS = 8;                   // 16 j (32-j far folds were 1% slower here)
     static constexpr bool UE2 = true;
     struct IS { float2 dh[3], dl[3]; float2 u, v, w, e; float2 a[3], j[3]; Comp ca[3], cj[3]; float px, pj; };
     __device__ static void load(IS &s, const PairArgs &a, size_t i) {

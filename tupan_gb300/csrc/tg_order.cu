@@ -3,7 +3,8 @@
 //
 // j-set: sorted by a 31-bit key, (heavy << 30) | Hilbert(x, y, z), so the
 // light particles come first in Hilbert-curve order over 10 bits per axis
-// and the heavy ones (mass above max(m) / 32) follow, also in that order.
+// and the heavy ones (mass above max(m) / 32 and above 16 min(m), so that
+// a set of equal masses has none) follow, also in that order.
 // (A Hilbert curve keeps neighbours in the key adjacent in space, without a
 // Morton curve's jumps at octant boundaries: on a Plummer sphere of 65536
 // particles 84% of (512-i tile, 64-j block) pairs come out far apart, 73%
@@ -29,7 +30,8 @@ namespace {
 
 constexpr int ORD_THREADS = 256;
 constexpr unsigned HEAVY_BIT = 1u << 30;
-constexpr float HEAVY_FRACTION = 1.0f / 32.0f;
+constexpr float HEAVY_FRACTION = 1.0f / 32.0f;   // of the largest mass
+constexpr float HEAVY_OVER_MIN = 16.0f;           // times the smallest mass
 
 __device__ __forceinline__ unsigned f2ord(float f) {
     const unsigned u = __float_as_uint(f);
@@ -39,17 +41,17 @@ __device__ __forceinline__ float ord2f(unsigned u) {
     return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
 }
 
-// scal[0..2] = min x, y, z; scal[3..5] = max; scal[6] = max mass (all as
-// order-preserving unsigned); scal[7] = number of light j.
+// scal[0..2] = min x, y, z; scal[3..5] = max; scal[6] = max mass; scal[8]
+// = min mass (all as order-preserving unsigned); scal[7] = number of light j.
 __global__ void ord_init(unsigned *scal) {
     const int t = threadIdx.x;
-    if (t < 3) scal[t] = 0xffffffffu;
+    if (t < 3 || t == 8) scal[t] = 0xffffffffu;
     else if (t < 8) scal[t] = 0u;
 }
 
 __global__ void ord_bounds(PSet S, size_t n, bool with_mass, unsigned *scal) {
     float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    float mmax = -INFINITY;
+    float mmax = -INFINITY, mmin = INFINITY;
     for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (size_t)gridDim.x * blockDim.x) {
         for (int k = 0; k < 3; ++k) {
             const float x = __double2float_rn(S.f[F_RX + k][p]);
@@ -57,7 +59,7 @@ __global__ void ord_bounds(PSet S, size_t n, bool with_mass, unsigned *scal) {
         }
         if (with_mass) {
             const float m = __double2float_rn(S.f[F_M][p]);
-            if (isfinite(m)) mmax = fmaxf(mmax, m);
+            if (isfinite(m)) { mmax = fmaxf(mmax, m); mmin = fminf(mmin, m); }
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -66,6 +68,7 @@ __global__ void ord_bounds(PSet S, size_t n, bool with_mass, unsigned *scal) {
             hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
         }
         mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
+        mmin = fminf(mmin, __shfl_xor_sync(0xffffffffu, mmin, o));
     }
     if ((threadIdx.x & 31) == 0) {
         for (int k = 0; k < 3; ++k) {
@@ -74,7 +77,10 @@ __global__ void ord_bounds(PSet S, size_t n, bool with_mass, unsigned *scal) {
                 atomicMax(scal + 3 + k, f2ord(hi[k]));
             }
         }
-        if (with_mass && mmax > -INFINITY) atomicMax(scal + 6, f2ord(mmax));
+        if (with_mass && mmax > -INFINITY) {
+            atomicMax(scal + 6, f2ord(mmax));
+            atomicMin(scal + 8, f2ord(mmin));
+        }
     }
 }
 
@@ -126,7 +132,8 @@ __global__ void ord_keys(PSet S, size_t n, bool heavy, const unsigned *scal, uns
         }
         if (span > 0.f && isfinite(span)) scale = 1023.999f / span;
     }
-    const float mcut = (scal[6] == 0u) ? INFINITY : ord2f(scal[6]) * HEAVY_FRACTION;
+    const float mcut = (scal[6] == 0u) ? INFINITY
+                                       : fmaxf(ord2f(scal[6]) * HEAVY_FRACTION, ord2f(scal[8]) * HEAVY_OVER_MIN);
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     unsigned light = 0;
     if (p < n) {
@@ -167,7 +174,7 @@ size_t cub_bytes(size_t n) {
 
 size_t order_workspace_bytes(size_t ni, size_t nj, bool same) {
     const size_t n = ni > nj ? ni : nj;
-    size_t b = align256(8 * sizeof(unsigned));
+    size_t b = align256(16 * sizeof(unsigned));
     b += 4 * align256(nj * sizeof(unsigned));            // j keys in/out, values in/out
     if (!same) b += 4 * align256(ni * sizeof(unsigned)); // i keys in/out, values in/out
     b += align256(cub_bytes(n));
@@ -188,7 +195,7 @@ cudaError_t build_order(const PSet &I, size_t ni, const PSet &J, size_t nj, bool
                         size_t ws_bytes, OrderOut &out, cudaStream_t s) {
     if (order_workspace_bytes(ni, nj, same) > ws_bytes) return cudaErrorInvalidValue;
     char *p = static_cast<char *>(ws);
-    unsigned *scal = reinterpret_cast<unsigned *>(p); p += align256(8 * sizeof(unsigned));
+    unsigned *scal = reinterpret_cast<unsigned *>(p); p += align256(16 * sizeof(unsigned));
     unsigned *kj = reinterpret_cast<unsigned *>(p); p += align256(nj * sizeof(unsigned));
     unsigned *kj2 = reinterpret_cast<unsigned *>(p); p += align256(nj * sizeof(unsigned));
     int *vj = reinterpret_cast<int *>(p); p += align256(nj * sizeof(int));
