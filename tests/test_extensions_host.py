@@ -42,3 +42,13 @@ def test_reference_backend_names_and_symbols(ext):
         ext.get_kernel("acc", "C", "float16")
     with pytest.raises(ValueError):
         ext.get_kernel("no_such_kernel", "C", "float64")
+
+
+def test_ds32x_maps_to_double_single_only_where_it_exists(ext):
+    from tupan_gb300 import _native
+    assert ext.get_kernel("acc", "C", "ds32x").prec == "ds32x"
+    assert ext.kernel_precision("acc", "ds32x") == _native.PREC_DS32X
+    assert ext.kernel_precision("acc_jerk", "ds32x") == _native.PREC_DS32X
+    for name in ("phi", "snap_crackle", "tstep", "pnacc"):
+        assert ext.kernel_precision(name, "ds32x") == _native.PREC_DS32
+    assert ext.kernel_precision("phi", "float64") == _native.PREC_FP64

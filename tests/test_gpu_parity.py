@@ -384,3 +384,22 @@ def test_headline_workload_force_error(ext):
         got = run_kernel(ext, name, "ds32", P, P, ())
         ok, err = within(name, got, want, 1e-6 if name == "phi" else DS32_TOL[name])
         assert ok, (name, err)
+
+
+def test_ds32x_through_the_extension_classes(ext):
+    """prec="ds32x": Acc and AccJerk in double-single arithmetic (~1e-12 of
+    FP64, here held to 1e-10); Phi, which has no double-single form, runs its
+    split-FP32 kernel (DS32_TOL)."""
+    from tupan_gb300.ics import Salpeter, plummer_arrays
+    d = plummer_arrays(5000, 1e-3, imf=Salpeter(0.1, 100.0), seed=7)
+    for f in ("ax", "ay", "az", "jx", "jy", "jz"):
+        d[f] = np.zeros(5000)
+    P = PS(d)
+    for name in ("acc", "acc_jerk"):
+        want = run_kernel(ext, name, "float64", P, P, ())
+        got = run_kernel(ext, name, "ds32x", P, P, ())
+        ok, err = within(name, got, want, 1e-10)
+        assert ok, (name, err)
+    ok, err = within("phi", run_kernel(ext, "phi", "ds32x", P, P, ()), run_kernel(ext, "phi", "float64", P, P, ()),
+                     DS32_TOL["phi"])
+    assert ok, err

@@ -9,8 +9,9 @@ libtupan_gb300.so, reached through a Kernel object with the reference's
 protocol (cty, set_gsize, set_args, map_buffers, run; cffi_backend.py:90-126).
 
 Precision ("prec") is "float64" (FP64 kernels, bit-identical to the reference
-for Phi/Acc/AccJerk/SnapCrackle/Tstep) or "ds32" (split FP32; "float32" is
-accepted as an alias).  The default is "ds32" when `--use_sp` is on the
+for Phi/Acc/AccJerk/SnapCrackle/Tstep), "ds32" (split FP32; "float32" is
+accepted as an alias) or "ds32x" (double-single arithmetic, ~1e-12, for Acc
+and AccJerk; the other kernels run it as "ds32").  The default is "ds32" when `--use_sp` is on the
 command line (as the reference selects single precision), else
 TUPAN_GB300_PREC, else float64; `--use_cl` (the reference's OpenCL switch)
 selects nothing: the only backend is CUDA.
@@ -42,7 +43,16 @@ __all__ = ["Phi", "phi",
            "Clight", "clight", "get_kernel"]
 
 PRECISIONS = {"float64": _native.PREC_FP64, "ds32": _native.PREC_DS32,
-              "float32": _native.PREC_DS32}
+              "float32": _native.PREC_DS32, "ds32x": _native.PREC_DS32X}
+# kernels with a double-single form; the others run "ds32x" as "ds32"
+DS32X_KERNELS = ("acc", "acc_jerk")
+
+
+def kernel_precision(name, prec):
+    """The TG_PREC_* code a kernel runs a precision name at."""
+    if prec == "ds32x" and name not in DS32X_KERNELS:
+        return _native.PREC_DS32
+    return PRECISIONS[prec]
 
 
 class Clight(object):
@@ -161,7 +171,7 @@ class CUDAKernel(object):
         optr = [_ptr(x) for x in a[2 + 2 * nf + ns:]]
         assert len(optr) == no
         stream = _native.current_stream()
-        _native.call_device(self.name, ni, iptr, nj, jptr, sc, optr, PRECISIONS[self.prec], stream)
+        _native.call_device(self.name, ni, iptr, nj, jptr, sc, optr, kernel_precision(self.name, self.prec), stream)
         if self.name == "sakura":
             st = _native.sync_status(stream)
             if st:
