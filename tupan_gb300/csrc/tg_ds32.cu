@@ -1,14 +1,15 @@
 // tg_ds32.cu -- split-FP32 ("double-single") pairwise kernels.
 //
 // Three families:
-//   * the unordered stream-K kernels below (Phi, SnapCrackle, Tstep, PNAcc;
-//     Acc and AccJerk of the segmented ensembles and of the no-allocation
-//     entry point);
-//   * the ordered Acc and AccJerk (ds32_ord, calls of 2^24 pairs and more):
-//     spatially sorted sets, single-float separations on far blocks,
-//     cost-weighted stream-K, recompute of strongly cancelling particles;
-//   * the double-single kernel ds32_exact: Acc and AccJerk below 2^24 pairs,
-//     the Acc adjoint, and that recompute.
+//   * the unordered stream-K kernels below (Phi below 2^31 pairs,
+//     SnapCrackle, Tstep, PNAcc; Acc and AccJerk of the segmented ensembles
+//     and of the no-allocation entry point);
+//   * the ordered kernels (ds32_ord: Acc and AccJerk from 2^24 pairs, Phi
+//     from 2^31): spatially sorted sets, single-float separations on far
+//     blocks, cost-weighted stream-K, recompute of strongly cancelling
+//     particles (Acc, AccJerk);
+//   * the double-single kernel ds32_exact: Acc and AccJerk below 2^24 pairs
+//     and at TG_PREC_DS32X, the Acc adjoint, and that recompute.
 //
 // Data layout in HBM (workspace, written by ds32_prepare once per call):
 //   the j-set as pair-interleaved float records.  Record p holds j = 2p and
@@ -850,10 +851,12 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
 
 
 // ===========================================================================
-// Ordered split-FP32 Acc and AccJerk (single-set calls of >= 2^24 pairs).
+// Ordered split-FP32 Acc and AccJerk (calls of >= 2^24 pairs) and Phi
+// (>= 2^31 pairs).
 //
 // Per call, tg_order.cu sorts the j-set (light particles in Hilbert order,
-// then the heavy ones, mass > max(m) / 32) and the i-set (Hilbert order), and
+// then the heavy ones, mass > max(m) / 32 and > 16 min(m)) and the i-set
+// (Hilbert order), and
 // ds32_ord_prepare writes the j-records in that order with positions
 // relative to the centre c_b of their 64-j block.  The pairwise kernel then
 // decides per 64-j block, from the block's and the i-tile's bounding boxes:
@@ -869,11 +872,12 @@ __global__ void __launch_bounds__(DS_THREADS, TG_DS32_MINB) ds32_streamk(DsArgs 
 // The acceleration's FP32 lane sums are folded into Kahan sums every
 // 2 ORD_ACC_FOLD_PAIRS j (far blocks of Acc: every 2 K::FAR_FOLD_PAIRS j,
 // 32; far terms are of one size within a block, and the longer fold left
-// the errors unchanged while saving 2% of Acc), the jerk's every 64 j.  A per-i proxy of the sum
-// of term magnitudes (the sum of |folded lane sums|) travels with the
-// partials; particles whose proxy exceeds tau |a| (strong cancellation,
-// ord_tau) are listed and their acceleration is recomputed in double-single
-// arithmetic (ds32_exact).
+// the errors unchanged while saving 2% of Acc), the jerk's every 64 j.  A
+// per-i proxy of the sum of term magnitudes (the sum of |folded lane sums|;
+// AccJerk: one for the jerk too) travels with the partials; particles whose
+// proxy exceeds tau |a| (or 2.5 tau |j|: strong cancellation, ord_tau) are
+// listed and recomputed in double-single arithmetic (ds32_exact), AccJerk
+// particles with their jerk.
 // ===========================================================================
 constexpr int ORD_BLOCK = 64;                              // j per block
 constexpr int ORD_BLOCK_PAIRS = ORD_BLOCK / 2;
