@@ -200,9 +200,6 @@ def reference_arm(args, rank, world):
 
 
 # ---------------------------------------------------------------------------
-# clocks sampler
-# ---------------------------------------------------------------------------
-# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 def rel_errors(got, want):
