@@ -10,6 +10,7 @@ logic and update expressions in numpy's evaluation order:
   the slow/fast split and FewBody             tupan/integrator/fewbody.py:13-57
   sakura_step / asakura step                  tupan/integrator/sakura.py:22-50, 100-159
   NREG nreg_x/nreg_v/anreg_step/nreg_step     tupan/integrator/nreg.py:22-165
+  worldline rows (dump_freq)                  tupan/integrator/__init__.py:86-97, hermite.py:318-327, 402-405
 
 With the FP64 oracle kernels (bit-identical to the reference C backend) the
 trajectories are bit-identical to the reference integrators; pinned in
@@ -92,11 +93,23 @@ class Kernels(object):
 
 
 class Base(object):
-    def __init__(self, eta, time, ps, kernels):
+    def __init__(self, eta, time, ps, kernels, dump_freq=None):
         self.eta = eta
         self.t_curr = float(time)
         self.ps = ps
         self.k = kernels
+        # with dump_freq set, `worldline` collects the rows the reference's
+        # dumpper receives: the whole set once before the first step, then
+        # the particles whose time is a multiple of dump_freq * tau
+        self.dump_freq = dump_freq
+        self.worldline = []
+        self.started = False
+
+    def record(self, ps, tau):
+        if self.dump_freq is not None:
+            slc = ps["time"] % (self.dump_freq * tau) == 0
+            if any(slc):
+                self.worldline.append(ps_select(ps, slc))
 
     def get_base_tstep(self, t_end):
         dt = min(abs(t_end) - abs(self.t_curr), abs(self.eta))
@@ -120,8 +133,13 @@ class Base(object):
         ps["tstep"][...] = tau
         ps["time"] += tau
         ps["nstep"] += 1
+        self.record(ps, tau)
 
     def evolve_step(self, t_end):
+        if not self.started:
+            self.started = True
+            if self.dump_freq is not None:
+                self.worldline.append(self.ps.copy())
         tau = self.get_base_tstep(t_end)
         self.ps = self.do_step(self.ps, tau)
 
@@ -336,6 +354,7 @@ class SIA(Base):
             slow["tstep"][...] = tau
             slow["time"] += tau
             slow["nstep"] += 1
+            self.record(slow, tau)
         return ps_join(slow, fast)
 
     def do_step(self, ps, tau):
@@ -433,17 +452,21 @@ class NREG(Base):
         ps["tstep"][...] = self.t_curr - t0
         ps["time"] += tau
         ps["nstep"] += 1
+        self.record(ps, tau)
         return ps
 
 
-def integrator(method, eta, ps, kernels=None, time=0.0):
+def integrator(method, eta, ps, kernels=None, time=0.0, dump_freq=None):
     kernels = kernels or Kernels()
     if method in ("nreg", "anreg"):
-        return NREG(eta, time, ps, method, kernels)
-    if "hermite" in method:
-        return Hermite(eta, time, ps, method, kernels)
-    if method.startswith("sia"):
-        return SIA(eta, time, ps, method, kernels)
-    if "sakura" in method:
-        return Sakura(eta, time, ps, method, kernels)
-    raise ValueError(method)
+        it = NREG(eta, time, ps, method, kernels)
+    elif "hermite" in method:
+        it = Hermite(eta, time, ps, method, kernels)
+    elif method.startswith("sia"):
+        it = SIA(eta, time, ps, method, kernels)
+    elif "sakura" in method:
+        it = Sakura(eta, time, ps, method, kernels)
+    else:
+        raise ValueError(method)
+    it.dump_freq = dump_freq
+    return it

@@ -1,0 +1,399 @@
+"""Snapshot files (tupan_gb300.io, tupan/io/hdf5io.py:23-146) on the CPU.
+
+* The reader against an HDF5 file written by the HDF5 library itself (the
+  MATLAB 7.3 file scipy ships as test data): superblock 0 behind a 512-byte
+  user block, a symbol-table root group, a contiguous float64 dataset and a
+  fixed-length string attribute.
+* The writer: round trips through the reader, appends across sessions
+  (merging the partial last chunk), groups and datasets large enough for
+  multi-level B-trees, and a structure walk that checks the rules the HDF5
+  library applies when it reads a file: nodes allocated at full size and not
+  overlapping, entry counts within 2K, sorted keys that bound their
+  children, local heaps whose free list ends in 1, global heap collections
+  of at least 4 KiB ending in a free-space object, message sizes in
+  multiples of 8, and the end-of-file address.
+* The IO interface with particle sets on the CPU: snapshots (plain and
+  numbered), appends, worldlines, the background writer, the error paths.
+"""
+import os
+import struct
+import warnings
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from tupan_gb300.io import BODIES_DTYPE, IO, class_of, hdf5, pickled_class  # noqa: E402
+from tupan_gb300.particles import ParticleSystem  # noqa: E402
+
+SCIPY_HDF5 = None
+try:
+    import scipy.io.matlab as _m
+    SCIPY_HDF5 = os.path.join(os.path.dirname(_m.__file__), "tests", "data", "testhdf5_7.4_GLNX86.mat")
+except ImportError:
+    pass
+
+
+def test_reader_on_a_library_written_file():
+    if SCIPY_HDF5 is None or not os.path.exists(SCIPY_HDF5):
+        pytest.skip("scipy's HDF5 test file is not installed")
+    with hdf5.File(SCIPY_HDF5) as f:
+        assert f.sb_at == 512 and f.keys() == ["testdouble"]
+        d = f["testdouble"]
+        assert d.shape == (9, 1) and d.dtype == np.float64 and d.layout[0] == "contiguous"
+        assert d.attrs == {"MATLAB_class": "double"}
+        # the MATLAB variable 0:pi/4:2*pi
+        assert np.array_equal(d.read().ravel(), np.arange(9) * (np.pi / 4))
+    _walk(SCIPY_HDF5)                           # the structure rules hold for the library's own file
+
+
+def test_append_to_a_library_written_file(tmp_path):
+    # new groups and a dataset added behind the library's own structures
+    # (addresses relative to the 512-byte user block); the original dataset
+    # and its attribute stay readable
+    if SCIPY_HDF5 is None or not os.path.exists(SCIPY_HDF5):
+        pytest.skip("scipy's HDF5 test file is not installed")
+    p = tmp_path / "lib.hdf5"
+    p.write_bytes(open(SCIPY_HDF5, "rb").read())
+    rows = _rows(100, 0, np.random.default_rng(5))
+    with hdf5.File(str(p), "a") as f:
+        f.require_group("Worldline/particlesystem").append_rows("bodies", rows)
+    with hdf5.File(str(p), "r+") as f:
+        f["Worldline/particlesystem"].append_rows("bodies", rows)
+    _walk(str(p))
+    with hdf5.File(str(p)) as f:
+        assert f.keys() == ["Worldline", "testdouble"]
+        assert np.array_equal(f["testdouble"].read().ravel(), np.arange(9) * (np.pi / 4))
+        assert f["testdouble"].attrs == {"MATLAB_class": "double"}
+        assert np.array_equal(f["Worldline/particlesystem/bodies"].read(), np.concatenate([rows, rows]))
+
+
+# ---- structure walk ----------------------------------------------------------------------
+
+def _walk(path):
+    """Every structure reachable from the superblock, checked; returns the
+    extents [(start, end, what)]."""
+    f = hdf5.File(path)
+    ext = [(f.sb_at - f.base, f.sb_at - f.base + 96, "superblock")]     # addresses relative to the base
+    size = os.path.getsize(path)
+    sb = f._read(-f.base + f.sb_at, 96)
+    eof = struct.unpack_from("<Q", sb, 40)[0]
+    assert eof == size                          # stored as an absolute address
+    ik, lk, ck = f.internal_k, f.leaf_k, f.chunk_k
+
+    def header(addr):
+        pre = f._read(addr, 16)
+        assert pre[0] == 1
+        nmsg, _r, hsize = struct.unpack_from("<HII", pre, 2)
+        ext.append((addr, addr + 16 + hsize, "header"))
+        buf = f._read(addr + 16, hsize)
+        p = count = 0
+        while p < hsize:
+            mtype, msize = struct.unpack_from("<HH", buf, p)
+            assert msize % 8 == 0
+            p += 8 + msize
+            count += 1
+        assert p == hsize and count == nmsg
+
+    def gcol(addr):
+        hdr = f._read(addr, 16)
+        assert hdr[:4] == b"GCOL"
+        n = struct.unpack_from("<Q", hdr, 8)[0]
+        assert n >= 4096
+        buf = f._read(addr, n)
+        p = 16
+        while True:
+            idx = struct.unpack_from("<H", buf, p)[0]
+            osz = struct.unpack_from("<Q", buf, p + 8)[0]
+            if idx == 0:
+                assert p + osz == n            # the free-space object's size includes its header
+                break
+            p += 16 + ((osz + 7) & ~7)
+        ext.append((addr, addr + n, "gcol"))
+
+    def tree(addr, ntype, ksz, node_size, cap, leaf):
+        hdr = f._read(addr, 24)
+        assert hdr[:4] == b"TREE" and hdr[4] == ntype
+        level, n = hdr[5], struct.unpack_from("<H", hdr, 6)[0]
+        assert n <= cap
+        ext.append((addr, addr + node_size, "tree%d" % ntype))
+        body = f._read(addr + 24, n * (ksz + 8) + ksz)
+        keys = [body[i * (ksz + 8):i * (ksz + 8) + ksz] for i in range(n + 1)]
+        kids = [struct.unpack_from("<Q", body, i * (ksz + 8) + ksz)[0] for i in range(n)]
+        out = []
+        for i, c in enumerate(kids):
+            if level:
+                out += tree(c, ntype, ksz, node_size, cap, leaf)
+            else:
+                out.append((keys[i], keys[i + 1], c))
+                leaf(keys[i], keys[i + 1], c)
+        return out
+
+    objs_seen = set()
+
+    def group(addr):
+        msgs = f._messages(addr)
+        header(addr)
+        st = [m for m in msgs if m[0] == hdf5.MSG_SYMTAB][0][3]
+        btree, heap = struct.unpack_from("<QQ", st, 0)
+        h = f._read(heap, 32)
+        assert h[:4] == b"HEAP"
+        hsize, free, daddr = struct.unpack_from("<QQQ", h, 8)
+        ext.append((heap, heap + 32, "heap"))
+        ext.append((daddr, daddr + hsize, "heapdata"))
+        data = f._read(daddr, hsize)
+        assert free == 1 or free + 16 <= hsize
+        while free != 1:                        # the free list ends in 1
+            nxt, fsz = struct.unpack_from("<QQ", data, free)
+            assert fsz >= 16 and free + fsz <= hsize
+            free = nxt
+        name_at = lambda k: hdf5._cstr(data, struct.unpack_from("<Q", k)[0]).encode()
+        children = []
+
+        def snod(lkey, rkey, c):
+            hd = f._read(c, 8)
+            assert hd[:4] == b"SNOD"
+            ns = struct.unpack_from("<H", hd, 6)[0]
+            assert 0 < ns <= 2 * lk
+            ext.append((c, c + 8 + 2 * lk * 40, "snod"))
+            ents = f._read(c + 8, 40 * ns)
+            names = []
+            for i in range(ns):
+                noff, oaddr, ctype = struct.unpack_from("<QQI", ents, 40 * i)
+                nm = hdf5._cstr(data, noff).encode()
+                assert noff % 8 == 0
+                names.append(nm)
+                children.append((oaddr, ctype, ents[40 * i + 24:40 * i + 40]))
+            assert names == sorted(names) and len(set(names)) == ns
+            assert names[0] > name_at(lkey) and names[-1] == name_at(rkey)
+
+        tree(btree, 0, 8, 24 + 2 * ik * 8 + (2 * ik + 1) * 8, 2 * ik, snod)
+        for oaddr, ctype, cache in children:
+            if oaddr in objs_seen:
+                continue
+            objs_seen.add(oaddr)
+            kinds = {m[0] for m in f._messages(oaddr)}
+            if hdf5.MSG_SYMTAB in kinds:
+                if ctype == 1:                  # a cached symbol table matches the message
+                    st2 = [m for m in f._messages(oaddr) if m[0] == hdf5.MSG_SYMTAB][0][3]
+                    assert cache == st2
+                group(oaddr)
+            else:
+                dataset(oaddr)
+        for m in msgs:
+            if m[0] == hdf5.MSG_ATTRIBUTE:
+                attr(m[3])
+
+    def attr(data):
+        assert data[0] == 1
+        nn, nt, ns = struct.unpack_from("<HHH", data, 2)
+        p = 8 + hdf5._pad8(nn)
+        if data[p] & 0x0F == 9:                 # variable-length string: heap reference
+            q = p + hdf5._pad8(nt) + hdf5._pad8(ns)
+            _len, coll, _idx = struct.unpack_from("<IQI", data, q)
+            if coll not in [e[0] for e in ext if e[2] == "gcol"]:
+                gcol(coll)
+
+    def dataset(addr):
+        header(addr)
+        ds = f._load_node("?", addr)
+        for m in f._messages(addr):
+            if m[0] == hdf5.MSG_ATTRIBUTE:
+                attr(m[3])
+        if ds.layout[0] != "chunked" or ds.layout[2] == hdf5.UNDEF:
+            return
+        rank = len(ds.layout[1])
+        ksz = 8 + 8 * (rank + 1)
+        c = ds.layout[1][0]
+
+        def chunk(lkey, rkey, caddr):
+            nb, _mask, off = struct.unpack_from("<IIQ", lkey)
+            roff = struct.unpack_from("<Q", rkey, 8)[0]
+            assert off % c == 0 and roff >= off + c and off < ds.shape[0]
+            ext.append((caddr, caddr + nb, "chunk"))
+
+        leaves = tree(ds.layout[2], 1, ksz, 24 + 2 * ck * 8 + (2 * ck + 1) * ksz, 2 * ck, chunk)
+        offs = [struct.unpack_from("<Q", lk_, 8)[0] for lk_, _r, _c in leaves]
+        assert offs == sorted(offs) and offs == list(range(0, ds.shape[0], c))
+
+    root = f.addr
+    objs_seen.add(root)
+    group(root)
+    ctype, _r, bt, hp = struct.unpack_from("<IIQQ", sb, 72)
+    st = [m for m in f._messages(root) if m[0] == hdf5.MSG_SYMTAB][0][3]
+    assert ctype == 1 and struct.pack("<QQ", bt, hp) == st
+    ext.sort()
+    for (a0, a1, w0), (b0, b1, w1) in zip(ext, ext[1:]):
+        assert a1 <= b0, "%s [%d,%d) overlaps %s [%d,%d)" % (w0, a0, a1, w1, b0, b1)
+    assert ext[-1][1] <= size - f.base
+    f.close()
+    return ext
+
+
+def _rows(n, start, rng):
+    a = np.zeros(n, BODIES_DTYPE)
+    a["id"] = np.arange(start, start + n)
+    for k in ("mass", "rx", "vy", "time"):
+        a[k] = rng.random(n)
+    a["nstep"] = rng.integers(0, 1 << 40, n)
+    return a
+
+
+def test_writer_round_trip_and_appends(tmp_path):
+    p = str(tmp_path / "t.hdf5")
+    rng = np.random.default_rng(7)
+    parts = []
+    with hdf5.File(p, "w") as f:
+        g = f.require_group("Snapshot/particlesystem")
+        g.set_attr("Class", pickled_class("tupan.particles.allparticles", "ParticleSystem"))
+        parts.append(_rows(1000, 0, rng))
+        g.append_rows("bodies", parts[-1]).set_attr("Class", pickled_class("tupan.particles.body", "Bodies"))
+    _walk(p)
+    for k in range(4):                          # appends into the partial last chunk, new groups
+        with hdf5.File(p, "a") as f:
+            g = f.require_group("Snapshot/particlesystem")
+            g.set_attr("Class", pickled_class("tupan.particles.allparticles", "ParticleSystem"))
+            parts.append(_rows(1 + 2000 * k, 1000, rng))
+            g.append_rows("bodies", parts[-1])
+            for j in range(70):
+                f.require_group("Snapshot_%06d" % (70 * k + j))
+        _walk(p)
+    with hdf5.File(p) as f:
+        assert len(f) == 281 and f.keys()[0] == "Snapshot"
+        d = f["Snapshot/particlesystem/bodies"]
+        assert d.chunks == (64,) and d.maxshape == (None,)
+        assert [x[0] for x in d.filters] == [hdf5.FILTER_SHUFFLE, hdf5.FILTER_DEFLATE]
+        assert class_of(d.attrs["Class"]) == ("tupan.particles.body", "Bodies")
+        got = d.read()
+    assert got.dtype == BODIES_DTYPE and np.array_equal(got, np.concatenate(parts))
+    with pytest.raises(ValueError):
+        hdf5.File(p).require_group("x")          # read-only
+
+
+def test_three_level_chunk_tree(tmp_path):
+    # 1024-row chunks of 8-byte records: 4100 chunks need a root over 65
+    # internal nodes over leaves of 64
+    p = str(tmp_path / "big.hdf5")
+    n = 4100 * 1024 - 5
+    a = np.zeros(n, np.dtype([("k", "<u8")]))
+    a["k"] = np.arange(n) // 3
+    with hdf5.File(p, "w") as f:
+        f.append_rows("d", a, level=1)
+    ext = _walk(p)
+    assert sum(1 for e in ext if e[2] == "tree1") == 67 + 1
+    with hdf5.File(p) as f:
+        assert np.array_equal(f["d"].read(), a)
+
+
+def test_empty_and_nested_groups(tmp_path):
+    p = str(tmp_path / "g.hdf5")
+    with hdf5.File(p, "w") as f:
+        f.require_group("a/b/c")
+        f.require_group("a/empty")
+        f.set_attr("note", "root é")
+    _walk(p)
+    with hdf5.File(p, "r+") as f:
+        assert f.attrs["note"] == "root é"
+        assert f["a"].keys() == ["b", "empty"] and len(f["a/empty"]) == 0
+        f["a/b/c"].append_rows("x", np.arange(5, dtype="<f8"))
+    _walk(p)
+    with hdf5.File(p) as f:
+        assert np.array_equal(f["a/b/c/x"][...], np.arange(5.0))
+    with pytest.raises(FileExistsError):
+        hdf5.File(p, "x")
+
+
+# ---- the IO interface ----------------------------------------------------------------------
+
+def _set(n, seed):
+    rng = np.random.default_rng(seed)
+    ps = ParticleSystem(n, device="cpu")
+    for k in ("mass", "eps2", "rx", "ry", "rz", "vx", "vy", "vz", "time", "tstep"):
+        ps.set_array(k, rng.random(n))
+    ps.set_array("nstep", rng.integers(0, 100, n))
+    ps.set_array("id", rng.permutation(n))
+    return ps
+
+
+FIELDS = [k for k, _t in [("id", 0), ("mass", 0), ("eps2", 0), ("rx", 0), ("ry", 0), ("rz", 0), ("vx", 0),
+                          ("vy", 0), ("vz", 0), ("time", 0), ("nstep", 0), ("tstep", 0)]]
+
+
+def _same(a, b):
+    return a.n == b.n and all(torch.equal(getattr(a, k).cpu(), getattr(b, k).cpu()) for k in FIELDS)
+
+
+def test_snapshots_and_worldlines(tmp_path):
+    p = str(tmp_path / "run.hdf5")
+    ps = _set(700, 1)
+    io = IO(p, "a")
+    io.dump_snapshot(ps)
+    io.dump_snapshot(ps[:300], 12)
+    io.dump_snapshot(ps[300:], 12)               # a second dump into a snapshot appends
+    io.dump_worldline(ps[:5])
+    io.dump_worldline(ps[0:0])                   # an empty worldline writes the group only
+    io.dump_worldline(ps[5:9])
+    _walk(p)
+    r = IO(p, "r")
+    assert _same(r.load_snapshot(device="cpu"), ps)
+    assert _same(r.load_snapshot(12, device="cpu"), ps)
+    assert _same(r.load_worldline(device="cpu"), ps[:9])
+    with hdf5.File(p) as f:
+        assert f.keys() == ["Snapshot", "Snapshot_000012", "Worldline"]
+        g = f["Snapshot_000012/particlesystem"]
+        assert class_of(g.attrs["Class"]) == ("tupan.particles.allparticles", "ParticleSystem")
+        assert f["Worldline/particlesystem/bodies"].dtype == BODIES_DTYPE
+
+
+def test_background_writer(tmp_path):
+    p = str(tmp_path / "bg.hdf5")
+    ps = _set(2000, 2)
+    io = IO(p, "a", background=True)
+    for k in range(10):
+        io.dump_worldline(ps[200 * k:200 * (k + 1)])
+    assert _same(io.load_worldline(device="cpu"), ps)     # load waits for the queue
+    io.close()
+    bad = IO(str(tmp_path / "missing_dir" / "x.hdf5"), "a", background=True)
+    bad.dump_worldline(ps)
+    with pytest.raises(FileNotFoundError):
+        bad.flush()
+    bad.close()
+
+
+def test_multi_kind_file_loads_as_one_set(tmp_path):
+    # a reference-layout file with two particle kinds (allparticles.py:29-39)
+    p = str(tmp_path / "kinds.hdf5")
+    rng = np.random.default_rng(3)
+    bodies = _rows(10, 0, rng)
+    sdt = np.dtype(BODIES_DTYPE.descr + [("spinx", "<f8"), ("age", "<f8")])
+    stars = np.zeros(4, sdt)
+    stars["id"] = np.arange(10, 14)
+    stars["mass"] = 2.0
+    stars["age"] = 5.0
+    with hdf5.File(p, "w") as f:
+        g = f.require_group("Snapshot/particlesystem")
+        g.append_rows("stars", stars)
+        g.append_rows("bodies", bodies)
+    ps = IO(p, "r").load_snapshot(device="cpu")
+    assert ps.n == 14
+    assert np.array_equal(ps.id.numpy(), np.arange(14))          # bodies before stars (name order)
+    assert np.array_equal(ps.age.numpy(), [0.0] * 10 + [5.0] * 4)
+
+
+def test_error_paths(tmp_path):
+    ps = _set(3, 0)
+    with pytest.raises(NotImplementedError, match="PSDF"):
+        IO(str(tmp_path / "x.psdf"), "a").dump_snapshot(ps)
+    with pytest.raises(NotImplementedError, match="Unknown format: 'txt'"):
+        IO(str(tmp_path / "x.txt"), "a").dump_worldline(ps)
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        with pytest.raises(SystemExit):
+            IO(str(tmp_path / "none.hdf5"), "r").load_snapshot()
+    assert "No such file" in str(w[0].message)
+    junk = tmp_path / "junk.hdf5"
+    junk.write_bytes(b"\0" * 2048)
+    with pytest.raises(ValueError, match="File not in a supported format"):
+        IO(str(junk), "r").load_snapshot()
+    assert class_of(pickled_class("m.n", "C")) == ("m.n", "C") and class_of("x") is None

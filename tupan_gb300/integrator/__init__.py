@@ -13,6 +13,7 @@ import math
 import sys
 
 import numpy as np
+import torch
 
 from ..lib import extensions
 
@@ -33,13 +34,24 @@ class Base(object):
             extensions.clight.pn_order = pn_order
             extensions.clight.clight = clight
         self.reporter = kwargs.pop("reporter", None)
+        self.viewer = kwargs.pop("viewer", None)
+        self.dumpper = kwargs.pop("dumpper", None)
+        self.dump_freq = kwargs.pop("dump_freq", 1)
+        self.gl_freq = kwargs.pop("gl_freq", 1)
+        self.wl = None
         if kwargs:
             raise TypeError("%s.__init__ received unexpected keyword arguments: %s."
                             % (type(self).__name__, ", ".join(kwargs.keys())))
 
     def initialize(self, t_end):
+        """The report, worldline dump and viewer event of the initial state
+        (hermite.py:318-327 and the same lines of sia.py, sakura.py, nreg.py)."""
         if self.reporter:
             self.reporter.diagnostic_report(self.ps)
+        if self.dumpper:
+            self.dumpper.dump_worldline(self.ps)
+        if self.viewer:
+            self.viewer.show_event(self.ps)
         self.is_initialized = True
 
     def finalize(self, t_end):
@@ -71,14 +83,34 @@ class Base(object):
         ps.tstep.fill_(tau)
         ps.time += tau
         ps.nstep += 1
+        self.record(ps, tau)
+
+    def record(self, ps, tau):
+        """Particles whose time is a multiple of dump_freq * tau join the
+        step's worldline, those at a multiple of gl_freq * tau go to the
+        viewer (hermite.py:402-409).  fmod is exact, and it is zero exactly
+        where the reference's numpy remainder is.  Selecting reads one flag
+        back to the host, and only when a dumpper or a viewer is set."""
+        if self.dumpper and self.wl is not None:
+            slc = torch.fmod(ps.time, self.dump_freq * tau) == 0
+            if bool(slc.any()):
+                self.wl.append(ps[slc])
+        if self.viewer:
+            slc = torch.fmod(ps.time, self.gl_freq * tau) == 0
+            if bool(slc.any()):
+                self.viewer.show_event(ps[slc])
 
     def evolve_step(self, t_end):
         if not self.is_initialized:
             self.initialize(t_end)
+        ps = self.ps
+        self.wl = ps[0:0]          # this step's worldline (integrator/__init__.py:89)
         tau = self.get_base_tstep(t_end)
-        self.ps = self.do_step(self.ps, tau)
+        self.ps = self.do_step(ps, tau)
         if self.reporter:
             self.reporter.diagnostic_report(self.ps)
+        if self.dumpper:
+            self.dumpper.dump_worldline(self.wl)
 
 
 from . import hermite, nreg, sakura, sia  # noqa: E402

@@ -94,4 +94,5 @@ class NREG(Base):
         ps.time += tau
         ps.nstep += 1
         self.t_curr = ps.t_curr
+        self.record(ps, tau)
         return ps

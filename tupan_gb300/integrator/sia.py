@@ -233,10 +233,13 @@ class SIA(Base):
             slow.tstep.fill_(tau)
             slow.time += tau
             slow.nstep += 1
+            self.record(slow, tau)
         return join(slow, fast)
 
     def do_step(self, ps, tau):
-        if self.native_h and self.update_tstep and not self.shared_tstep:
+        # the native recursion has no per-level worldline or viewer hook
+        if (self.native_h and self.update_tstep and not self.shared_tstep
+                and not self.dumpper and not self.viewer):
             return self.native_step(ps, tau)
         return self.recurse(ps, tau, self.evolve, self.scheme.bridge)
 
