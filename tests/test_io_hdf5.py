@@ -381,6 +381,26 @@ def test_multi_kind_file_loads_as_one_set(tmp_path):
     assert np.array_equal(ps.age.numpy(), [0.0] * 10 + [5.0] * 4)
 
 
+def test_numpy_particle_sets(tmp_path):
+    # what the reference's integrators hand their dumpper: a set whose
+    # attributes are numpy arrays (an empty one at the start of a step)
+    class NumpySet(object):
+        pass
+    ps = _set(50, 4)
+    q = NumpySet()
+    q.n = ps.n
+    for k in FIELDS:
+        setattr(q, k, getattr(ps, k).numpy().astype(np.uint64 if k in ("id", "nstep") else np.float64))
+    empty = NumpySet()
+    empty.n = 0
+    p = str(tmp_path / "np.hdf5")
+    io = IO(p, "a")
+    io.dump_worldline(q)
+    io.dump_worldline(empty)
+    io.dump_snapshot(q, 0)
+    assert _same(io.load_worldline(device="cpu"), ps) and _same(io.load_snapshot(0, device="cpu"), ps)
+
+
 def test_error_paths(tmp_path):
     ps = _set(3, 0)
     with pytest.raises(NotImplementedError, match="PSDF"):

@@ -88,9 +88,16 @@ def snapshot_name(snap_number):
 
 class _Staged(object):
     """One dump in flight: the host copies of a set's blocks and the event
-    after which they are valid."""
+    after which they are valid.  A set that is not a tupan_gb300
+    ParticleSystem (the reference's numpy ParticleSystem, given to this IO
+    as the dumpper of the reference's own integrators) is read field by
+    field through its attributes."""
 
     def __init__(self, ps, pinned):
+        self.fields = None
+        if not hasattr(ps, "_layout"):
+            self.fields = _fields_of(ps)
+            return
         lay = ps._layout
         rrows = [lay[k][1] for k, t in BODIES_FIELDS if lay[k][0] == "_real"]
         irows = [lay[k][1] for k, t in BODIES_FIELDS if lay[k][0] == "_int"]
@@ -109,6 +116,8 @@ class _Staged(object):
             self.real, self.int_ = real.cpu(), int_.cpu()
 
     def records(self):
+        if self.fields is not None:
+            return self.fields
         if self.event is not None:
             self.event.synchronize()
         real, int_ = self.real.numpy(), self.int_.numpy()
@@ -122,6 +131,17 @@ class _Staged(object):
                 out[k] = int_[ii].astype(np.uint64)
                 ii += 1
         return out
+
+
+def _fields_of(ps):
+    n = int(getattr(ps, "n", 0) or 0)
+    out = np.zeros(n, dtype=BODIES_DTYPE)
+    if n:
+        for k, _t in BODIES_FIELDS:
+            v = getattr(ps, k)
+            v = v.detach().cpu().numpy() if isinstance(v, torch.Tensor) else np.asarray(v)
+            out[k] = v
+    return out
 
 
 def particles_from_records(arrays, device=None):
