@@ -51,6 +51,18 @@ CHUNK_TARGET_BYTES = 8192                              # chunk size h5py picks f
 DEFLATE_LEVEL = 4                                      # h5py's compression="gzip" default
 
 
+_POOL = []
+
+
+def _pool():
+    """Threads for chunk compression, made on first use."""
+    if not _POOL:
+        from concurrent.futures import ThreadPoolExecutor
+        _POOL.append(ThreadPoolExecutor(max_workers=max(1, min(8, (os.cpu_count() or 2) - 1)),
+                                        thread_name_prefix="hdf5-deflate"))
+    return _POOL[0]
+
+
 def _pad8(n):
     return (n + 7) & ~7
 
@@ -352,9 +364,7 @@ class Dataset(_Node):
         if old % c:                                 # merge into the partial last chunk
             buf[:old % c] = f._read_chunk(self, (first * c,))[:old % c]
         buf[old % c:old % c + len(rows)] = rows
-        for k in range(len(buf) // c):
-            off = (first + k) * c
-            f._write_chunk(self, (off,), buf[k * c:(k + 1) * c])
+        f._write_chunks(self, first * c, buf)
         self.shape = (new,)
         self._dirty = True
 
@@ -795,19 +805,37 @@ class File(Group):
                 out[dst] = chunk[src]
         return out
 
-    def _write_chunk(self, ds, offs, rows):
-        raw = rows.tobytes()
+    def _write_chunks(self, ds, first, buf):
+        """Write the whole chunks of record array `buf`, the first at element
+        offset `first`: the shuffle of all chunks in one array operation,
+        deflate of the chunks on a thread pool (zlib releases the GIL), the
+        stored chunks appended in order."""
+        c = ds.layout[1][0]
+        nch = len(buf) // c
+        s = ds.dtype.itemsize
+        data = np.ascontiguousarray(buf).view(np.uint8).reshape(nch, c * s)
+        level = None
         for fid, _fl, cd in ds.filters:
             if fid == FILTER_SHUFFLE:
-                s = cd[0]
-                n = len(raw) // s
-                raw = np.frombuffer(raw, np.uint8, count=n * s).reshape(n, s).T.tobytes() + raw[n * s:]
+                if cd[0] != s:
+                    raise NotImplementedError("shuffle with an element size other than the record's")
+                data = np.ascontiguousarray(data.reshape(nch, c, s).transpose(0, 2, 1)).reshape(nch, c * s)
             elif fid == FILTER_DEFLATE:
-                raw = zlib.compress(raw, cd[0] if cd else DEFLATE_LEVEL)
+                level = cd[0] if cd else DEFLATE_LEVEL
             else:
                 raise NotImplementedError("writing through filter %d" % fid)
-        addr = self._append(raw)
-        ds._chunks[tuple(offs)] = (addr, len(raw), 0)
+        if level is None:
+            rows = [data[k].tobytes() for k in range(nch)]
+        else:
+            def deflate(lo_hi):
+                return [zlib.compress(data[k].tobytes(), level) for k in range(*lo_hi)]
+            pool = _pool()
+            nb = min(nch, 4 * pool._max_workers)
+            cuts = [(nch * i // nb, nch * (i + 1) // nb) for i in range(nb)]
+            rows = [r for part in (pool.map(deflate, cuts) if nch > 8 else [deflate((0, nch))]) for r in part]
+        for k, raw in enumerate(rows):
+            addr = self._append(raw)
+            ds._chunks[(first + k * c,)] = (addr, len(raw), 0)
 
     # ---- writing metadata
     def _flush(self):

@@ -7,6 +7,7 @@ configurations, each reporting a JSON summary.
     python -m tupan_gb300.runs ensemble       # 512 clusters, Hermite-6, CUDA graph
     python -m tupan_gb300.runs kernels --n N  # per-kernel device time, ds32 and FP64
     python -m tupan_gb300.runs integrators    # ms per step of the integrators, N=256
+    python -m tupan_gb300.runs snapshots      # snapshot/worldline file cost, N=65536 SIA21
 
 All inputs are seeded synthetic Plummer spheres (tupan_gb300.ics).
 """
@@ -433,10 +434,82 @@ def integrators_run(n=256, steps=8, methods="sia21h.dkd,sia21h.kdk,sia44h.kdk,si
     return out
 
 
+def snapshots_run(n=65536, steps=16, dt=1.0 / 1024, seed=20261203):
+    """Cost of the snapshot files (tupan_gb300.io) for the Plummer-Salpeter
+    set of the precision configuration: one snapshot dump written
+    synchronously and through the background writer (time until the call
+    returns, and until the file is complete), the load back (checked
+    bit-equal), and the wall-clock ms per step of sia21s.kdk in split FP32
+    without a dumpper, with a per-step worldline dump written synchronously,
+    and with it written by the background writer (dump_freq 1: every
+    particle is dumped every step)."""
+    import os
+    import shutil
+    import tempfile
+    from .io import IO
+    extensions.set_precision("ds32")
+    d = plummer_arrays(n, 1e-3, imf=Salpeter(0.1, 100.0), seed=seed)
+    tmp = tempfile.mkdtemp(prefix="tupan_snap_")
+    out = {"config": {"n": n, "steps": steps, "dt": dt, "seed": seed, "method": "sia21s.kdk",
+                      "precision": "ds32", "record_bytes": 96}}
+    try:
+        ps = ParticleSystem.from_arrays(**d)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ps._real[:, :8].cpu()                       # the process's first device-to-host copy
+        t1 = time.perf_counter()
+        IO(os.path.join(tmp, "warm.hdf5"), "a").dump_snapshot(ps)
+        t2 = time.perf_counter()
+        out["first_d2h_ms"], out["first_dump_ms"] = (t1 - t0) * 1e3, (t2 - t1) * 1e3
+        for tag, bg in (("sync", False), ("background", True)):
+            path = os.path.join(tmp, tag + ".hdf5")
+            io = IO(path, "a", background=bg)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            io.dump_snapshot(ps)
+            t1 = time.perf_counter()
+            io.flush()
+            t2 = time.perf_counter()
+            io.close()
+            out["dump_" + tag] = {"call_ms": (t1 - t0) * 1e3, "complete_ms": (t2 - t0) * 1e3,
+                                  "file_bytes": os.path.getsize(path)}
+        t0 = time.perf_counter()
+        back = IO(os.path.join(tmp, "sync.hdf5"), "r").load_snapshot()
+        torch.cuda.synchronize()
+        out["load_ms"] = (time.perf_counter() - t0) * 1e3
+        out["load_bit_equal"] = all(torch.equal(getattr(back, k), getattr(ps, k))
+                                    for k in ("id", "mass", "rx", "ry", "rz", "vx", "vy", "vz"))
+        out["ms_per_step"] = {}
+        for tag, bg in (("no dumpper", None), ("worldline sync", False), ("worldline background", True)):
+            ps = ParticleSystem.from_arrays(**d)
+            io = None if bg is None else IO(os.path.join(tmp, "wl_%s.hdf5" % tag.split()[-1]), "a",
+                                            background=bg)
+            kw = {} if io is None else {"dumpper": io, "dump_freq": 1}
+            integ = Integrator(dt, 0.0, ps, method="sia21s.kdk", **kw)
+            integ.evolve_step(dt)
+            if io is not None:
+                io.flush()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for k in range(steps):
+                integ.evolve_step((k + 2) * dt)
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            if io is not None:
+                io.close()
+            t2 = time.perf_counter()
+            out["ms_per_step"][tag] = (t1 - t0) / steps * 1e3
+            if io is not None:
+                out["ms_per_step"][tag + ", writes drained"] = (t2 - t0) / steps * 1e3
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("which", choices=["precision", "adjoint", "binaries", "ensemble", "kernels",
-                                            "integrators"])
+                                            "integrators", "snapshots"])
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--reps", type=int, default=None, help="kernels: timed calls per kernel")
@@ -453,7 +526,8 @@ def main():
         if getattr(args, k) is not None:
             kw[k] = getattr(args, k)
     fn = {"precision": precision_run, "adjoint": adjoint_run, "binaries": binaries_run,
-          "ensemble": ensemble_run, "kernels": kernels_run, "integrators": integrators_run}[args.which]
+          "ensemble": ensemble_run, "kernels": kernels_run, "integrators": integrators_run,
+          "snapshots": snapshots_run}[args.which]
     from .clocks import Clocks
     clocks = Clocks(torch.cuda.current_device())
     clocks.start()
