@@ -56,6 +56,9 @@ def test_append_to_a_library_written_file(tmp_path):
         pytest.skip("scipy's HDF5 test file is not installed")
     p = tmp_path / "lib.hdf5"
     p.write_bytes(open(SCIPY_HDF5, "rb").read())
+    with hdf5.File(str(p), "a") as f:            # opened for writing, nothing changed:
+        f.keys()
+    assert p.read_bytes() == open(SCIPY_HDF5, "rb").read()     # not a byte written
     rows = _rows(100, 0, np.random.default_rng(5))
     with hdf5.File(str(p), "a") as f:
         f.require_group("Worldline/particlesystem").append_rows("bodies", rows)
@@ -269,6 +272,16 @@ def test_writer_round_trip_and_appends(tmp_path):
     assert got.dtype == BODIES_DTYPE and np.array_equal(got, np.concatenate(parts))
     with pytest.raises(ValueError):
         hdf5.File(p).require_group("x")          # read-only
+    # rows of other fields are stored by field name, the dataset's others zero
+    part = np.zeros(3, np.dtype([("rx", "<f8"), ("id", "<u8")]))
+    part["rx"], part["id"] = 1.5, 9
+    with hdf5.File(p, "a") as f:
+        f["Snapshot/particlesystem"].append_rows("bodies", part)
+        with pytest.raises(ValueError):
+            f["Snapshot/particlesystem"].append_rows("bodies", np.zeros(1, [("nope", "<f8")]))
+    with hdf5.File(p) as f:
+        tail = f["Snapshot/particlesystem/bodies"].read()[-3:]
+    assert (tail["rx"] == 1.5).all() and (tail["id"] == 9).all() and (tail["mass"] == 0).all()
 
 
 def test_three_level_chunk_tree(tmp_path):

@@ -352,7 +352,16 @@ class Dataset(_Node):
         if self.layout[0] != "chunked" or len(self.shape) != 1 or self.maxshape[0] is not None:
             raise NotImplementedError("appending needs a 1-D chunked dataset of unlimited extent")
         if rows.dtype != self.dtype:
-            rows = rows.astype(self.dtype)
+            if rows.dtype.names is None or self.dtype.names is None:
+                rows = rows.astype(self.dtype)
+            else:                                   # fields by name; the dataset's others are zero
+                extra = set(rows.dtype.names) - set(self.dtype.names)
+                if extra:
+                    raise ValueError("fields %s are not in dataset %s" % (sorted(extra), self.name))
+                conv = np.zeros(len(rows), dtype=self.dtype)
+                for k in rows.dtype.names:
+                    conv[k] = rows[k]
+                rows = conv
         if self._chunks is None:
             self._chunks = f._read_chunk_index(self)
         c = self.layout[1][0]
@@ -387,18 +396,23 @@ class File(Group):
         self._parents = {}
         self._gheaps = {}
         self._closed = False
-        if create:
-            Group.__init__(self, self, "/", None)
-            self._children = {}
-            self.sb_at, self.base = 0, 0
-            self.leaf_k, self.internal_k, self.chunk_k = GROUP_LEAF_K, GROUP_INTERNAL_K, CHUNK_K
-            self._sb_version = 0
-            self._fh.write(b"\0" * 96)              # superblock, written on close
-            self._eof = 96
-        else:
-            self._read_superblock()
-            if self._writable:
-                self._load_tree(self)
+        self._changed = create          # nothing is written back unless something changed
+        try:
+            if create:
+                Group.__init__(self, self, "/", None)
+                self._children = {}
+                self.sb_at, self.base = 0, 0
+                self.leaf_k, self.internal_k, self.chunk_k = GROUP_LEAF_K, GROUP_INTERNAL_K, CHUNK_K
+                self._sb_version = 0
+                self._fh.write(b"\0" * 96)              # superblock, written on close
+                self._eof = 96
+            else:
+                self._read_superblock()
+                if self._writable:
+                    self._load_tree(self)
+        except BaseException:
+            self._fh.close()
+            raise
 
     # ---- context / lifetime
     def __enter__(self):
@@ -408,14 +422,16 @@ class File(Group):
         self.close()
 
     def _check_writable(self):
+        """Called before every change."""
         if not self._writable:
             raise ValueError("file %s is open read-only" % self.path)
+        self._changed = True
 
     def close(self):
         if self._closed:
             return
         try:
-            if self._writable:
+            if self._writable and self._changed:
                 self._flush()
         finally:
             self._fh.close()
@@ -469,7 +485,6 @@ class File(Group):
             p = 28
         base, _free, eof, _drv = struct.unpack_from("<QQQQ", sb, p)
         self.sb_at, self.base = at, base
-        self._sb_root_at = p + 32                   # root symbol-table entry, from the superblock start
         _name, root_addr = struct.unpack_from("<QQ", sb, p + 32)
         Group.__init__(self, self, "/", root_addr)
         self._eof = max(eof, size) - base          # the stored end of file is absolute
