@@ -82,7 +82,7 @@ def _walk(path):
     size = os.path.getsize(path)
     sb = f._read(-f.base + f.sb_at, 96)
     eof = struct.unpack_from("<Q", sb, 40)[0]
-    assert eof == size                          # stored as an absolute address
+    assert eof <= size                          # stored as an absolute address; an aborted write may trail it
     ik, lk, ck = f.internal_k, f.leaf_k, f.chunk_k
 
     def header(addr):
@@ -229,7 +229,7 @@ def _walk(path):
     ext.sort()
     for (a0, a1, w0), (b0, b1, w1) in zip(ext, ext[1:]):
         assert a1 <= b0, "%s [%d,%d) overlaps %s [%d,%d)" % (w0, a0, a1, w1, b0, b1)
-    assert ext[-1][1] <= size - f.base
+    assert ext[-1][1] <= eof - f.base
     f.close()
     return ext
 
@@ -254,6 +254,7 @@ def test_writer_round_trip_and_appends(tmp_path):
         g.append_rows("bodies", parts[-1]).set_attr("Class", pickled_class("tupan.particles.body", "Bodies"))
     _walk(p)
     for k in range(4):                          # appends into the partial last chunk, new groups
+        assert os.path.getsize(p) == struct.unpack_from("<Q", open(p, "rb").read(48), 40)[0]
         with hdf5.File(p, "a") as f:
             g = f.require_group("Snapshot/particlesystem")
             g.set_attr("Class", pickled_class("tupan.particles.allparticles", "ParticleSystem"))
@@ -282,6 +283,15 @@ def test_writer_round_trip_and_appends(tmp_path):
     with hdf5.File(p) as f:
         tail = f["Snapshot/particlesystem/bodies"].read()[-3:]
     assert (tail["rx"] == 1.5).all() and (tail["id"] == 9).all() and (tail["mass"] == 0).all()
+    # an exception inside the block leaves the file at its previous state
+    with pytest.raises(RuntimeError):
+        with hdf5.File(p, "a") as f:
+            f["Snapshot/particlesystem"].append_rows("bodies", _rows(500, 0, rng))
+            f.require_group("never")
+            raise RuntimeError("stop")
+    _walk(p)
+    with hdf5.File(p) as f:
+        assert "never" not in f and len(f["Snapshot/particlesystem/bodies"]) == len(got) + 3
 
 
 def test_three_level_chunk_tree(tmp_path):

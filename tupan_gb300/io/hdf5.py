@@ -18,7 +18,9 @@ absent) and "r+" (read/write) load the group tree eagerly and write on
 file, object headers that already exist are patched in place (their
 dataspace, layout and symbol-table messages keep their encoded sizes), and
 the superblock is rewritten last.  Space held by replaced B-trees, heaps and
-rewritten partial chunks is not reused.
+rewritten partial chunks is not reused.  A file left through an exception
+(`with` block) or opened without a change is not written back: new chunks
+may trail its end, unreferenced, and its structures are those it had.
 
 Read as well (written by other producers of the same format version):
 contiguous and compact storage, fixed-length strings, array datatypes and
@@ -418,8 +420,12 @@ class File(Group):
     def __enter__(self):
         return self
 
-    def __exit__(self, *exc):
-        self.close()
+    def __exit__(self, exc_type, exc, tb):
+        if exc_type is None:
+            self.close()
+        else:                       # leave the file as it was: nothing linked, nothing patched
+            self._changed = False
+            self.close()
 
     def _check_writable(self):
         """Called before every change."""
