@@ -14,6 +14,9 @@
   multiples of 8, and the end-of-file address.
 * The IO interface with particle sets on the CPU: snapshots (plain and
   numbered), appends, worldlines, the background writer, the error paths.
+* PSDF streams (tupan/io/psdfio.py): the text PyYAML writes for the
+  `!Particle` mappings, block and flow sequences read back, exact round
+  trips and the conversions between the two formats.
 """
 import os
 import struct
@@ -426,8 +429,6 @@ def test_numpy_particle_sets(tmp_path):
 
 def test_error_paths(tmp_path):
     ps = _set(3, 0)
-    with pytest.raises(NotImplementedError, match="PSDF"):
-        IO(str(tmp_path / "x.psdf"), "a").dump_snapshot(ps)
     with pytest.raises(NotImplementedError, match="Unknown format: 'txt'"):
         IO(str(tmp_path / "x.txt"), "a").dump_worldline(ps)
     with warnings.catch_warnings(record=True) as w:
@@ -440,3 +441,61 @@ def test_error_paths(tmp_path):
     with pytest.raises(ValueError, match="File not in a supported format"):
         IO(str(junk), "r").load_snapshot()
     assert class_of(pickled_class("m.n", "C")) == ("m.n", "C") and class_of("x") is None
+
+
+# ---- PSDF streams ------------------------------------------------------------------------
+
+def test_psdf_text_is_what_pyyaml_writes(tmp_path):
+    # one particle, the keys of psdfio.py's Stream.to_yaml in sorted order,
+    # floats as PyYAML represents them
+    from tupan_gb300.io import psdf
+    cols = {"id": np.array([3]), "mass": np.array([0.5]), "eps2": np.array([1e-3]),
+            "rx": np.array([1.0]), "ry": np.array([-2.5]), "rz": np.array([1e-5]),
+            "vx": np.array([0.0]), "vy": np.array([np.inf]), "vz": np.array([-0.0]),
+            "time": np.array([0.125])}
+    assert psdf.dump_text(cols) == (
+        "--- !Particle\neps2: 0.001\nid: 3\nm: 0.5\nr:\n- 1.0\n- -2.5\n- 1.0e-05\n"
+        "t: 0.125\ntype: body\nv:\n- 0.0\n- .inf\n- -0.0\n")
+    assert [psdf.yaml_float(x) for x in (1e20, 2.5e-300, float("nan"), -np.inf)] == \
+        ["1.0e+20", "2.5e-300", ".nan", "-.inf"]
+
+
+def test_psdf_reads_block_and_flow_forms():
+    from tupan_gb300.io import psdf
+    text = ("%YAML 1.1\n# a comment line\n--- !Particle\nid: 0\nm: 1.0\nt: 0.0\nr: [1.0, 2.0, 3.0]  # flow form\n"
+            "v:\n  - 0.5\n  - -0.5\n  - 0\npot: -1.25\neps2: 0.0\n---\nid: 1\nm: 2.0\nt: 0.0\n"
+            "type: blackhole\nr: [0, 0, 0]\nv: [0, 0, 1.0e-3]\npot: -2.0\neps2: 0.0\n...\n")
+    cols = psdf.columns_from_docs(psdf.parse_text(text))
+    assert list(cols["id"]) == [0, 1] and list(cols["mass"]) == [1.0, 2.0]
+    assert list(cols["rz"]) == [3.0, 0.0] and list(cols["vz"]) == [0.0, 1e-3]
+    assert list(cols["phi"]) == [-1.25, -2.0] and "ax" not in cols
+    with pytest.raises(ValueError):
+        psdf.columns_from_docs(psdf.parse_text("---\nid: 0\nm: 1.0\n"))        # no r, v, t
+    with pytest.raises(ValueError):
+        psdf.columns_from_docs(psdf.parse_text("---\nid: 0\nm: 1\nt: 0\nr: [0,0,0]\nv: [0,0,0]\ntype: gas\n"))
+
+
+def test_psdf_round_trip_and_conversions(tmp_path):
+    ps = _set(40, 9)
+    ps.register_auxiliary_attribute("phi", "real")
+    ps.phi.copy_(-ps.mass * 3.0)
+    for k in ("ax", "ay", "az"):
+        ps.register_auxiliary_attribute(k, "real")
+        getattr(ps, k).copy_(ps.rx * 0.5)
+    p = str(tmp_path / "s.psdf")
+    io = IO(p, "w")
+    io.dump_snapshot(ps[:25])
+    IO(p, "a").dump_worldline(ps[25:])              # appends to the stream
+    back = IO(p, "r").load_snapshot(device="cpu")
+    for k in ("id", "mass", "eps2", "rx", "ry", "rz", "vx", "vy", "vz", "time", "phi", "ax", "az"):
+        assert torch.equal(getattr(back, k), getattr(ps, k)), k
+    IO(p, "r").to_hdf5()                             # s.hdf5 beside it
+    h = IO(str(tmp_path / "s.hdf5"), "r")
+    assert torch.equal(h.load_snapshot(device="cpu").rx, ps.rx)
+    os.remove(p)
+    h.to_psdf()                                      # and back
+    assert torch.equal(IO(p, "r").load_snapshot(device="cpu").vz, ps.vz)
+    with pytest.raises(ValueError, match="already in 'psdf'"):
+        IO(p, "r").to_psdf()
+    with pytest.raises(ValueError, match="already in 'hdf5'"):
+        h.to_hdf5()

@@ -26,11 +26,19 @@ every step does not wait for zlib; `flush()` (called by every load, by
 `close()` and at interpreter exit) waits for the queued writes and re-raises
 the first error of the writer.
 
-Differences from the reference: PSDF (YAML) streams are not written or read
-(the reference's PSDF path cannot run: tupan/io/__init__.py:28 constructs
-PSDFIO with two arguments, psdfio.py:22 takes one, and PSDFIO has neither
-dump_snapshot nor dump_worldline); `load_worldline` returns the worldline's
-rows (the reference's raises NotImplementedError, hdf5io.py:117-121); a set
+A ".psdf" name selects a PSDF stream (tupan_gb300.io.psdf): one YAML
+`!Particle` document per particle with the keys of psdfio.py's
+`Stream.to_yaml` (position, velocity, mass, id, time, softening, and the
+acceleration and potential when the set carries them); dumps append to the
+stream, a load reads every particle in it, and `to_psdf` / `to_hdf5`
+convert between the two formats as hdf5io.py:134-146 and psdfio.py:46-57 do.
+
+Differences from the reference: the reference's PSDF path cannot run as it
+stands (tupan/io/__init__.py:28 constructs PSDFIO with two arguments,
+psdfio.py:22 takes one; PSDFIO has neither dump_snapshot nor
+dump_worldline); here it follows the mapping `Stream.to_yaml` and
+`Stream.from_loader` define.  `load_worldline` returns the worldline's rows
+(the reference's raises NotImplementedError, hdf5io.py:117-121).  A set
 with several particle kinds loads as one set, the kinds' datasets in name
 order, fields a kind lacks set to zero.
 """
@@ -45,7 +53,7 @@ import warnings
 import numpy as np
 import torch
 
-from . import hdf5
+from . import hdf5, psdf
 
 __all__ = ["IO", "BODIES_FIELDS"]
 
@@ -87,24 +95,32 @@ def snapshot_name(snap_number):
 # ---- device <-> records ----------------------------------------------------------------
 
 class _Staged(object):
-    """One dump in flight: the host copies of a set's blocks and the event
-    after which they are valid.  A set that is not a tupan_gb300
-    ParticleSystem (the reference's numpy ParticleSystem, given to this IO
-    as the dumpper of the reference's own integrators) is read field by
-    field through its attributes."""
+    """One dump in flight: host copies of the named attributes of a set and
+    the event after which they are valid.  A tupan_gb300 ParticleSystem is
+    gathered on the device (one index_select per block) and copied into
+    pinned host buffers asynchronously; any other set (the reference's numpy
+    ParticleSystem, given to this IO as the dumpper of the reference's own
+    integrators) is read attribute by attribute."""
 
-    def __init__(self, ps):
-        self.fields = None
+    def __init__(self, ps, names):
+        self.names = list(names)
+        self.cols = None
+        self.event = None
         if not hasattr(ps, "_layout"):
-            self.fields = _fields_of(ps)
+            n = int(getattr(ps, "n", 0) or 0)
+            self.cols = {}
+            for k in self.names:
+                v = getattr(ps, k) if n else np.zeros(0)
+                self.cols[k] = v.detach().cpu().numpy() if isinstance(v, torch.Tensor) else np.asarray(v)
             return
         lay = ps._layout
-        rrows = [lay[k][1] for k, t in BODIES_FIELDS if lay[k][0] == "_real"]
-        irows = [lay[k][1] for k, t in BODIES_FIELDS if lay[k][0] == "_int"]
+        self.rnames = [k for k in self.names if lay[k][0] == "_real"]
+        self.inames = [k for k in self.names if lay[k][0] == "_int"]
         dev = ps._real.device
-        real = ps._real.index_select(0, torch.tensor(rrows, device=dev))
-        int_ = ps._int.index_select(0, torch.tensor(irows, device=dev))
-        self.event = None
+        real = ps._real.index_select(0, torch.tensor([lay[k][1] for k in self.rnames], device=dev,
+                                                     dtype=torch.int64))
+        int_ = ps._int.index_select(0, torch.tensor([lay[k][1] for k in self.inames], device=dev,
+                                                    dtype=torch.int64))
         if dev.type == "cuda":
             # pinned host buffers: on the Grace host a process's first copy
             # into pageable memory took 4 s, into pinned memory 0.1 s
@@ -117,41 +133,45 @@ class _Staged(object):
         else:
             self.real, self.int_ = real.cpu(), int_.cpu()
 
+    def columns(self):
+        """name -> host numpy array"""
+        if self.cols is None:
+            if self.event is not None:
+                self.event.synchronize()
+            real, int_ = self.real.numpy(), self.int_.numpy()
+            self.cols = {k: real[i] for i, k in enumerate(self.rnames)}
+            self.cols.update({k: int_[i] for i, k in enumerate(self.inames)})
+        return self.cols
+
     def records(self):
-        if self.fields is not None:
-            return self.fields
-        if self.event is not None:
-            self.event.synchronize()
-        real, int_ = self.real.numpy(), self.int_.numpy()
-        out = np.empty(real.shape[1], dtype=BODIES_DTYPE)
-        ri = ii = 0
+        """The Bodies records (BODIES_DTYPE) of the staged columns."""
+        cols = self.columns()
+        n = len(cols["id"])
+        out = np.empty(n, dtype=BODIES_DTYPE)
         for k, t in BODIES_FIELDS:
-            if t == "<f8":
-                out[k] = real[ri]
-                ri += 1
-            else:
-                out[k] = int_[ii].astype(np.uint64)
-                ii += 1
+            out[k] = cols[k].astype(np.uint64) if t == "<u8" else cols[k]
         return out
 
 
-def _fields_of(ps):
-    n = int(getattr(ps, "n", 0) or 0)
-    out = np.zeros(n, dtype=BODIES_DTYPE)
-    if n:
-        for k, _t in BODIES_FIELDS:
-            v = getattr(ps, k)
-            v = v.detach().cpu().numpy() if isinstance(v, torch.Tensor) else np.asarray(v)
-            out[k] = v
-    return out
+def particles_from_columns(cols, device=None):
+    """A ParticleSystem from name -> 1-D numpy arrays: the Bodies fields and
+    any other numeric field as an auxiliary attribute."""
+    from ..particles import ParticleSystem
+    n = len(cols["id"]) if "id" in cols else len(next(iter(cols.values())))
+    ps = ParticleSystem(n, device=device)
+    for k, v in cols.items():
+        v = np.asarray(v)
+        if v.dtype.kind in "iu":
+            ps.set_array(k, torch.from_numpy(v.astype(np.int64)))
+        elif v.dtype.kind == "f":
+            ps.set_array(k, torch.from_numpy(v.astype(np.float64)))
+    return ps
 
 
 def particles_from_records(arrays, device=None):
-    """A ParticleSystem from record arrays (one per particle kind): the Bodies
-    fields, plus any other numeric field as an auxiliary attribute."""
-    from ..particles import ParticleSystem
+    """A ParticleSystem from record arrays (one per particle kind), the kinds
+    concatenated; a field a kind lacks is zero for its particles."""
     arrays = [a for a in arrays if len(a)]
-    n = sum(len(a) for a in arrays)
     names = []
     for a in arrays:
         names += [k for k in a.dtype.names if k not in names]
@@ -163,14 +183,10 @@ def particles_from_records(arrays, device=None):
                 parts.append(np.asarray(a[k]).reshape(len(a), -1)[:, 0] if a[k].ndim > 1 else np.asarray(a[k]))
             else:
                 parts.append(np.zeros(len(a)))
-        cols[k] = np.concatenate(parts) if parts else np.zeros(0)
-    ps = ParticleSystem(n, device=device)
-    for k, v in cols.items():
-        if v.dtype.kind in "iu":
-            ps.set_array(k, torch.from_numpy(v.astype(np.int64)))
-        elif v.dtype.kind == "f":
-            ps.set_array(k, torch.from_numpy(v.astype(np.float64)))
-    return ps
+        cols[k] = np.concatenate(parts)
+    if not cols:
+        cols = {k: np.zeros(0, dtype=np.dtype(t)) for k, t in BODIES_FIELDS}
+    return particles_from_columns(cols, device)
 
 
 # ---- the writer thread -----------------------------------------------------------------
@@ -235,9 +251,7 @@ class IO(object):
         if fname.endswith(".hdf5"):
             return "hdf5"
         if fname.endswith(".psdf"):
-            raise NotImplementedError(
-                "PSDF (YAML) streams are not supported: the reference's PSDF path "
-                "cannot run and no YAML library is available; use '.hdf5'")
+            return "psdf"
         raise NotImplementedError("Unknown format: '{}'. Choose from: {}".format(
             fname.rpartition('.')[-1], self.PROVIDED_FORMATS))
 
@@ -264,18 +278,31 @@ class IO(object):
             self._writer = None
 
     def _dump(self, base, ps):
-        self._format()
-        staged = _Staged(ps)
+        fmt = self._format()
         fname, fmode = self.fname, self.fmode
+        if fmt == "psdf":
+            lay = getattr(ps, "_layout", None)
+            extra = [k for k in psdf.VECTORS["a"] + ("phi",)
+                     if (k in lay if lay is not None else hasattr(ps, k))]
+            if len([k for k in extra if k != "phi"]) != 3:
+                extra = [k for k in extra if k == "phi"]
+            staged = _Staged(ps, [k for k, _t in BODIES_FIELDS] + extra)
 
-        def job():
-            rows = staged.records()
-            with hdf5.File(fname, fmode) as f:
-                g = f.require_group(base + "/" + GROUP_NAME)
-                g.set_attr("Class", pickled_class(*SYSTEM_CLASS))
-                if len(rows):
-                    ds = g.append_rows(MEMBER_NAME, rows)
-                    ds.set_attr("Class", pickled_class(*MEMBER_CLASSES[MEMBER_NAME]))
+            def job():
+                text = psdf.dump_text(staged.columns())
+                with open(fname, "w" if fmode == "w" else "a") as fobj:
+                    fobj.write(text)
+        else:
+            staged = _Staged(ps, [k for k, _t in BODIES_FIELDS])
+
+            def job():
+                rows = staged.records()
+                with hdf5.File(fname, fmode) as f:
+                    g = f.require_group(base + "/" + GROUP_NAME)
+                    g.set_attr("Class", pickled_class(*SYSTEM_CLASS))
+                    if len(rows):
+                        ds = g.append_rows(MEMBER_NAME, rows)
+                        ds.set_attr("Class", pickled_class(*MEMBER_CLASSES[MEMBER_NAME]))
         self._submit(job)
 
     def _load(self, base, device):
@@ -284,6 +311,10 @@ class IO(object):
             warnings.warn("No such file or directory: '{}'".format(self.fname), stacklevel=3)
             sys.exit()
         try:
+            if self._format() == "psdf":
+                with open(self.fname) as fobj:
+                    return particles_from_columns(psdf.columns_from_docs(psdf.parse_text(fobj.read())),
+                                                  device)
             with hdf5.File(self.fname, "r") as f:
                 top = f[base]
                 groups = top.values()
@@ -291,18 +322,21 @@ class IO(object):
                     raise ValueError("group %s is empty" % base)
                 group = groups[0]                   # hdf5io.py:81
                 arrays = [ds.read() for ds in group.values() if isinstance(ds, hdf5.Dataset)]
+        except NotImplementedError:
+            raise
         except Exception as exc:
             logger.exception(str(exc))
             raise ValueError("File not in a supported format.")
         return particles_from_records(arrays, device)
 
-    # -- tupan/io/__init__.py:22-73
+    # -- tupan/io/__init__.py:22-113
     def dump_snapshot(self, ps, snap_number=None):
-        """hdf5io.py:51-72"""
+        """hdf5io.py:51-72; a PSDF stream has no snapshot groups: the
+        particles are appended to it."""
         self._dump(snapshot_name(snap_number), ps)
 
     def load_snapshot(self, snap_number=None, device=None):
-        """hdf5io.py:74-95"""
+        """hdf5io.py:74-95; for a PSDF stream, every particle in it."""
         return self._load(snapshot_name(snap_number), device)
 
     def dump_worldline(self, wl):
@@ -315,9 +349,20 @@ class IO(object):
         return self._load("Worldline", device)
 
     def to_psdf(self):
-        self._format()
-        raise NotImplementedError("PSDF (YAML) streams are not supported")
+        """An HDF5 file's snapshot (or, without one, its worldline) as a PSDF
+        stream beside it (hdf5io.py:134-146)."""
+        if self._format() != "hdf5":
+            raise ValueError("This file is already in 'psdf' format!")
+        try:
+            ps = self.load_snapshot(device="cpu")
+        except ValueError:
+            ps = self.load_worldline(device="cpu")
+        IO(self.fname[:-len(".hdf5")] + ".psdf", "w").dump_snapshot(ps)
 
     def to_hdf5(self):
-        self._format()
-        raise ValueError("This file is already in 'hdf5' format!")
+        """A PSDF stream as the snapshot of an HDF5 file beside it
+        (psdfio.py:46-57)."""
+        if self._format() != "psdf":
+            raise ValueError("This file is already in 'hdf5' format!")
+        ps = self.load_snapshot(device="cpu")
+        IO(self.fname[:-len(".psdf")] + ".hdf5", "w").dump_snapshot(ps)
