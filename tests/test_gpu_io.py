@@ -2,7 +2,8 @@
 
 * Snapshots of a 65536-particle Plummer-Salpeter set round-trip bit-exactly,
   through the synchronous path and through the background writer (pinned
-  copies, encoding on the writer thread).
+  copies, encoding on the writer thread); a PSDF stream of a set with its
+  potential does too.
 * Worldlines: the GPU integrators with a dumpper write the rows the
   reference's dumpper receives -- the whole set before the first step, then
   per step the particles whose time is a multiple of dump_freq * tau
@@ -56,6 +57,19 @@ def test_snapshot_round_trip_65536(mods, tmp_path, background):
         assert torch.equal(getattr(back, k), getattr(ps, k)), k
     wl = r.load_worldline()
     assert torch.equal(wl.rx, ps.rx[:1000])
+
+
+def test_psdf_round_trip_from_the_device(mods, tmp_path):
+    _integ, io, ParticleSystem = mods
+    from tupan_gb300 import ics
+    from tupan_gb300.lib import extensions
+    ps = ParticleSystem.from_arrays(**ics.plummer_arrays(1000, 1e-2, seed=3))
+    extensions.phi.calc(ps, ps)                     # registers phi on the set
+    path = str(tmp_path / "s.psdf")
+    io.IO(path, "w", background=True).dump_snapshot(ps)
+    back = io.IO(path, "r").load_snapshot()
+    for k in FIELDS[:10] + ("phi",):
+        assert torch.equal(getattr(back, k), getattr(ps, k)), k
 
 
 @pytest.mark.parametrize("method,dump_freq", [("ahermite4", 1), ("ahermite4", 4), ("sia21s.kdk", 2),

@@ -380,6 +380,9 @@ def test_background_writer(tmp_path):
         io.dump_worldline(ps[200 * k:200 * (k + 1)])
     assert _same(io.load_worldline(device="cpu"), ps)     # load waits for the queue
     io.close()
+    q = str(tmp_path / "bg2.hdf5")
+    IO(q, "a", background=True).dump_snapshot(ps)        # queued by an object never flushed
+    assert _same(IO(q, "r").load_snapshot(device="cpu"), ps)
     bad = IO(str(tmp_path / "missing_dir" / "x.hdf5"), "a", background=True)
     bad.dump_worldline(ps)
     with pytest.raises(FileNotFoundError):

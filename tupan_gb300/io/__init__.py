@@ -24,7 +24,8 @@ the chunks on a thread pool.  With `background=True` the encoding,
 compression and file writes run on a writer thread, so an integrator that dumps its worldline
 every step does not wait for zlib; `flush()` (called by every load, by
 `close()` and at interpreter exit) waits for the queued writes and re-raises
-the first error of the writer.
+the first error of the writer; a load also waits for the writes other IO
+objects have queued for the same file.
 
 A ".psdf" name selects a PSDF stream (tupan_gb300.io.psdf): one YAML
 `!Particle` document per particle with the keys of psdfio.py's
@@ -261,6 +262,7 @@ class IO(object):
             return
         if self._writer is None:
             self._writer = _Writer()
+            self._writer.path = os.path.abspath(self.fname)
             _writers.append(self._writer)
         self._writer.submit(job)
 
@@ -307,6 +309,10 @@ class IO(object):
 
     def _load(self, base, device):
         self.flush()
+        path = os.path.abspath(self.fname)
+        for w in list(_writers):            # dumps other IO objects queued for this file
+            if w.path == path:
+                w.flush()
         if not os.path.exists(self.fname):
             warnings.warn("No such file or directory: '{}'".format(self.fname), stacklevel=3)
             sys.exit()
