@@ -192,7 +192,8 @@ def _walk(path):
                 attr(m[3])
 
     def attr(data):
-        assert data[0] == 1
+        if data[0] != 1:                        # what this walk follows: v1 heap references
+            return
         nn, nt, ns = struct.unpack_from("<HHH", data, 2)
         p = 8 + hdf5._pad8(nn)
         if data[p] & 0x0F == 9:                 # variable-length string: heap reference
@@ -502,3 +503,78 @@ def test_psdf_round_trip_and_conversions(tmp_path):
         IO(p, "r").to_psdf()
     with pytest.raises(ValueError, match="already in 'hdf5'"):
         h.to_hdf5()
+
+
+def test_reader_paths_the_writer_does_not_make(tmp_path):
+    # objects assembled here message by message, as other writers of the
+    # same format version lay them out: contiguous and compact storage, a
+    # big-endian float, a version-2 dataspace, a version-2 compound with an
+    # array member and a fixed string, the Fletcher-32 filter through a
+    # version-2 pipeline message, version-2 and -3 attributes, and an object
+    # header whose attribute sits in a continuation block
+    p = str(tmp_path / "hand.hdf5")
+
+    def msg(mtype, data, flags=0):
+        data = data + b"\0" * (hdf5._pad8(len(data)) - len(data))
+        return struct.pack("<HHB3x", mtype, len(data), flags) + data
+
+    def header(f, msgs):
+        body = b"".join(msgs)
+        return f._append(struct.pack("<BxHII4x", 1, len(msgs), 1, len(body)) + body)
+
+    be_f4 = bytes([0x11, 0x21, 31, 0]) + struct.pack("<IHHBBBBI", 4, 0, 32, 23, 8, 0, 23, 127)
+    f8 = hdf5._encode_dtype(np.dtype("<f8"))
+    arr3 = bytes([0x2A, 0, 0, 0]) + struct.pack("<I", 24) + bytes([1, 0, 0, 0]) + struct.pack("<II", 3, 0) + f8
+    s4 = bytes([0x13, 0, 0, 0]) + struct.pack("<I", 4)
+    comp = (bytes([0x26, 2, 0, 0]) + struct.pack("<I", 28) + b"pos\0\0\0\0\0" + struct.pack("<I", 0) + arr3
+            + b"tag\0\0\0\0\0" + struct.pack("<I", 24) + s4)
+    cdt = np.dtype({"names": ["pos", "tag"], "formats": [("<f8", (3,)), "S4"], "offsets": [0, 24],
+                    "itemsize": 28})
+    recs = np.zeros(5, cdt)
+    recs["pos"] = np.arange(15.0).reshape(5, 3)
+    recs["tag"] = [b"ab", b"cd", b"ef", b"gh", b"ij"]
+    with hdf5.File(p, "w") as f:
+        # contiguous big-endian float32 (2, 3), dataspace version 2
+        data = (np.arange(6).reshape(2, 3) / 4).astype(">f4")
+        daddr = f._append(data.tobytes())
+        attr3 = (struct.pack("<BBHHHB", 3, 0, 5, 8, 8, 0) + b"unit\0" + bytes([0x13, 0, 0, 0])
+                 + struct.pack("<I", 3) + bytes([1, 0, 0, 0, 0, 0, 0, 0]) + b"kpc")
+        block = msg(hdf5.MSG_ATTRIBUTE, attr3)
+        cont = f._append(block)
+        contig = header(f, [msg(hdf5.MSG_DATASPACE, bytes([2, 2, 0, 1]) + struct.pack("<QQ", 2, 3)),
+                            msg(hdf5.MSG_DATATYPE, be_f4, 1),
+                            msg(hdf5.MSG_LAYOUT, struct.pack("<BBQQ", 3, 1, daddr, data.nbytes)),
+                            msg(hdf5.MSG_CONTINUATION, struct.pack("<QQ", cont, len(block)))])
+        # compact int16 (4,), version-2 attribute with three int32 values
+        i2 = np.array([-1, 2, -3, 4], "<i2")
+        attr2 = (struct.pack("<BBHHH", 2, 0, 5, 12, 16) + b"dims\0" + hdf5._encode_dtype(np.dtype("<i4"))
+                 + bytes([1, 1, 0, 0, 0, 0, 0, 0]) + struct.pack("<Q", 3) + np.array([7, 8, 9], "<i4").tobytes())
+        compact = header(f, [msg(hdf5.MSG_DATASPACE, bytes([1, 1, 0, 0, 0, 0, 0, 0]) + struct.pack("<Q", 4)),
+                             msg(hdf5.MSG_DATATYPE, hdf5._encode_dtype(np.dtype("<i2")), 1),
+                             msg(hdf5.MSG_LAYOUT, struct.pack("<BBH", 3, 0, i2.nbytes) + i2.tobytes()),
+                             msg(hdf5.MSG_ATTRIBUTE, attr2)])
+        # chunked compound, 2-record chunks, Fletcher-32 (checksum appended, not checked)
+        entries = []
+        for k in range(3):
+            chunk = np.zeros(2, cdt)
+            part = recs[2 * k:2 * k + 2]
+            chunk[:len(part)] = part
+            raw = chunk.tobytes() + b"\x12\x34\x56\x78"
+            entries.append(((2 * k,), (f._append(raw), len(raw), 0)))
+        bt = f._write_chunk_btree(entries, 2, 28)
+        pipe = struct.pack("<BB", 2, 1) + struct.pack("<HHH", hdf5.FILTER_FLETCHER32, 1, 0)
+        chunked = header(f, [msg(hdf5.MSG_DATASPACE, bytes([1, 1, 1, 0, 0, 0, 0, 0]) + struct.pack("<QQ", 5, hdf5.UNDEF)),
+                             msg(hdf5.MSG_DATATYPE, comp, 1),
+                             msg(hdf5.MSG_LAYOUT, struct.pack("<BBBQII", 3, 2, 2, bt, 2, 28)),
+                             msg(hdf5.MSG_PIPELINE, pipe, 1)])
+        f._entries().update({"contig": contig, "compact": compact, "chunked": chunked})
+        f._mark_dirty()
+    _walk(p)
+    with hdf5.File(p) as f:
+        c = f["contig"]
+        assert c.shape == (2, 3) and c.dtype == np.dtype(">f4") and np.array_equal(c.read(), data)
+        assert c.attrs == {"unit": "kpc"}
+        assert np.array_equal(f["compact"].read(), i2)
+        assert list(f["compact"].attrs["dims"]) == [7, 8, 9]
+        got = f["chunked"].read()
+        assert got.dtype == cdt and np.array_equal(got, recs)
