@@ -817,13 +817,31 @@ class File(Group):
         if ds._chunks is None:
             ds._chunks = self._read_chunk_index(ds)
         cdims = ds.layout[1]
+        csize = int(np.prod(cdims))
         out = np.zeros(shape, dtype=dt)
-        for offs in ds._chunks:
-            chunk = self._read_chunk(ds, offs).reshape(cdims)
-            dst = tuple(slice(o, min(o + c, s)) for o, c, s in zip(offs, cdims, shape))
-            src = tuple(slice(0, d.stop - d.start) for d in dst)
-            if all(d.stop > d.start for d in dst):
-                out[dst] = chunk[src]
+        # the chunks inside the extent, read in file order, then unfiltered
+        # on the thread pool (zlib releases the GIL) and placed
+        items = sorted(((ent[0], offs, ent) for offs, ent in ds._chunks.items()
+                        if all(o < s for o, s in zip(offs, shape))))
+        raws = [self._read(addr, ent[1]) for addr, _offs, ent in items]
+
+        def decode(lo_hi):
+            return [self._unfilter(ds, raws[k], items[k][2][2]) for k in range(*lo_hi)]
+        nch = len(items)
+        if nch > 8:
+            pool = _pool()
+            nb = min(nch, 4 * pool._max_workers)
+            parts = pool.map(decode, [(nch * i // nb, nch * (i + 1) // nb) for i in range(nb)])
+        else:
+            parts = [decode((0, nch))]
+        k = 0
+        for part in parts:
+            for raw in part:
+                offs = items[k][1]
+                k += 1
+                chunk = np.frombuffer(raw, dtype=dt, count=csize).reshape(cdims)
+                dst = tuple(slice(o, min(o + c, s)) for o, c, s in zip(offs, cdims, shape))
+                out[dst] = chunk[tuple(slice(0, d.stop - d.start) for d in dst)]
         return out
 
     def _write_chunks(self, ds, first, buf):
