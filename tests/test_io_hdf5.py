@@ -578,3 +578,54 @@ def test_reader_paths_the_writer_does_not_make(tmp_path):
         assert list(f["compact"].attrs["dims"]) == [7, 8, 9]
         got = f["chunked"].read()
         assert got.dtype == cdt and np.array_equal(got, recs)
+
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = os.path.join(ROOT, "baseline", "_ref")
+
+REF_CHILD = r"""
+import sys
+import numpy as np
+sys.path.insert(0, %(ref)r)
+sys.path.insert(1, %(root)r)
+import tupan.lib
+import tupan_gb300.lib.extensions as backend
+tupan.lib.extensions = backend
+sys.modules["tupan.lib.extensions"] = backend
+from tupan.particles.allparticles import ParticleSystem
+from tupan_gb300.io import IO
+ps = ParticleSystem(nstars=5)
+ps.rx[...] = np.arange(5.0) + 0.25
+ps.mass[...] = 0.2
+ps.stars.age[...] = 3.0
+IO(%(path)r, "a").dump_snapshot(ps, 2)
+IO(%(path)r, "a").dump_worldline(ps)
+IO(%(path)r, "a").dump_worldline(type(ps)())
+"""
+
+
+def test_reference_particle_sets_keep_their_kinds(tmp_path):
+    # the reference's own ParticleSystem handed to this IO (as its
+    # integrators hand their dumpper): each kind's dataset holds that kind's
+    # get_state() records under its own Class, as hdf5io.py:51-66 stores them
+    import subprocess
+    import sys
+    if not os.path.isdir(os.path.join(REF, "tupan", "particles")):
+        pytest.skip("no installed reference tree (baseline/_ref)")
+    path = str(tmp_path / "ref.hdf5")
+    env = dict(os.environ, HOME=str(tmp_path))
+    r = subprocess.run([sys.executable, "-c", REF_CHILD % {"ref": REF, "root": ROOT, "path": path}],
+                       capture_output=True, text=True, env=env, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    _walk(path)
+    with hdf5.File(path) as f:
+        g = f["Snapshot_000002/particlesystem"]
+        assert g.keys() == ["stars"]
+        assert class_of(g.attrs["Class"]) == ("tupan.particles.allparticles", "ParticleSystem")
+        assert class_of(g["stars"].attrs["Class"]) == ("tupan.particles.star", "Stars")
+        rec = g["stars"].read()
+        assert rec.dtype.names[:12] == BODIES_DTYPE.names and "metallicity" in rec.dtype.names
+        assert list(rec["rx"]) == [0.25, 1.25, 2.25, 3.25, 4.25] and (rec["age"] == 3.0).all()
+    back = IO(path, "r").load_snapshot(2, device="cpu")
+    assert back.n == 5 and torch.equal(back.age, torch.full((5,), 3.0, dtype=torch.float64))
+    assert IO(path, "r").load_worldline(device="cpu").n == 5

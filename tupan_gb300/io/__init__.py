@@ -15,7 +15,11 @@ shuffle+deflate compressed, with its own "Class" attribute.  Dumping into an
 existing snapshot or worldline appends rows, as the reference's
 `store_dset` does.  The Class attributes hold the protocol-0 pickle text of
 the reference's classes (what h5py stores there); reading parses the class
-name from that text and never unpickles it.
+name from that text and never unpickles it.  A particle set of the
+reference's own classes (its numpy ParticleSystem, handed to this IO as the
+dumpper of its integrators) is stored as the reference stores it: one
+dataset per particle kind ("bodies", "stars", "blackholes", "sphs") of that
+kind's `get_state()` records, each with its own class.
 
 The particles live on the GPU: a dump gathers the record fields of the set on
 the device, copies them into pinned host memory in one asynchronous transfer
@@ -294,6 +298,20 @@ class IO(object):
                 text = psdf.dump_text(staged.columns())
                 with open(fname, "w" if fmode == "w" else "a") as fobj:
                     fobj.write(text)
+        elif not hasattr(ps, "_layout") and isinstance(getattr(ps, "members", None), dict):
+            # the reference's ParticleSystem: one dataset per particle kind
+            # with that kind's own records, as hdf5io.py:51-66 stores them
+            group = type(ps).__name__.lower()
+            gcls = pickled_class(type(ps).__module__, type(ps).__name__)
+            kinds = [(key, pickled_class(type(obj).__module__, type(obj).__name__), obj.get_state())
+                     for key, obj in sorted(ps.members.items()) if obj.n]
+
+            def job():
+                with hdf5.File(fname, fmode) as f:
+                    g = f.require_group(base + "/" + group)
+                    g.set_attr("Class", gcls)
+                    for key, cls, rows in kinds:
+                        g.append_rows(key, rows).set_attr("Class", cls)
         else:
             staged = _Staged(ps, [k for k, _t in BODIES_FIELDS])
 
