@@ -629,3 +629,29 @@ def test_reference_particle_sets_keep_their_kinds(tmp_path):
     back = IO(path, "r").load_snapshot(2, device="cpu")
     assert back.n == 5 and torch.equal(back.age, torch.full((5,), 3.0, dtype=torch.float64))
     assert IO(path, "r").load_worldline(device="cpu").n == 5
+
+
+def test_worldline_selection_matches_numpy_remainder():
+    # Base.record selects with torch.fmod; the reference with numpy's %:
+    # zero at exactly the same times, for either sign of the step
+    from tupan_gb300.integrator import Base
+
+    class Dumpper(object):
+        def __init__(self):
+            self.sets = []
+
+        def dump_worldline(self, wl):
+            self.sets.append(wl)
+
+    rng = np.random.default_rng(11)
+    tau = 2.0 ** -7
+    t = np.concatenate([np.arange(64) * tau, rng.random(64), np.arange(64) * (tau / 3), [0.1, 0.3, 1e-300]])
+    for sign in (1.0, -1.0):
+        for freq in (1, 2, 4, 3):
+            ps = ParticleSystem(len(t), device="cpu")
+            ps.set_array("time", sign * t)
+            b = Base(sign * tau, 0.0, ps, dumpper=Dumpper(), dump_freq=freq)
+            b.wl = ps[0:0]
+            b.record(ps, sign * tau)
+            want = np.nonzero(np.remainder(sign * t, freq * sign * tau) == 0)[0]
+            assert np.array_equal(b.wl.id.numpy(), want), (sign, freq)
