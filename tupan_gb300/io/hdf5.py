@@ -54,15 +54,21 @@ DEFLATE_LEVEL = 4                                      # h5py's compression="gzi
 
 
 _POOL = []
+POOL_THREADS = max(1, min(8, (os.cpu_count() or 2) - 1))
 
 
 def _pool():
-    """Threads for chunk compression, made on first use."""
+    """Threads for chunk (de)compression, made on first use."""
     if not _POOL:
         from concurrent.futures import ThreadPoolExecutor
-        _POOL.append(ThreadPoolExecutor(max_workers=max(1, min(8, (os.cpu_count() or 2) - 1)),
-                                        thread_name_prefix="hdf5-deflate"))
+        _POOL.append(ThreadPoolExecutor(max_workers=POOL_THREADS, thread_name_prefix="hdf5-deflate"))
     return _POOL[0]
+
+
+def _batches(n):
+    """[lo, hi) ranges splitting n items into about four per pool thread."""
+    nb = max(1, min(n, 4 * POOL_THREADS))
+    return [(n * i // nb, n * (i + 1) // nb) for i in range(nb)]
 
 
 def _pad8(n):
@@ -829,9 +835,7 @@ class File(Group):
             return [self._unfilter(ds, raws[k], items[k][2][2]) for k in range(*lo_hi)]
         nch = len(items)
         if nch > 8:
-            pool = _pool()
-            nb = min(nch, 4 * pool._max_workers)
-            parts = pool.map(decode, [(nch * i // nb, nch * (i + 1) // nb) for i in range(nb)])
+            parts = _pool().map(decode, _batches(nch))
         else:
             parts = [decode((0, nch))]
         k = 0
@@ -868,10 +872,8 @@ class File(Group):
         else:
             def deflate(lo_hi):
                 return [zlib.compress(data[k].tobytes(), level) for k in range(*lo_hi)]
-            pool = _pool()
-            nb = min(nch, 4 * pool._max_workers)
-            cuts = [(nch * i // nb, nch * (i + 1) // nb) for i in range(nb)]
-            rows = [r for part in (pool.map(deflate, cuts) if nch > 8 else [deflate((0, nch))]) for r in part]
+            parts = _pool().map(deflate, _batches(nch)) if nch > 8 else [deflate((0, nch))]
+            rows = [r for part in parts for r in part]
         for k, raw in enumerate(rows):
             addr = self._append(raw)
             ds._chunks[(first + k * c,)] = (addr, len(raw), 0)
