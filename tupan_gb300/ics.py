@@ -14,6 +14,12 @@ Random numbers come from numpy.random.Generator(PCG64(seed)).
 The Salpeter IMF draws dN/dm ~ m^-2.35 on [mlow, mhigh] by inverse CDF; the
 reference's IMF class refuses mlow < 0.4 (ics/imf.py:85-88), so this one is
 used for the [0.1, 100] range of the precision workload.
+
+`IMF` has the reference's mass functions (ics/imf.py:67-112: equal mass,
+Salpeter 1955, Padoan et al. 2007, Parravano et al. 2011), each normalised
+over its own mass range and sampled by rejection under its peak from a
+log-uniform proposal; drawn from numpy's global random state (rng=None)
+they give the reference's samples for the same seed.
 """
 import numpy as np
 
@@ -32,6 +38,62 @@ class Salpeter(object):
 class EqualMass(object):
     def sample(self, n, rng):
         return np.ones(n)
+
+
+class IMFSample(object):
+    """A mass function f(m) restricted to [mlow, mhigh] inside the range
+    [min_mlow, max_mhigh] it is defined on (tupan/ics/imf.py:20-64): f is
+    normalised by the integral of f(m)/m over the whole range, its peak is
+    located on that range, and a sample keeps the log-uniform proposals m
+    with u * peak < f(m), u uniform, from batches that grow until one
+    batch holds n accepted masses."""
+
+    def __init__(self, func, min_mlow, max_mhigh, mlow, mhigh):
+        from scipy.integrate import quad
+        from scipy.optimize import fminbound
+        if mlow < min_mlow or mhigh > max_mhigh:
+            raise ValueError("Mass range outer of limits [{0}:{1}].".format(min_mlow, max_mhigh))
+        norm = quad(lambda m: func(m) / m, min_mlow, max_mhigh)[0]
+        self.func = lambda m: func(m) / norm
+        self.mpeak = float(fminbound(lambda m: -self.func(m), min_mlow, max_mhigh, xtol=1.0e-8))
+        self.peak = self.func(self.mpeak)
+        self.mlow, self.mhigh = mlow, mhigh
+        self.min_mlow, self.max_mhigh = min_mlow, max_mhigh
+
+    def sample(self, n, rng=None):
+        r = np.random if rng is None else rng
+        size, kept = n, np.empty(0)
+        while len(kept) < n:
+            u = r.uniform(0.0, self.peak, size=size)
+            m = np.exp(r.uniform(np.log(self.mlow), np.log(self.mhigh), size=size))
+            kept = m[u < self.func(m)]
+            size *= int(1 + n / max(len(kept), 1))
+        return kept[:n]
+
+
+class IMF(object):
+    """The reference's mass functions (tupan/ics/imf.py:67-112)."""
+
+    @staticmethod
+    def equalmass():
+        return IMFSample(lambda m: (1.0 + m) - m, 0.1, 10.0, 1.0, 1.0)
+
+    @staticmethod
+    def salpeter1955(mlow, mhigh):
+        return IMFSample(lambda m: m ** (-1.35), 0.4, 120.0, mlow, mhigh)
+
+    @staticmethod
+    def padoan2007(mlow, mhigh):
+        from scipy.special import erf
+        gamma, m_ch, sigma = 1.4, 1.0, 1.8
+        return IMFSample(lambda m: (m ** (-gamma)) * (1.0 + erf((4.0 * np.log(m / m_ch) + sigma ** 2)
+                                                              / (np.sqrt(8.0) * sigma))),
+                         0.004, 120.0, mlow, mhigh)
+
+    @staticmethod
+    def parravano2011(mlow, mhigh):
+        return IMFSample(lambda m: (m ** (-1.35)) * (1.0 - np.exp(-(m / 0.35) ** (0.51 + 1.35))),
+                         0.004, 120.0, mlow, mhigh)
 
 
 def plummer_positions(n, rng, mfrac=0.999):
