@@ -4,8 +4,9 @@ Restates the generators of tupan/ics/plummer.py:21-221 (Plummer.set_pos:
 mass-stratified radii r = (m^(-2/3) - 1)^(-1/2) with mfrac = 0.999;
 set_vel: |v| = sqrt(-2 q phi) with q drawn from the triangular density
 2(1 - q) by pairwise rejection; per-particle eps2 = eps^2 / 2 for constant
-softening; then com_to_origin, to_nbody_units and scale_to_virial) and of
-tupan/ics/fewbody.py:13-50 (a two-body orbit of given a, e).  The potential
+softening; then com_to_origin, to_nbody_units and scale_to_virial) and, as
+tupan/ics/fewbody.py:13-50 does, a two-body orbit of given a, e (here
+starting at pericentre).  The potential
 used by make_plummer for the velocities and the unit scalings comes from the
 GPU Phi kernel; plummer_arrays needs no GPU and imports nothing of the
 compiled library (the CPU baseline builds its workload with it).
@@ -144,7 +145,11 @@ def make_plummer(n, eps, imf=None, seed=0, device=None, prec="float64"):
 
 
 def make_binary(m1, m2, a, e, rng=None):
-    """Relative orbit at pericentre, c.o.m. at rest (fewbody.py:13-50)."""
+    """Two bodies on a Kepler orbit of semi-major axis a and eccentricity e,
+    centre of mass at rest, optionally in a random orientation.  The
+    relative orbit starts at pericentre; the reference's make_binary
+    (tupan/ics/fewbody.py:13-50) starts it at apocentre, along x with the
+    velocities along y."""
     m = m1 + m2
     rp = a * (1 - e)
     vp = np.sqrt(m * (1 + e) / rp)
