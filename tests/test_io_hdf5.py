@@ -429,6 +429,13 @@ def test_numpy_particle_sets(tmp_path):
     io.dump_worldline(empty)
     io.dump_snapshot(q, 0)
     assert _same(io.load_worldline(device="cpu"), ps) and _same(io.load_snapshot(0, device="cpu"), ps)
+    # a queued dump holds the values of the call, not later ones
+    bg = IO(str(tmp_path / "np_bg.hdf5"), "a", background=True)
+    bg._submit(lambda: __import__("time").sleep(0.2))       # keep the writer busy
+    bg.dump_snapshot(q)
+    q.rx[...] = -1.0
+    assert _same(bg.load_snapshot(device="cpu"), ps)
+    bg.close()
 
 
 def test_error_paths(tmp_path):

@@ -114,9 +114,9 @@ class _Staged(object):
         if not hasattr(ps, "_layout"):
             n = int(getattr(ps, "n", 0) or 0)
             self.cols = {}
-            for k in self.names:
+            for k in self.names:      # copies: the set may change before a queued dump runs
                 v = getattr(ps, k) if n else np.zeros(0)
-                self.cols[k] = v.detach().cpu().numpy() if isinstance(v, torch.Tensor) else np.asarray(v)
+                self.cols[k] = v.detach().cpu().numpy().copy() if isinstance(v, torch.Tensor) else np.array(v)
             return
         lay = ps._layout
         self.rnames = [k for k in self.names if lay[k][0] == "_real"]
