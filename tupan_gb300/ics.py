@@ -117,8 +117,122 @@ def triangular(n, rng):
     return out[:n]
 
 
+def _gpu_phi(mass, rx, ry, rz, eps2, device=None):
+    """phi_i = -sum_j m_j / sqrt(r_ij^2 + e2_i + e2_j) by the FP64 kernel
+    (bit-identical to the reference C backend)."""
+    from .lib import extensions
+    from .particles import ParticleSystem
+    ps = ParticleSystem.from_arrays(device=device, mass=mass, rx=rx, ry=ry, rz=rz, eps2=eps2)
+    extensions.Phi("CUDA", "float64").calc(ps, ps)
+    return ps.phi.cpu().numpy()
+
+
+def plummer_reference(n, eps, imf, seed=None, mfrac=0.999, softening_type=0, device=None, phi=None):
+    """The reference's Plummer model, value for value (tupan/ics/plummer.py:
+    22-133, 213-221): masses from the mass function `imf` (a tuple such as
+    ("equalmass",) or ("salpeter1955", 0.5, 100.0) naming an `IMF`, or any
+    object with .sample(n)), softening of `softening_type` 0-4 scaled to a
+    mean of eps^2 and halved, positions from the random state the masses
+    started from, speeds sqrt(-2 q phi) with q drawn pair by pair, then the
+    centre of mass moved to the origin, N-body units and virial
+    equilibrium, each step with the reference's numpy expressions, all
+    drawn from numpy's global random state seeded with `seed`.  The
+    potential comes from `phi(mass, rx, ry, rz, eps2)`, by default the FP64
+    Phi kernel on the GPU, which the reference computes with its C backend
+    to the same bits; so for the same seed the particle set equals the
+    reference's make_plummer.  Returns a ParticleSystem on `device`."""
+    from .particles import ParticleSystem
+    n = max(int(n), 2)
+    if isinstance(imf, (tuple, list)):
+        imf = getattr(IMF, imf[0])(*imf[1:])
+    if phi is None:
+        def phi(*a):
+            return _gpu_phi(*a, device=device)
+    np.random.seed(seed)
+    ilist = np.arange(n)
+    srand = np.random.get_state()
+    mass = np.zeros(n)
+    mass[...] = imf.sample(n)
+    mass /= float(mass.sum())
+    if softening_type == 0:
+        e2 = np.ones(n)
+    elif softening_type == 1:
+        e2 = mass ** 2
+    elif softening_type == 2:
+        e2 = mass / n
+    elif softening_type == 3:
+        e2 = (mass / n ** 2) ** (2.0 / 3)
+    elif softening_type == 4:
+        e2 = (1.0 / (mass * n ** 2)) ** 2
+    else:
+        raise ValueError("Unexpected value for softening_type: {}.".format(softening_type))
+    e2 *= (eps * eps) / np.mean(e2)
+    eps2 = e2 / 2
+    np.random.set_state(srand)
+    irand = np.random.permutation(ilist)
+    mrand = (irand + np.random.random(n)) * mfrac / n
+    radius = 1.0 / np.sqrt(np.power(mrand, -2.0 / 3.0) - 1.0)
+    theta = np.arccos(np.random.uniform(-1.0, 1.0, size=n))
+    ang = np.random.uniform(0.0, 2.0 * np.pi, size=n)
+    rx = radius * np.sin(theta) * np.cos(ang)
+    ry = radius * np.sin(theta) * np.sin(ang)
+    rz = radius * np.cos(theta)
+    pot = phi(mass, rx, ry, rz, eps2)
+    rnd = np.empty(n)
+    count = 0
+    while count < n:                     # q with density 2(1 - q), one pair at a time
+        r1 = np.random.random()
+        r2 = np.random.random()
+        if r2 < r1:
+            rnd[count] = r2
+            count += 1
+    speed = np.sqrt(-2 * rnd * pot)
+    theta = np.arccos(np.random.uniform(-1.0, 1.0, size=n))
+    ang = np.random.uniform(0.0, 2.0 * np.pi, size=n)
+    vx = speed * np.sin(theta) * np.cos(ang)
+    vy = speed * np.sin(theta) * np.sin(ang)
+    vz = speed * np.cos(theta)
+
+    def total_mass():
+        return float(mass.sum())
+
+    def potential_energy():
+        return 0.5 * float((mass * phi(mass, rx, ry, rz, eps2)).sum())
+
+    # com_to_origin (body.py:85-176)
+    mtot = total_mass()
+    com_r = np.array([mass * rx, mass * ry, mass * rz]).T.sum(0) / mtot
+    com_v = np.array([mass * vx, mass * vy, mass * vz]).T.sum(0) / mtot
+    for a, c in ((rx, -com_r[0]), (ry, -com_r[1]), (rz, -com_r[2]),
+                 (vx, -com_v[0]), (vy, -com_v[1]), (vz, -com_v[2])):
+        a += c
+    # to_nbody_units: dynrescale_total_mass(1.0), dynrescale_virial_radius(1.0) (body.py:405-461)
+    m_ratio = 1.0 / total_mass()
+    for a in (mass, rx, ry, rz):
+        a *= m_ratio
+    r_scale = 1.0 / (total_mass() ** 2 / (-2 * potential_energy()))
+    v_scale = 1 / r_scale ** 0.5
+    for a in (rx, ry, rz):
+        a *= r_scale
+    for a in (vx, vy, vz):
+        a *= v_scale
+    # scale_to_virial (body.py:444-453)
+    ke = float((0.5 * mass * (vx ** 2 + vy ** 2 + vz ** 2)).sum())
+    pe = potential_energy()
+    v_scale = ((-0.5 * pe) / ke) ** 0.5
+    for a in (vx, vy, vz):
+        a *= v_scale
+    return ParticleSystem.from_arrays(device=device, id=ilist, mass=mass, eps2=eps2, rx=rx, ry=ry, rz=rz,
+                                      vx=vx, vy=vy, vz=vz)
+
+
 def make_plummer(n, eps, imf=None, seed=0, device=None, prec="float64"):
-    """Plummer sphere in N-body (Henon) units: M = 1, E = -1/4, Q = 1/2."""
+    """Plummer sphere in N-body (Henon) units: M = 1, E = -1/4, Q = 1/2.
+    With `imf` given as the reference's tuple (("equalmass",),
+    ("salpeter1955", mlow, mhigh), ...) this is plummer_reference: the
+    reference's own model for that seed."""
+    if isinstance(imf, (tuple, list)):
+        return plummer_reference(n, eps, imf, seed=seed, device=device)
     from .lib import extensions
     from .particles import ParticleSystem
     rng = np.random.default_rng(seed)
