@@ -568,7 +568,7 @@ def test_reader_paths_the_writer_does_not_make(tmp_path):
             chunk[:len(part)] = part
             raw = chunk.tobytes() + b"\x12\x34\x56\x78"
             entries.append(((2 * k,), (f._append(raw), len(raw), 0)))
-        bt = f._write_chunk_btree(entries, 2, 28)
+        bt, _nodes = f._write_chunk_btree(entries, 2, 28)
         pipe = struct.pack("<BB", 2, 1) + struct.pack("<HHH", hdf5.FILTER_FLETCHER32, 1, 0)
         chunked = header(f, [msg(hdf5.MSG_DATASPACE, bytes([1, 1, 1, 0, 0, 0, 0, 0]) + struct.pack("<QQ", 5, hdf5.UNDEF)),
                              msg(hdf5.MSG_DATATYPE, comp, 1),
@@ -662,3 +662,23 @@ def test_worldline_selection_matches_numpy_remainder():
             b.record(ps, sign * tau)
             want = np.nonzero(np.remainder(sign * t, freq * sign * tau) == 0)[0]
             assert np.array_equal(b.wl.id.numpy(), want), (sign, freq)
+
+
+def test_appends_rewrite_only_the_index_edge(tmp_path):
+    # a worldline appended in 150 separate sessions (one per dump, as the IO
+    # layer opens the file): the chunk index keeps its full nodes and
+    # rewrites only its right edge, so the file stays within 30% of the same
+    # rows written at once (a full index rewrite per append made it 2.2
+    # times that size here)
+    p, q = str(tmp_path / "many.hdf5"), str(tmp_path / "once.hdf5")
+    rng = np.random.default_rng(1)
+    parts = [_rows(700, 700 * k, rng) for k in range(150)]
+    for r in parts:
+        with hdf5.File(p, "a") as f:
+            f.require_group("Worldline/particlesystem").append_rows("bodies", r)
+    with hdf5.File(q, "w") as f:
+        f.require_group("Worldline/particlesystem").append_rows("bodies", np.concatenate(parts))
+    assert os.path.getsize(p) < 1.3 * os.path.getsize(q)
+    _walk(p)
+    with hdf5.File(p) as f:
+        assert np.array_equal(f["Worldline/particlesystem/bodies"].read(), np.concatenate(parts))

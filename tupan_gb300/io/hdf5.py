@@ -760,8 +760,33 @@ class File(Group):
                 out.append((key, child) if ntype == 1 else child)
         return out
 
+    def _btree_walk(self, addr, ntype, ksz, levels):
+        """The leaves' (key, child) of the B-tree at addr, left to right; every
+        node visited is recorded in levels[level] (left to right) with its
+        items, right key and sibling addresses."""
+        hdr = self._read(addr, 24)
+        if hdr[:4] != b"TREE" or hdr[4] != ntype:
+            raise ValueError("no type-%d B-tree node at %d" % (ntype, addr))
+        level, n = hdr[5], struct.unpack_from("<H", hdr, 6)[0]
+        lsib, rsib = struct.unpack_from("<QQ", hdr, 8)
+        body = self._read(addr + 24, n * (ksz + 8) + ksz)
+        items = [(body[i * (ksz + 8):i * (ksz + 8) + ksz],
+                  struct.unpack_from("<Q", body, i * (ksz + 8) + ksz)[0]) for i in range(n)]
+        levels.setdefault(level, []).append({"addr": addr, "items": items, "right": body[n * (ksz + 8):],
+                                             "lsib": lsib, "rsib": rsib})
+        out = []
+        for key, child in items:
+            if level:
+                out.extend(self._btree_walk(child, ntype, ksz, levels))
+            else:
+                out.append((key, child))
+        return out
+
     # ---- dataset data
     def _read_chunk_index(self, ds):
+        """offsets -> (address, stored bytes, filter mask) of every chunk; the
+        index's nodes are kept (ds._tree) so that rewriting the index after
+        an append writes only the nodes that change."""
         if ds.layout[0] != "chunked":
             return None
         addr = ds.layout[2] if len(ds.layout) > 2 else None
@@ -769,11 +794,12 @@ class File(Group):
             return {}
         rank = len(ds.layout[1])
         ksz = 8 + 8 * (rank + 1)
-        out = {}
-        for key, child in self._btree_children(addr, 1, ksz):
+        out, levels = {}, {}
+        for key, child in self._btree_walk(addr, 1, ksz, levels):
             nbytes, mask = struct.unpack_from("<II", key, 0)
             offs = struct.unpack_from("<%dQ" % rank, key, 8)
             out[offs] = (child, nbytes, mask)
+        ds._tree = levels
         return out
 
     def _unfilter(self, ds, raw, mask):
@@ -937,7 +963,7 @@ class File(Group):
     def _write_dataset(self, ds):
         c = ds.layout[1][0]
         entries = sorted(ds._chunks.items())
-        btree = self._write_chunk_btree(entries, c, ds.dtype.itemsize)
+        btree, ds._tree = self._write_chunk_btree(entries, c, ds.dtype.itemsize, getattr(ds, "_tree", None))
         if ds.addr is not None:
             ver, rank, hasmax = ds._space_rank_max
             self._patch(ds._space_at + (8 if ver == 1 else 4), struct.pack("<Q", ds.shape[0]))
@@ -959,10 +985,14 @@ class File(Group):
         ds._new_attrs = []
         ds._dirty = False
 
-    def _write_chunk_btree(self, entries, c, itemsize):
+    def _write_chunk_btree(self, entries, c, itemsize, old=None):
         """Version-1 B-tree of the chunks (offset tuple -> (addr, bytes, mask)),
         built bottom-up with nodes of 2K entries allocated at full size; the key
-        after the last chunk is its offset plus the chunk size."""
+        after the last chunk is its offset plus the chunk size.  A node of the
+        previous index (`old`, per level) that holds the same entries is kept
+        where it is, its right key and sibling links patched in place: an
+        append rewrites only the nodes along the index's right edge.
+        Returns (root address, the index's nodes per level)."""
         ksz = 24
         cap = 2 * self.chunk_k
         node_size = 24 + cap * 8 + (cap + 1) * ksz
@@ -971,35 +1001,52 @@ class File(Group):
             return struct.pack("<IIQQ", nbytes, mask, off, 0)
 
         if not entries:
-            return UNDEF                                  # no chunk written yet: no index
-        level = [(key(nb, m, offs[0]), (key(nb, m, offs[0]), addr)) for offs, (addr, nb, m) in entries]
+            return UNDEF, None                            # no chunk written yet: no index
+        items = [(key(nb, m, offs[0]), addr) for offs, (addr, nb, m) in entries]
         last = key(0, 0, entries[-1][0][0] + c)
-        level = self._btree_level(level, last, cap, node_size, 1, 0, ksz)
-        depth = 1
-        while len(level) > 1:
-            level = self._btree_level(level, last, cap, node_size, 1, depth, ksz)
+        levels, depth = {}, 0
+        while True:
+            nodes = self._btree_nodes(items, last, cap, node_size, 1, depth, ksz, (old or {}).get(depth))
+            levels[depth] = nodes
+            if len(nodes) == 1:
+                return nodes[0]["addr"], levels
+            items = [(nd["items"][0][0], nd["addr"]) for nd in nodes]
             depth += 1
-        return level[0][1][1]
 
-    def _btree_level(self, items, last_key, cap, node_size, ntype, depth, ksz):
-        """Write one level of B-tree nodes over `items` = [(left key, (key, child addr))]
-        -> the next level's items [(left key, (left key, node addr))]."""
+    def _btree_nodes(self, items, last_key, cap, node_size, ntype, depth, ksz, old=None):
+        """One level of B-tree nodes over `items` = [(key, child address)],
+        2K to a node: a node of `old` with the same items is kept (its right
+        key and sibling links patched if they changed), the others are
+        written at the end of the file.  Returns the level's nodes."""
         groups = [items[i:i + cap] for i in range(0, len(items), cap)]
-        base = _pad8(self._eof)
-        addrs = [base + i * _pad8(node_size) for i in range(len(groups))]
+        keep = [old is not None and gi < len(old) and old[gi]["items"] == grp for gi, grp in enumerate(groups)]
+        base, k, addrs = _pad8(self._eof), 0, []
+        for gi in range(len(groups)):
+            if keep[gi]:
+                addrs.append(old[gi]["addr"])
+            else:
+                addrs.append(base + k * _pad8(node_size))
+                k += 1
         out = []
         for gi, grp in enumerate(groups):
             right = groups[gi + 1][0][0] if gi + 1 < len(groups) else last_key
-            left_sib = addrs[gi - 1] if gi else UNDEF
-            right_sib = addrs[gi + 1] if gi + 1 < len(groups) else UNDEF
-            data = b"TREE" + bytes([ntype, depth]) + struct.pack("<HQQ", len(grp), left_sib, right_sib)
-            for _lk, (k, child) in grp:
-                data += k + struct.pack("<Q", child)
-            data += right
-            data += b"\0" * (_pad8(node_size) - len(data))
-            a = self._append(data)
-            assert a == addrs[gi]
-            out.append((grp[0][0], (grp[0][0], a)))
+            lsib = addrs[gi - 1] if gi else UNDEF
+            rsib = addrs[gi + 1] if gi + 1 < len(groups) else UNDEF
+            if keep[gi]:
+                o = old[gi]
+                if o["right"] != right:
+                    self._patch(o["addr"] + 24 + len(grp) * (ksz + 8), right)
+                if o["lsib"] != lsib or o["rsib"] != rsib:
+                    self._patch(o["addr"] + 8, struct.pack("<QQ", lsib, rsib))
+            else:
+                data = b"TREE" + bytes([ntype, depth]) + struct.pack("<HQQ", len(grp), lsib, rsib)
+                for kb, child in grp:
+                    data += kb + struct.pack("<Q", child)
+                data += right
+                data += b"\0" * (_pad8(node_size) - len(data))
+                a = self._append(data)
+                assert a == addrs[gi]
+            out.append({"addr": addrs[gi], "items": grp, "right": right, "lsib": lsib, "rsib": rsib})
         return out
 
     def _write_group(self, g):
@@ -1041,18 +1088,20 @@ class File(Group):
         level = []
         prev = struct.pack("<Q", 0)
         for right, a in items:
-            level.append((prev, (prev, a)))
+            level.append((prev, a))
             prev = right
         if not level:                                    # an empty group: a root with no children
             data = b"TREE" + bytes([0, 0]) + struct.pack("<HQQ", 0, UNDEF, UNDEF) + prev
             btree = self._append(data + b"\0" * (node_size - len(data)))
         else:
-            lvl = self._btree_level(level, prev, cap, node_size, 0, 0, 8)
-            depth = 1
-            while len(lvl) > 1:
-                lvl = self._btree_level(lvl, prev, cap, node_size, 0, depth, 8)
+            depth = 0
+            while True:
+                nodes = self._btree_nodes(level, prev, cap, node_size, 0, depth, 8)
+                if len(nodes) == 1:
+                    btree = nodes[0]["addr"]
+                    break
+                level = [(nd["items"][0][0], nd["addr"]) for nd in nodes]
                 depth += 1
-            btree = lvl[0][1][1]
         g._btree, g._heap = btree, heap_addr
         stab = struct.pack("<QQ", btree, heap_addr)
         if g.addr is not None:
