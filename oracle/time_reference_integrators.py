@@ -17,7 +17,6 @@ import sys
 import tempfile
 import time
 
-import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)

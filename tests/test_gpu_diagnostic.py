@@ -7,7 +7,6 @@ kernel reproduces exactly); eerr, geerr and the drifts follow their
 definitions."""
 import math
 
-import numpy as np
 import pytest
 
 torch = pytest.importorskip("torch")

@@ -2,7 +2,6 @@
 split-FP32 Acc and AccJerk call records exactly one pairwise-kernel launch
 under its own kernel id (the bench's roofline is quoted on these events),
 and nothing is recorded with timing off."""
-import numpy as np
 import pytest
 
 torch = pytest.importorskip("torch")

@@ -16,7 +16,7 @@ torch = pytest.importorskip("torch")
 
 pytestmark = pytest.mark.gpu
 
-from test_gpu_parity import DS32_TOL, GROUPS, KCLASS, PS, rel_err, within  # noqa: E402
+from test_gpu_parity import DS32_TOL, KCLASS, PS, within  # noqa: E402
 
 N = 256
 PN = (7, 128.0)

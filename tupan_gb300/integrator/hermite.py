@@ -8,7 +8,6 @@ The predictor and corrector are the fused FP64 kernels tg_hermite_predict /
 tg_hermite_correct; the derivatives come from AccJerk (and SnapCrackle for
 orders 6 and 8, Acc for order 2).
 """
-import torch
 
 from .. import _native
 from ..lib import extensions

@@ -15,7 +15,6 @@ The state the reference keeps as class attributes of the particle type
 reductions use tg_sum (numpy's order) and r = mr / M is an IEEE division
 per element (tg_div3), so FP64 trajectories equal the reference's.
 """
-import torch
 
 from .. import _native
 from .._native import psum

@@ -5,7 +5,6 @@ flag -1 then +1 over tau/2 each (the Sakura kernel returns the increments
 dr, dv, added by tg_add_increments), half drift.  asakura takes the step
 from the Tstep kernel's sum and max criteria (sakura.py:100-117).
 """
-import torch
 
 from .. import _native
 from ..lib import extensions
