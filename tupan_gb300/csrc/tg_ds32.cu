@@ -1396,7 +1396,6 @@ __device__ __forceinline__ void ord_block(typename K::IS (&st)[K::IPT], const fl
             for (int q = 0; q < K::IPT; ++q) { K::fold_acc(st[q]); K::fold_jerk(st[q]); }
         }
     } else {
-#pragma unroll 1
         constexpr int FOLD = FORM == ORD_FAR ? K::FAR_FOLD_PAIRS : ORD_ACC_FOLD_PAIRS;
         static_assert(ORD_BLOCK_PAIRS % FOLD == 0, "folds must tile a block");
         for (int r0 = 0; r0 < ORD_BLOCK_PAIRS; r0 += FOLD) {
