@@ -415,6 +415,12 @@ def ours(args, rank, world, dist):
                          "flop_per_interaction": FLOP_ACC_JERK,
                          "peak_source": "measured: tg_probe_fma_tflops (FFMA2 chains, this GPU)",
                          "peak_fp64_tflops": peak64,
+                         # the FP32 issue-rate view of the same kernel: pipe
+                         # utilisation from its ncu capture (a profile of
+                         # this kernel and workload, not of this run)
+                         "issue_rate_ncu": {"sm__pipe_fma_cycles_active": 0.782,
+                                            "sm__pipe_xu_cycles_active": 0.247,
+                                            "source": "profiles/ds32_ord_acc_jerk_n65536.txt"},
                          "acc_frac": (FLOP_ACC * n * n / (kacc_ms * 1e-3) / 1e12) / peak32 if peak32 > 0 else None},
             "clocks": clk, "wall_s": wall}
 
